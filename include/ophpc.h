@@ -1,0 +1,145 @@
+/*
+ * ophpc — GB300-native point-cloud hologram generation (C ABI).
+ *
+ * Drop-in for Openholo's point-cloud path:
+ *   ophPointCloud::generateHologram(PC_DIFF_RS | PC_DIFF_FRESNEL)
+ *     (ophgen/src/ophPointCloud.cpp:151-191 -> genCghPointCloudGPU,
+ *      ophgen/src/ophPointCloud_GPU.cpp:179-413)
+ *   ophGen::encoding(ENCODE_PHASE | ENCODE_AMPLITUDE) + ophGen::normalize()
+ *     (ophgen/src/ophGen.cpp:816-849, 654-687)
+ *
+ * Conventions (all entry points):
+ *   - every call returns an ophpc_status and never exits the process
+ *     (the reference's HANDLE_ERROR calls exit(): ophPointCloud_GPU.h:71-81);
+ *   - plain pointers and sizes only; `stream` is a cudaStream_t passed as
+ *     void* (NULL = the legacy default stream);
+ *   - device-pointer entry points are asynchronous on `stream`; host-pointer
+ *     entry points are synchronous;
+ *   - a context may be used from several host threads; calls on one context
+ *     are serialised by its lock. Device work of calls on different streams
+ *     may overlap: each call allocates its own stream-ordered scratch.
+ *   - one GPU per context, chosen at creation.
+ */
+#ifndef OPHPC_H
+#define OPHPC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OPHPC_API_VERSION 1
+#define OPHPC_MAX_CHANNELS 3
+
+typedef enum ophpc_status {
+    OPHPC_SUCCESS = 0,
+    OPHPC_ERROR_INVALID_ARGUMENT = 1,
+    OPHPC_ERROR_CUDA = 2,
+    OPHPC_ERROR_OUT_OF_MEMORY = 3,
+    OPHPC_ERROR_IO = 4,
+    OPHPC_ERROR_CONFIG = 5,
+    OPHPC_ERROR_UNSUPPORTED = 6,
+    OPHPC_ERROR_QUEUE_FULL = 7,
+    OPHPC_ERROR_TIMEOUT = 8,
+    OPHPC_ERROR_NOT_READY = 9,
+    OPHPC_ERROR_NO_DEVICE = 10
+} ophpc_status;
+
+/* PC_DIFF_FLAG values (ophgen/src/ophPointCloud.h:550-553). */
+#define OPHPC_DIFF_RS 0u
+#define OPHPC_DIFF_FRESNEL 1u
+
+/* Mode bits, bit-compatible with Openholo/src/define.h:155-159. */
+#define OPHPC_MODE_CPU 0u
+#define OPHPC_MODE_GPU 1u
+#define OPHPC_MODE_DOUBLE 0u
+#define OPHPC_MODE_FLOAT 2u
+#define OPHPC_MODE_FASTMATH 4u
+/* GB300 additions (no reference counterpart): Fresnel as a separable complex
+ * contraction on the tcgen05 tensor cores, FP16 operands or split-BF16
+ * (hi/lo, three products), FP32 accumulation. Ignored for RS. */
+#define OPHPC_MODE_TENSOR_FP16 0x100u
+#define OPHPC_MODE_TENSOR_BF16X3 0x200u
+
+/* ophGen::ENCODE_FLAG values (ophgen/src/ophGen.h:84-95) handled on device. */
+#define OPHPC_ENCODE_PHASE 0u
+#define OPHPC_ENCODE_AMPLITUDE 1u
+#define OPHPC_ENCODE_REAL 2u
+#define OPHPC_ENCODE_IMAGINARY 3u
+
+/* Vertex (Openholo/src/struct.h:86-106): packed pos[3], color[3], phase —
+ * 56 bytes, colour channels in [0, 1]; color[ch] is channel ch's amplitude. */
+typedef struct ophpc_vertex {
+    double pos[3];
+    double color[3];
+    double phase;
+} ophpc_vertex;
+
+/* The OphConfig (Openholo/src/Openholo.h:96-120) and OphPointCloudConfig
+ * (ophgen/src/ophGen.h:546-567) fields the path reads. */
+typedef struct ophpc_config {
+    int32_t pixel_number[2];   /* SLM_PixelNumX/Y */
+    int32_t offset[2];         /* context_.offset (setOffset) */
+    double pixel_pitch[2];     /* SLM_PixelPitchX/Y, metres */
+    double scale[3];           /* ScaleX/Y/Z */
+    double distance;           /* Distance, metres, added to scaled z */
+    double field_length;       /* FieldLength, used when viewing_window != 0 */
+    int32_t viewing_window;    /* setViewingWindow(true): transVW before scaling */
+    uint32_t n_channels;       /* SLM_WaveNum, 1..OPHPC_MAX_CHANNELS */
+    double wave_length[OPHPC_MAX_CHANNELS]; /* SLM_WaveLength_i, metres */
+} ophpc_config;
+
+typedef struct ophpc_context ophpc_context;
+
+/* Version of this header's ABI. */
+int32_t ophpc_api_version(void);
+
+/* Human-readable text of a status code (static storage). */
+const char* ophpc_status_string(ophpc_status status);
+
+/* Detail of the last failure on this context (valid until the next call). */
+const char* ophpc_last_error(const ophpc_context* ctx);
+
+/* Creates a context on CUDA device `device`. Replaces cudaWrapper's
+ * singleton device query (ophgen/src/cudaWrapper.cpp:50-177), which divides
+ * by zero on sm_10x. */
+ophpc_status ophpc_create(int32_t device, ophpc_context** out);
+ophpc_status ophpc_destroy(ophpc_context* ctx);
+
+/* Device path of generateHologram: d_vertices holds n_points ophpc_vertex
+ * records in device memory; d_field receives the complex field of every
+ * channel as interleaved doubles [n_channels][pnY][pnX][re, im] (the
+ * layout of complex_H, Openholo/src/Openholo.h:490), overwritten. mode takes
+ * the OPHPC_MODE_* bits; the kernels always run on the GPU. Asynchronous on
+ * `stream`. Replaces genCghPointCloudGPU's single-GPU branch
+ * (ophgen/src/ophPointCloud_GPU.cpp:218-286) and the launchers
+ * cudaPointCloud_RS / cudaPointCloud_Fresnel (ophgen/src/ophPCKernel.cu:893-933). */
+ophpc_status ophpc_generate(ophpc_context* ctx, const ophpc_config* cfg,
+                            const ophpc_vertex* d_vertices, uint64_t n_points,
+                            uint32_t diff_flag, uint32_t mode, double* d_field, void* stream);
+
+/* Host path, what genCghPointCloudGPU does end to end: host vertices in,
+ * one host buffer of pnX*pnY Complex<double> per channel out (complex_H[ch]).
+ * Synchronous. seconds_out (optional) receives the elapsed wall time, as
+ * generateHologram returns it (ophgen/src/ophPointCloud.cpp:187-190). */
+ophpc_status ophpc_generate_host(ophpc_context* ctx, const ophpc_config* cfg,
+                                 const ophpc_vertex* h_vertices, uint64_t n_points,
+                                 uint32_t diff_flag, uint32_t mode,
+                                 double* const* h_field_per_channel, double* seconds_out);
+
+/* Device encoding + normalisation (ophGen::encoding + ophGen::normalize):
+ * d_field: [n_channels][n_pixels][re, im] doubles. d_encoded (optional,
+ * NULL to skip): [n_channels][n_pixels] doubles = m_lpEncoded.
+ * d_normalized (optional): [n_channels][n_pixels] bytes = m_lpNormalized,
+ * using the min/max over all channels. Asynchronous on `stream`. */
+ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_channels,
+                          uint64_t n_pixels, uint32_t encode_flag, double* d_encoded,
+                          uint8_t* d_normalized, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* OPHPC_H */

@@ -1,0 +1,97 @@
+"""openholo_gb300 — GB300-native point-cloud hologram generation.
+
+Python view of the C ABI in ``include/ophpc.h`` (``lib/libophpc.so``, built
+by ``_build.py``). The hot path is entirely in the CUDA library; this module
+only binds it with ctypes. There is no CPU fallback: importing works without
+a GPU (for the host-side tests), but every compute call goes to the library
+and fails loudly when it or the GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence
+
+from ._abi import (  # noqa: F401
+    DIFF_FRESNEL, DIFF_RS, ENCODE_AMPLITUDE, ENCODE_IMAGINARY, ENCODE_PHASE, ENCODE_REAL, MODE_CPU,
+    MODE_DOUBLE, MODE_FASTMATH, MODE_FLOAT, MODE_GPU, MODE_TENSOR_BF16X3, MODE_TENSOR_FP16, OphpcConfig,
+    OphpcError, STATUS, lib, lib_path, make_config,
+)
+
+__all__ = [
+    "Context", "OphpcConfig", "OphpcError", "make_config", "lib", "lib_path",
+    "DIFF_RS", "DIFF_FRESNEL", "MODE_CPU", "MODE_GPU", "MODE_DOUBLE", "MODE_FLOAT", "MODE_FASTMATH",
+    "MODE_TENSOR_FP16", "MODE_TENSOR_BF16X3", "ENCODE_PHASE", "ENCODE_AMPLITUDE", "ENCODE_REAL",
+    "ENCODE_IMAGINARY",
+]
+
+
+class Context:
+    """One ophpc_context (one GPU). Thin wrapper; pointers are ints."""
+
+    def __init__(self, device: int = 0):
+        self._lib = lib()
+        self._h = ctypes.c_void_p()
+        st = self._lib.ophpc_create(int(device), ctypes.byref(self._h))
+        if st != 0:
+            raise OphpcError(st, "ophpc_create failed")
+        self.device = device
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.ophpc_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def _check(self, st: int, what: str) -> None:
+        if st != 0:
+            detail = self._lib.ophpc_last_error(self._h)
+            raise OphpcError(st, f"{what}: {detail.decode() if detail else ''}")
+
+    def generate(self, cfg: OphpcConfig, d_vertices: int, n_points: int, diff_flag: int, mode: int,
+                 d_field: int, stream: int = 0) -> None:
+        st = self._lib.ophpc_generate(self._h, ctypes.byref(cfg), ctypes.c_void_p(d_vertices),
+                                      ctypes.c_uint64(n_points), diff_flag, mode, ctypes.c_void_p(d_field),
+                                      ctypes.c_void_p(stream))
+        self._check(st, "ophpc_generate")
+
+    def generate_host(self, cfg: OphpcConfig, h_vertices: int, n_points: int, diff_flag: int, mode: int,
+                      h_fields: Sequence[int]) -> float:
+        arr = (ctypes.c_void_p * len(h_fields))(*h_fields)
+        secs = ctypes.c_double()
+        st = self._lib.ophpc_generate_host(self._h, ctypes.byref(cfg), ctypes.c_void_p(h_vertices),
+                                           ctypes.c_uint64(n_points), diff_flag, mode, arr, ctypes.byref(secs))
+        self._check(st, "ophpc_generate_host")
+        return secs.value
+
+    def encode(self, d_field: int, n_channels: int, n_pixels: int, encode_flag: int,
+               d_encoded: Optional[int], d_normalized: Optional[int], stream: int = 0) -> None:
+        st = self._lib.ophpc_encode(self._h, ctypes.c_void_p(d_field), n_channels, ctypes.c_uint64(n_pixels),
+                                    encode_flag, ctypes.c_void_p(d_encoded or 0), ctypes.c_void_p(d_normalized or 0),
+                                    ctypes.c_void_p(stream))
+        self._check(st, "ophpc_encode")
+
+
+def build(force: bool = False) -> str:
+    """Compile libophpc.so in-tree (nvcc, sm_103a)."""
+    from . import _build
+    return _build.build(force=force)
+
+
+def library_loaded_path() -> str:
+    return os.path.realpath(lib_path())

@@ -1,0 +1,90 @@
+// Shared definitions of the point-cloud hologram kernels (sm_103a).
+//
+// Data layout in HBM for one generate call:
+//   vertices  : caller's ophpc_vertex[n] (56 B packed AoS, read once by prep)
+//   PointRec  : [n_channels][n_points] 64-byte records written by prep_points
+//               (FP64 scaled position, amplitude coefficient, window rectangle)
+//   field     : [n_channels][pnY][pnX] double2 (re, im), the complex_H layout
+//   partials  : [ksplit-1][n_channels][pnY][pnX] double2, only when the point
+//               range is split across CTAs to fill the GPU on small fields
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace ophpc {
+
+// Pixel tile of one CTA and the per-thread pixel block.
+constexpr int kTileW = 64;          // pixels along x per CTA
+constexpr int kTileH = 32;          // pixels along y per CTA
+constexpr int kThreads = 128;       // 16 x 8 threads
+constexpr int kPixW = 4;            // columns per thread (adjacent)
+constexpr int kPixH = 4;            // rows per thread (adjacent)
+constexpr int kThreadsX = kTileW / kPixW;   // 16
+constexpr int kChunk = 256;         // points staged per shared-memory round
+
+static_assert(kThreadsX * (kTileH / kPixH) == kThreads, "tile / thread layout mismatch");
+
+// Per (channel, point) record produced by prep_points.
+struct __align__(16) PointRec {
+    double x, y, z;     // scaled (and viewing-window transformed) position; z includes Distance
+    double coef;        // RS: amp*z/lambda   Fresnel: amp/(lambda*z)
+    int32_t x_lo, x_hi; // window rectangle, pixel columns [x_lo, x_hi), clipped to [0, pnX]
+    int32_t y_lo, y_hi; // pixel rows [y_lo, y_hi), clipped to [0, pnY]
+    double aux;         // Fresnel: 1/(2*z*lambda); RS: z*z
+    double pad;
+};
+static_assert(sizeof(PointRec) == 64, "PointRec must stay 64 bytes");
+
+// Geometry of one channel, passed by value.
+struct ChannelGeom {
+    int32_t pnX, pnY, offX, offY;
+    double ppX, ppY;
+    double x0, y0;          // -ssX/2, -ssY/2 with ss = pn*pp (ophGen.cpp:368-379)
+    double lambda, inv_lambda;
+    double detx, dety;      // RS window slopes tx/sqrt(1-tx^2), tx = lambda/(2pp)
+};
+
+struct JobGeom {
+    ChannelGeom ch[3];
+    int32_t n_channels;
+    int32_t tiles_x, tiles_y;
+    int32_t ksplit;         // point-range splits per tile
+    int64_t n_points;
+    int64_t points_per_split;
+};
+
+// Pixel-centre coordinates, exactly as the reference forms them
+// (ophGen.cpp:413,422; ophPCKernel.cu:97-98): explicit roundings, no FMA.
+__device__ __forceinline__ double pixel_x(const ChannelGeom& g, int xi) {
+    return __dadd_rn(g.x0, __dmul_rn((double)(xi - 1 + g.offX), g.ppX));
+}
+__device__ __forceinline__ double pixel_y(const ChannelGeom& g, int yi) {
+    return __dadd_rn(g.y0, __dmul_rn((double)(g.pnY - yi + g.offY), g.ppY));
+}
+
+// Reduce a phase in turns to [-0.5, 0.5]: t - rint(t) with the 1.5*2^23
+// round-to-nearest constant, kept on the FP32 add pipe.
+__device__ __forceinline__ float reduce_turns(float t) {
+    const float kMagic = 12582912.0f;
+    float r = __fsub_rn(__fadd_rn(t, kMagic), kMagic);
+    return __fsub_rn(t, r);
+}
+
+// Launchers (defined in the .cu files).
+void launch_prep(const void* d_vertices, int64_t n_points, const double* scale, double distance,
+                 double field_length, int viewing_window, int diff_flag, const JobGeom& jg,
+                 PointRec* d_recs, cudaStream_t stream);
+void launch_rs(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
+               cudaStream_t stream);
+void launch_fresnel(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
+                    cudaStream_t stream);
+void launch_sum_partials(const JobGeom& jg, double2* d_field, const double2* d_partials,
+                         cudaStream_t stream);
+void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int encode_flag,
+                   double* d_encoded, uint8_t* d_normalized, unsigned long long* d_minmax,
+                   cudaStream_t stream);
+int rs_blocks_per_sm();
+int fresnel_blocks_per_sm();
+
+}  // namespace ophpc

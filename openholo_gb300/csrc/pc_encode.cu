@@ -1,0 +1,132 @@
+// Device encoding and 8-bit normalisation.
+//
+// ophGen::encoding (ophgen/src/ophGen.cpp:816-849) maps every complex pixel
+// to a real value; ophGen::normalize (ophgen/src/ophGen.cpp:654-687) then
+// takes the min and max over ALL channels (minOfArr/maxOfArr,
+// Openholo/src/function.h:79-99: min starts at MAX_DOUBLE, max at
+// MIN_DOUBLE = 2.2250738585072014e-308, strict comparisons, so NaNs never
+// win) and writes (uchar)(((v - min) / gap) * 255 + 0.5).
+//
+// Two launches, both grid-stride over [n_channels * n_pixels]:
+//   encode_minmax : value per pixel (FP64, optional store) + block min/max,
+//                   folded into two 64-bit words with atomicMin/atomicMax on
+//                   an order-preserving integer image of the doubles;
+//   normalize     : re-derives (or re-reads) the value and writes the byte.
+// The encoded value is recomputed in the second pass when it is not stored,
+// so the field is read twice but no FP64 intermediate is written.
+// All FP64 arithmetic uses explicit _rn operations (no FMA) to round exactly
+// as the x86-64 reference does.
+#include "pc_common.cuh"
+
+#include <cfloat>
+
+namespace ophpc {
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kMaxDouble = 1.7976931348623158e+308;
+constexpr double kMinDouble = 2.2250738585072014e-308;
+
+__device__ __forceinline__ double encode_value(double2 h, int flag) {
+    switch (flag) {
+        case 0: {  // Phase: (atan2(im, re) + pi) / (2 pi)   (ophGen.cpp:1843-1853)
+            const double pi2 = kPi * 2;
+            return __ddiv_rn(__dadd_rn(atan2(h.y, h.x), kPi), pi2);
+        }
+        case 1:    // Amplitude: sqrt(re^2 + im^2)            (ophGen.cpp:1855-1864)
+            return sqrt(__dadd_rn(__dmul_rn(h.x, h.x), __dmul_rn(h.y, h.y)));
+        case 2:    // RealPart                                 (ophGen.cpp:1821-1830)
+            return h.x;
+        default:   // ImaginaryPart                            (ophGen.cpp:1832-1841)
+            return h.y;
+    }
+}
+
+// Order-preserving map double -> uint64 (for non-NaN values).
+__device__ __forceinline__ unsigned long long ordered_bits(double d) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(256) encode_minmax_kernel(const double2* __restrict__ field, int64_t n,
+                                                            int flag, double* __restrict__ encoded,
+                                                            unsigned long long* __restrict__ minmax) {
+    double mn = kMaxDouble, mx = kMinDouble;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double e = encode_value(field[i], flag);
+        if (encoded) encoded[i] = e;
+        if (e < mn) mn = e;
+        if (e > mx) mx = e;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    __shared__ double s_mn[8], s_mx[8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_mn[w] = mn;
+        s_mx[w] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            mn = fmin(mn, s_mn[k]);
+            mx = fmax(mx, s_mx[k]);
+        }
+        atomicMin(&minmax[0], ordered_bits(mn));
+        atomicMax(&minmax[1], ordered_bits(mx));
+    }
+}
+
+__device__ __forceinline__ double from_ordered(unsigned long long b) {
+    b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
+    return __longlong_as_double((long long)b);
+}
+
+__global__ void __launch_bounds__(256) normalize_kernel(const double2* __restrict__ field,
+                                                        const double* __restrict__ encoded, int64_t n,
+                                                        int flag, const unsigned long long* __restrict__ minmax,
+                                                        uint8_t* __restrict__ out) {
+    const double mn = from_ordered(minmax[0]);
+    const double mx = from_ordered(minmax[1]);
+    const double gap = __dsub_rn(mx, mn);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double e = encoded ? encoded[i] : encode_value(field[i], flag);
+        const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(e, mn), gap), 255.0), 0.5);
+        // double -> uchar truncation; NaN (gap == 0) and out-of-range map to 0
+        out[i] = (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
+    }
+}
+
+__global__ void init_minmax_kernel(unsigned long long* minmax) {
+    // initial values MAX_DOUBLE / MIN_DOUBLE of minOfArr / maxOfArr
+    minmax[0] = ordered_bits(kMaxDouble);
+    minmax[1] = ordered_bits(kMinDouble);
+}
+
+}  // namespace
+
+void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int encode_flag,
+                   double* d_encoded, uint8_t* d_normalized, unsigned long long* d_minmax,
+                   cudaStream_t stream) {
+    const int64_t n = (int64_t)n_channels * n_pixels;
+    if (n <= 0) return;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int threads = 256;
+    int64_t want = (n + threads - 1) / threads;
+    const int blocks = (int)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
+    init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
+    encode_minmax_kernel<<<blocks, threads, 0, stream>>>(d_field, n, encode_flag, d_encoded, d_minmax);
+    if (d_normalized)
+        normalize_kernel<<<blocks, threads, 0, stream>>>(d_field, d_encoded, n, encode_flag, d_minmax,
+                                                         d_normalized);
+}
+
+}  // namespace ophpc

@@ -1,0 +1,234 @@
+// Fresnel point-cloud kernel on the FP32 cores (sm_103a).
+//
+// Computes the reference's sum (ophgen/src/ophGen.cpp:447-514; GPU
+// counterpart ophgen/src/ophPCKernel.cu:516-601)
+//   H(p) = sum_j  a_j / (lambda z_j) * (sin phi, -cos phi),
+//   phi/2pi = ((X-x)^2 + (Y-y)^2 + 2 z^2) / (2 z lambda),
+// over the points whose window rectangle contains p. The Fresnel window is a
+// rectangle (no per-pixel cone test), so the term factorises over columns and
+// rows: with the tile centre (Xc, Yc), dx = dxc + u, dy = dyc + v,
+//   phi/2pi = tau_c + s(2 dxc u + u^2) + s(2 dyc v + v^2),  s = 1/(2 z lambda).
+// tau_c is evaluated in FP64 per (point, tile) and reduced mod 1 (the one FP64
+// step); each thread then forms one complex factor per column and per row of
+// its 4x4 pixel block (8 sin/cos pairs) and accumulates their products: a
+// complex rank-1 update per point, four FMAs per pixel. The rectangle is
+// applied as 0/1 masks on the factors. Sums run in FP32 per chunk of 256
+// points and fold into FP64 shared-memory sums; every pixel is stored once.
+#include "pc_common.cuh"
+
+namespace ophpc {
+
+namespace {
+
+struct __align__(16) FrSRec {
+    float P, Q, s, fc;       // 2 dxc s, 2 dyc s, s, frac(tau_c)
+    float ac;                // amp / (lambda z)
+    int32_t xl, xh;          // window columns relative to the tile origin
+    int32_t yl, yh;          // window rows relative to the tile origin
+    int32_t pad[3];
+};
+static_assert(sizeof(FrSRec) == 48, "FrSRec size");
+
+constexpr float kTwoPi = 6.283185307179586f;
+
+__device__ __forceinline__ int warp_prefix(unsigned ballot) {
+    return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
+}
+
+__global__ void __launch_bounds__(kThreads, 4)
+fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restrict__ field,
+               double2* __restrict__ partials) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    FrSRec* s_rec = reinterpret_cast<FrSRec*>(s_raw);
+    // FP64 running sums, [pixel][thread]: consecutive threads hit consecutive 16-byte words
+    double2* s_acc = reinterpret_cast<double2*>(s_raw + sizeof(FrSRec) * kChunk);
+    __shared__ int s_cnt[2][kThreads / 32];
+
+    const int ch = blockIdx.z / jg.ksplit;
+    const int part = blockIdx.z % jg.ksplit;
+    const ChannelGeom& g = jg.ch[ch];
+    const int X0 = blockIdx.x * kTileW, Y0 = blockIdx.y * kTileH;
+    const int vx1 = min(X0 + kTileW, g.pnX), vy1 = min(Y0 + kTileH, g.pnY);
+    const double Xc = pixel_x(g, X0 + kTileW / 2), Yc = pixel_y(g, Y0 + kTileH / 2);
+
+    const int tx = threadIdx.x % kThreadsX, ty = threadIdx.x / kThreadsX;
+    const int warp = threadIdx.x >> 5;
+    float u[kPixW], uu[kPixW], v[kPixH], vv[kPixH];
+#pragma unroll
+    for (int c = 0; c < kPixW; ++c) {
+        u[c] = (float)((double)(tx * kPixW + c - kTileW / 2) * g.ppX);
+        uu[c] = u[c] * u[c];
+    }
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) {
+        v[r] = (float)((double)(kTileH / 2 - (ty * kPixH + r)) * g.ppY);
+        vv[r] = v[r] * v[r];
+    }
+
+#pragma unroll
+    for (int k = 0; k < kPixH * kPixW; ++k) s_acc[k * kThreads + threadIdx.x] = make_double2(0.0, 0.0);
+
+    const int64_t n = jg.n_points;
+    const int64_t p_beg = (int64_t)part * jg.points_per_split;
+    const int64_t p_end = min(n, p_beg + jg.points_per_split);
+    const PointRec* chrec = recs + (int64_t)ch * n;
+
+    for (int64_t cb = p_beg; cb < p_end; cb += kChunk) {
+        bool keep[2];
+        FrSRec tmp[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            keep[q] = false;
+            const int64_t idx = cb + threadIdx.x + q * kThreads;
+            if (idx < p_end) {
+                const PointRec p = chrec[idx];
+                const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
+                const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
+                if (ix0 < ix1 && iy0 < iy1) {
+                    keep[q] = true;
+                    const double dxc = Xc - p.x, dyc = Yc - p.y;
+                    const double s = p.aux;   // 1 / (2 z lambda)
+                    const double tc = (dxc * dxc + dyc * dyc + 2.0 * p.z * p.z) * s;
+                    FrSRec& t = tmp[q];
+                    t.P = (float)(2.0 * dxc * s);
+                    t.Q = (float)(2.0 * dyc * s);
+                    t.s = (float)s;
+                    t.fc = (float)(tc - rint(tc));
+                    t.ac = (float)p.coef;
+                    t.xl = p.x_lo - X0;
+                    t.xh = p.x_hi - X0;
+                    t.yl = p.y_lo - Y0;
+                    t.yh = p.y_hi - Y0;
+                }
+            }
+        }
+        unsigned bk[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            bk[q] = __ballot_sync(0xffffffffu, keep[q]);
+            if ((threadIdx.x & 31) == 0) s_cnt[q][warp] = __popc(bk[q]);
+        }
+        __syncthreads();
+        int n_keep = 0, off[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+#pragma unroll
+            for (int w = 0; w < kThreads / 32; ++w) {
+                if (w == warp) off[q] = n_keep;
+                n_keep += s_cnt[q][w];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+            if (keep[q]) s_rec[off[q] + warp_prefix(bk[q])] = tmp[q];
+        __syncthreads();
+
+        float sr[kPixH * kPixW], si[kPixH * kPixW];
+#pragma unroll
+        for (int k = 0; k < kPixH * kPixW; ++k) sr[k] = si[k] = 0.f;
+#pragma unroll 1
+        for (int j = 0; j < n_keep; ++j) {
+            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);
+            const float ac = s_rec[j].ac;
+            const int4 wb = *reinterpret_cast<const int4*>(&s_rec[j].xl);
+            float exr[kPixW], exi[kPixW], eyr[kPixH], eyi[kPixH];
+#pragma unroll
+            for (int c = 0; c < kPixW; ++c) {
+                const int cl = tx * kPixW + c;
+                float t = fmaf(a.x, u[c], a.z * uu[c]) + a.w;
+                t = reduce_turns(t);
+                float s, co;
+                __sincosf(t * kTwoPi, &s, &co);
+                const float m = (cl >= wb.x && cl < wb.y) ? ac : 0.f;
+                exr[c] = m * co;
+                exi[c] = m * s;
+            }
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) {
+                const int rl = ty * kPixH + r;
+                float t = fmaf(a.y, v[r], a.z * vv[r]);
+                t = reduce_turns(t);
+                float s, co;
+                __sincosf(t * kTwoPi, &s, &co);
+                const bool m = rl >= wb.z && rl < wb.w;
+                eyr[r] = m ? co : 0.f;
+                eyi[r] = m ? s : 0.f;
+            }
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) {
+#pragma unroll
+                for (int c = 0; c < kPixW; ++c) {
+                    const int k = r * kPixW + c;
+                    sr[k] = fmaf(exr[c], eyr[r], fmaf(-exi[c], eyi[r], sr[k]));
+                    si[k] = fmaf(exr[c], eyi[r], fmaf(exi[c], eyr[r], si[k]));
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPixH * kPixW; ++k) {
+            double2 a = s_acc[k * kThreads + threadIdx.x];
+            a.x += (double)sr[k];
+            a.y += (double)si[k];
+            s_acc[k * kThreads + threadIdx.x] = a;
+        }
+        __syncthreads();
+    }
+
+    // H = -i * S: the reference's (sin phi, -cos phi) = (Im e^{i phi}, -Re e^{i phi})
+    double2* dst = (part == 0) ? field
+                               : partials + (int64_t)(part - 1) * jg.n_channels * g.pnX * (int64_t)g.pnY;
+    dst += (int64_t)ch * g.pnX * (int64_t)g.pnY;
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) {
+        const int row = Y0 + ty * kPixH + r;
+        if (row >= g.pnY) continue;
+#pragma unroll
+        for (int c = 0; c < kPixW; ++c) {
+            const int col = X0 + tx * kPixW + c;
+            if (col >= g.pnX) continue;
+            const double2 a = s_acc[(r * kPixW + c) * kThreads + threadIdx.x];
+            dst[(int64_t)row * g.pnX + col] = make_double2(a.y, -a.x);
+        }
+    }
+}
+
+__global__ void sum_partials_kernel(double2* __restrict__ field, const double2* __restrict__ partials,
+                                    int64_t n, int nparts) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double2 a = field[i];
+    for (int p = 0; p < nparts; ++p) {
+        const double2 b = partials[(int64_t)p * n + i];
+        a.x += b.x;
+        a.y += b.y;
+    }
+    field[i] = a;
+}
+
+}  // namespace
+
+constexpr size_t kFresnelSmem = sizeof(FrSRec) * kChunk + sizeof(double2) * kPixH * kPixW * kThreads;
+
+int fresnel_blocks_per_sm() {
+    cudaFuncSetAttribute(fresnel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFresnelSmem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fresnel_kernel, kThreads, kFresnelSmem) != cudaSuccess) nb = 1;
+    return nb > 0 ? nb : 1;
+}
+
+void launch_fresnel(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
+                    cudaStream_t stream) {
+    dim3 grid((unsigned)jg.tiles_x, (unsigned)jg.tiles_y, (unsigned)(jg.n_channels * jg.ksplit));
+    fresnel_kernel<<<grid, kThreads, kFresnelSmem, stream>>>(d_recs, jg, d_field, d_partials);
+}
+
+void launch_sum_partials(const JobGeom& jg, double2* d_field, const double2* d_partials,
+                         cudaStream_t stream) {
+    if (jg.ksplit <= 1) return;
+    const int64_t n = (int64_t)jg.n_channels * jg.ch[0].pnX * (int64_t)jg.ch[0].pnY;
+    const int threads = 256;
+    sum_partials_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(
+        d_field, d_partials, n, jg.ksplit - 1);
+}
+
+}  // namespace ophpc

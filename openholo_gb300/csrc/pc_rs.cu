@@ -1,0 +1,332 @@
+// Rayleigh-Sommerfeld point-cloud kernel (sm_103a, FP32 core with FP64 phase
+// reduction).
+//
+// Computes, for every pixel p of every channel, the reference's sum
+//   H(p) = sum_j  a_j z_j / (lambda r_pj^2) * (sin(k r_pj), -cos(k r_pj))
+// over the points whose anti-aliasing window contains p
+// (ophgen/src/ophGen.cpp:361-445; GPU counterpart ophgen/src/ophPCKernel.cu:66-176).
+//
+// Work decomposition: one CTA owns a 64x32 pixel tile (4x4 adjacent pixels
+// per thread) of one channel and streams the point list through shared
+// memory in chunks of 256. Per (point, tile) the CTA evaluates in FP64 the
+// distance r_c from the point to the tile centre and keeps only
+// frac(r_c/lambda) — the only FP64 step; k*r reaches ~6e6 rad. Per pixel the
+// remaining phase is carried in FP32 through the compensated form
+//   r_p - r_c = r_c (sqrt(1+w) - 1),  w = (r_p^2 - r_c^2) / r_c^2,
+// where r_p^2 - r_c^2 = 2 dx_c u + u^2 + 2 dy_c v + v^2 is formed from small
+// tile-local offsets (u, v) and splits into a per-column plus a per-row part.
+// In the FAST class (tile inside the window, |w| small) the series
+// w/2 - w^2/8 replaces sqrt and division, so a pixel costs ~11 FP32 ops and
+// two MUFU (sin, cos). Tiles the window cuts, or with large |w|, go to the
+// EXACT class: integer rectangle test, the reference's cone test (FP32 with
+// a margin, FP64 replica of ophGen.cpp:415-428 when inside the margin) and
+// the exact r_p. Sums run in FP32 per chunk and are folded into FP64
+// shared-memory sums after every chunk; every pixel is stored once.
+#include "pc_common.cuh"
+
+namespace ophpc {
+
+namespace {
+
+struct __align__(16) RsSRec {
+    float P, Q, h, g;        // FAST: 2dxc/rc2, 2dyc/rc2, 1/rc2, rc/lambda. EXACT: 2dxc, 2dyc, rc2, rc
+    float fc, ac, dxc, dyc;  // frac(rc/lambda) in [-.5,.5]; FAST: coef/rc2, EXACT: coef
+    float zz, mabs;          // EXACT: z^2, absolute margin of the FP32 cone test
+    int32_t idx;             // EXACT: point index (FP64 fallback)
+    int32_t xl, xh, yl, yh;  // EXACT: window rectangle relative to the tile origin
+    int32_t pad;
+};
+static_assert(sizeof(RsSRec) == 64, "RsSRec size");
+
+constexpr float kTwoPi = 6.283185307179586f;
+// FAST requires (rc/lambda) * |w|^3 / 16 below this many turns (series error)
+// and |w| below kMaxW (the dropped amplitude term is w^2).
+constexpr double kSeriesTol = 2e-8;
+constexpr double kMaxW = 1e-3;
+
+__device__ __forceinline__ int warp_prefix(unsigned ballot) {
+    return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
+}
+
+__global__ void __launch_bounds__(kThreads, 4)
+rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restrict__ field,
+          double2* __restrict__ partials) {
+    extern __shared__ __align__(16) unsigned char s_raw[];
+    RsSRec* s_rec = reinterpret_cast<RsSRec*>(s_raw);
+    // FP64 running sums, [pixel][thread]: consecutive threads hit consecutive 16-byte words
+    double2* s_acc = reinterpret_cast<double2*>(s_raw + sizeof(RsSRec) * kChunk);
+    __shared__ int s_cnt[2][2][kThreads / 32];   // [fast|exact][q][warp]
+
+    const int ch = blockIdx.z / jg.ksplit;
+    const int part = blockIdx.z % jg.ksplit;
+    const ChannelGeom& g = jg.ch[ch];
+    const int X0 = blockIdx.x * kTileW, Y0 = blockIdx.y * kTileH;
+    const int vx1 = min(X0 + kTileW, g.pnX), vy1 = min(Y0 + kTileH, g.pnY);
+    const int xc = X0 + kTileW / 2, yc = Y0 + kTileH / 2;
+    const double Xc = pixel_x(g, xc), Yc = pixel_y(g, yc);
+    // valid-pixel coordinate ranges of this tile (X grows with the column,
+    // Y falls with the row)
+    const double Xmin = pixel_x(g, X0), Xmax = pixel_x(g, vx1 - 1);
+    const double Ymax = pixel_y(g, Y0), Ymin = pixel_y(g, vy1 - 1);
+    const double umax = (kTileW / 2) * g.ppX, vmax = (kTileH / 2) * g.ppY;
+
+    const int tx = threadIdx.x % kThreadsX, ty = threadIdx.x / kThreadsX;
+    const int warp = threadIdx.x >> 5;
+    float u[kPixW], uu[kPixW], v[kPixH], vv[kPixH];
+#pragma unroll
+    for (int c = 0; c < kPixW; ++c) {
+        u[c] = (float)((double)(tx * kPixW + c - kTileW / 2) * g.ppX);
+        uu[c] = u[c] * u[c];
+    }
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) {
+        v[r] = (float)((double)(kTileH / 2 - (ty * kPixH + r)) * g.ppY);
+        vv[r] = v[r] * v[r];
+    }
+    const float inv_lambda_f = (float)g.inv_lambda;
+    const float detx_f = (float)g.detx, dety_f = (float)g.dety;
+
+#pragma unroll
+    for (int k = 0; k < kPixH * kPixW; ++k) s_acc[k * kThreads + threadIdx.x] = make_double2(0.0, 0.0);
+
+    const int64_t n = jg.n_points;
+    const int64_t p_beg = (int64_t)part * jg.points_per_split;
+    const int64_t p_end = min(n, p_beg + jg.points_per_split);
+    const PointRec* chrec = recs + (int64_t)ch * n;
+
+    for (int64_t cb = p_beg; cb < p_end; cb += kChunk) {
+        // ---- classify the chunk's points against this tile (FP64) --------
+        int cls[2];
+        RsSRec tmp[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            cls[q] = 0;  // 0 skip, 1 fast, 2 exact
+            const int64_t idx = cb + threadIdx.x + q * kThreads;
+            if (idx < p_end) {
+                const PointRec p = chrec[idx];
+                const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
+                const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
+                if (ix0 < ix1 && iy0 < iy1) {
+                    const double dxc = Xc - p.x, dyc = Yc - p.y;
+                    const double zz = p.aux;
+                    const double rc2 = dxc * dxc + dyc * dyc + zz;
+                    const double rc = sqrt(rc2);
+                    const double tc = rc * g.inv_lambda;
+                    const double fc = tc - rint(tc);
+                    const bool rect_full = p.x_lo <= X0 && p.x_hi >= vx1 && p.y_lo <= Y0 && p.y_hi >= vy1;
+                    // conservative cone test over the whole tile
+                    const double ax0 = fabs(Xmin - p.x), ax1 = fabs(Xmax - p.x);
+                    const double ay0 = fabs(Ymin - p.y), ay1 = fabs(Ymax - p.y);
+                    const double maxdx = fmax(ax0, ax1), maxdy = fmax(ay0, ay1);
+                    const double mindx = (p.x >= Xmin && p.x <= Xmax) ? 0.0 : fmin(ax0, ax1);
+                    const double mindy = (p.y >= Ymin && p.y <= Ymax) ? 0.0 : fmin(ay0, ay1);
+                    const bool cone_full =
+                        maxdx < g.detx * sqrt(mindy * mindy + zz) * (1.0 - 1e-9) &&
+                        maxdy < g.dety * sqrt(mindx * mindx + zz) * (1.0 - 1e-9);
+                    const double nmax = 2.0 * fabs(dxc) * umax + umax * umax + 2.0 * fabs(dyc) * vmax + vmax * vmax;
+                    const double wmax = nmax / rc2;
+                    const bool series_ok = wmax < kMaxW && tc * wmax * wmax * wmax * (1.0 / 16.0) < kSeriesTol;
+                    RsSRec& t = tmp[q];
+                    t.fc = (float)fc;
+                    if (rect_full && cone_full && series_ok) {
+                        cls[q] = 1;
+                        const double h = 1.0 / rc2;
+                        t.P = (float)(2.0 * dxc * h);
+                        t.Q = (float)(2.0 * dyc * h);
+                        t.h = (float)h;
+                        t.g = (float)tc;
+                        t.ac = (float)(p.coef * h);
+                    } else {
+                        cls[q] = 2;
+                        t.P = (float)(2.0 * dxc);
+                        t.Q = (float)(2.0 * dyc);
+                        t.h = (float)rc2;
+                        t.g = (float)rc;
+                        t.ac = (float)p.coef;
+                        t.dxc = (float)dxc;
+                        t.dyc = (float)dyc;
+                        t.zz = (float)zz;
+                        t.mabs = (float)(1e-6 * (fabs(dxc) + fabs(dyc) + umax + vmax + sqrt(zz)) *
+                                         (1.0 + g.detx + g.dety));
+                        t.idx = (int32_t)idx;
+                        t.xl = p.x_lo - X0;
+                        t.xh = p.x_hi - X0;
+                        t.yl = p.y_lo - Y0;
+                        t.yh = p.y_hi - Y0;
+                    }
+                }
+            }
+        }
+        // ---- deterministic compaction: FAST from the front, EXACT from the back
+        unsigned bf[2], be[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            bf[q] = __ballot_sync(0xffffffffu, cls[q] == 1);
+            be[q] = __ballot_sync(0xffffffffu, cls[q] == 2);
+            if ((threadIdx.x & 31) == 0) {
+                s_cnt[0][q][warp] = __popc(bf[q]);
+                s_cnt[1][q][warp] = __popc(be[q]);
+            }
+        }
+        __syncthreads();
+        int n_fast = 0, n_exact = 0;
+        int off_f[2], off_e[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+#pragma unroll
+            for (int w = 0; w < kThreads / 32; ++w) {
+                if (w == warp) {
+                    off_f[q] = n_fast;
+                    off_e[q] = n_exact;
+                }
+                n_fast += s_cnt[0][q][w];
+                n_exact += s_cnt[1][q][w];
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (cls[q] == 1) s_rec[off_f[q] + warp_prefix(bf[q])] = tmp[q];
+            else if (cls[q] == 2) s_rec[kChunk - 1 - (off_e[q] + warp_prefix(be[q]))] = tmp[q];
+        }
+        __syncthreads();
+
+        // ---- FAST: whole tile inside the window, series phase --------------
+        float sr[kPixH * kPixW], si[kPixH * kPixW];
+#pragma unroll
+        for (int k = 0; k < kPixH * kPixW; ++k) sr[k] = si[k] = 0.f;
+#pragma unroll 1
+        for (int j = 0; j < n_fast; ++j) {
+            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);
+            const float2 b = *reinterpret_cast<const float2*>(&s_rec[j].fc);
+            float A[kPixW], B[kPixH];
+#pragma unroll
+            for (int c = 0; c < kPixW; ++c) A[c] = fmaf(a.x, u[c], a.z * uu[c]);
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) B[r] = fmaf(a.y, v[r], a.z * vv[r]);
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) {
+#pragma unroll
+                for (int c = 0; c < kPixW; ++c) {
+                    const float w = A[c] + B[r];
+                    const float q = fmaf(w, -0.125f, 0.5f);
+                    float t = fmaf(a.w * w, q, b.x);
+                    t = reduce_turns(t);
+                    float s, co;
+                    __sincosf(t * kTwoPi, &s, &co);
+                    const float amp = fmaf(-b.y, w, b.y);
+                    const int k = r * kPixW + c;
+                    sr[k] = fmaf(amp, s, sr[k]);
+                    si[k] = fmaf(amp, co, si[k]);
+                }
+            }
+        }
+        // ---- EXACT: window cuts the tile, or |w| too large for the series ---
+#pragma unroll 1
+        for (int j = 0; j < n_exact; ++j) {
+            const RsSRec& e = s_rec[kChunk - 1 - j];
+            bool inx[kPixW], iny[kPixH];
+            float dx[kPixW], dy[kPixH], nx[kPixW], ny[kPixH];
+#pragma unroll
+            for (int c = 0; c < kPixW; ++c) {
+                const int cl = tx * kPixW + c;
+                inx[c] = cl >= e.xl && cl < e.xh;
+                dx[c] = e.dxc + u[c];
+                nx[c] = u[c] * (e.P + u[c]);
+            }
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) {
+                const int rl = ty * kPixH + r;
+                iny[r] = rl >= e.yl && rl < e.yh;
+                dy[r] = e.dyc + v[r];
+                ny[r] = v[r] * (e.Q + v[r]);
+            }
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) {
+#pragma unroll
+                for (int c = 0; c < kPixW; ++c) {
+                    if (!(inx[c] && iny[r])) continue;
+                    // cone test (ophGen.cpp:415-428): |X-x| < detx*sqrt((Y-y)^2+z^2)
+                    // and |Y-y| < dety*sqrt((X-x)^2+z^2)
+                    const float lx = fabsf(dx[c]), rx = detx_f * sqrtf(fmaf(dy[r], dy[r], e.zz));
+                    const float ly = fabsf(dy[r]), ry = dety_f * sqrtf(fmaf(dx[c], dx[c], e.zz));
+                    const float mx = 1e-5f * (lx + rx) + e.mabs, my = 1e-5f * (ly + ry) + e.mabs;
+                    const bool xpass = rx - lx > mx, xfail = lx - rx > mx;
+                    const bool ypass = ry - ly > my, yfail = ly - ry > my;
+                    bool inside;
+                    if (xfail || yfail) {
+                        inside = false;
+                    } else if (xpass && ypass) {
+                        inside = true;
+                    } else {
+                        // FP64 replica of the reference decision
+                        const PointRec p = chrec[e.idx];
+                        const double xxx = pixel_x(g, X0 + tx * kPixW + c);
+                        const double yyy = pixel_y(g, Y0 + ty * kPixH + r);
+                        const double ddy = __dsub_rn(yyy, p.y), ddx = __dsub_rn(xxx, p.x);
+                        const double hx = fabs(__dmul_rn(g.detx, sqrt(__dadd_rn(__dmul_rn(ddy, ddy), p.aux))));
+                        const double hy = fabs(__dmul_rn(g.dety, sqrt(__dadd_rn(__dmul_rn(ddx, ddx), p.aux))));
+                        inside = (xxx < __dadd_rn(p.x, hx)) && (xxx > __dsub_rn(p.x, hx)) &&
+                                 (yyy < __dadd_rn(p.y, hy)) && (yyy > __dsub_rn(p.y, hy));
+                    }
+                    if (!inside) continue;
+                    const float nn = nx[c] + ny[r];
+                    const float rp2 = e.h + nn;
+                    const float ri = rsqrtf(rp2);
+                    const float rp = rp2 * ri;
+                    const float dt = __fdividef(nn * inv_lambda_f, rp + e.g);
+                    const float t = reduce_turns(e.fc + dt);
+                    float s, co;
+                    __sincosf(t * kTwoPi, &s, &co);
+                    const float amp = e.ac * ri * ri;
+                    const int k = r * kPixW + c;
+                    sr[k] = fmaf(amp, s, sr[k]);
+                    si[k] = fmaf(amp, co, si[k]);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPixH * kPixW; ++k) {
+            double2 a = s_acc[k * kThreads + threadIdx.x];
+            a.x += (double)sr[k];
+            a.y += (double)si[k];
+            s_acc[k * kThreads + threadIdx.x] = a;
+        }
+        __syncthreads();   // s_rec is rewritten by the next chunk
+    }
+
+    // ---- store: (sum a sin, -sum a cos), the reference's (sin, -cos) terms
+    double2* dst = (part == 0) ? field
+                               : partials + (int64_t)(part - 1) * jg.n_channels * g.pnX * (int64_t)g.pnY;
+    dst += (int64_t)ch * g.pnX * (int64_t)g.pnY;
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) {
+        const int row = Y0 + ty * kPixH + r;
+        if (row >= g.pnY) continue;
+#pragma unroll
+        for (int c = 0; c < kPixW; ++c) {
+            const int col = X0 + tx * kPixW + c;
+            if (col >= g.pnX) continue;
+            const double2 a = s_acc[(r * kPixW + c) * kThreads + threadIdx.x];
+            dst[(int64_t)row * g.pnX + col] = make_double2(a.x, -a.y);
+        }
+    }
+}
+
+}  // namespace
+
+constexpr size_t kRsSmem = sizeof(RsSRec) * kChunk + sizeof(double2) * kPixH * kPixW * kThreads;
+
+int rs_blocks_per_sm() {
+    cudaFuncSetAttribute(rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRsSmem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rs_kernel, kThreads, kRsSmem) != cudaSuccess) nb = 1;
+    return nb > 0 ? nb : 1;
+}
+
+void launch_rs(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
+               cudaStream_t stream) {
+    dim3 grid((unsigned)jg.tiles_x, (unsigned)jg.tiles_y, (unsigned)(jg.n_channels * jg.ksplit));
+    rs_kernel<<<grid, kThreads, kRsSmem, stream>>>(d_recs, jg, d_field, d_partials);
+}
+
+}  // namespace ophpc

@@ -1,0 +1,271 @@
+"""Python bindings for the CPU oracle (test infrastructure only).
+
+Two checkers live here:
+
+* ``libophpc_oracle.so`` (built from ``ophpc_oracle.c``): the C restatement
+  of Openholo's point-cloud CPU path. It always builds (gcc + OpenMP) and is
+  what the GPU parity tests, ``smoke()`` and the CPU arm of ``bench.py`` use.
+* ``_ref/libophref.so``: the reference's own CPU path compiled from the
+  reference sources (``make -C oracle ref``). It exists only where the
+  reference tree is present; it pins the restatement through the fixtures in
+  ``tests/golden/`` that ``tests/golden/make_golden.py`` writes.
+
+Nothing in the product package imports this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+from dataclasses import dataclass, field
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "lib", "libophpc_oracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libophref.so")
+REFERENCE_TREE = os.environ.get("OPHPC_REFERENCE_TREE", "/root/reference")
+
+_lock = threading.Lock()
+_ora = None
+_ref = None
+
+
+def build(with_reference: Optional[bool] = None, quiet: bool = True) -> None:
+    """Compile the restatement (always) and the reference build (when the
+    reference tree is present, or when ``with_reference`` is True)."""
+    if with_reference is None:
+        with_reference = os.path.isdir(os.path.join(REFERENCE_TREE, "ophgen", "src"))
+    target = "ref" if with_reference else "all"
+    cmd = ["make", "-C", HERE, "-j8", target, f"REF={REFERENCE_TREE}"]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{out.stdout}\n{out.stderr}")
+    if not quiet:
+        print(out.stdout)
+
+
+class OracleConfig(ctypes.Structure):
+    _fields_ = [
+        ("pixel_number", ctypes.c_int32 * 2),
+        ("offset", ctypes.c_int32 * 2),
+        ("pixel_pitch", ctypes.c_double * 2),
+        ("scale", ctypes.c_double * 3),
+        ("distance", ctypes.c_double),
+        ("field_length", ctypes.c_double),
+        ("viewing_window", ctypes.c_int32),
+        ("n_channels", ctypes.c_int32),
+        ("wave_length", ctypes.c_double * 3),
+    ]
+
+
+@dataclass
+class Geometry:
+    """One hologram job's geometry: the OphConfig/OphPointCloudConfig fields
+    the point-cloud path reads."""
+    pnx: int
+    pny: int
+    ppx: float
+    ppy: float
+    wavelengths: Sequence[float]
+    scale: Sequence[float] = (1.0, 1.0, 1.0)
+    distance: float = 0.0
+    offset: Sequence[int] = (0, 0)
+    field_length: float = 0.0
+    viewing_window: bool = False
+    extra_xml: dict = field(default_factory=dict)
+
+    @property
+    def n_channels(self) -> int:
+        return len(self.wavelengths)
+
+    def to_c(self) -> OracleConfig:
+        c = OracleConfig()
+        c.pixel_number[0], c.pixel_number[1] = self.pnx, self.pny
+        c.offset[0], c.offset[1] = int(self.offset[0]), int(self.offset[1])
+        c.pixel_pitch[0], c.pixel_pitch[1] = self.ppx, self.ppy
+        for i in range(3):
+            c.scale[i] = float(self.scale[i])
+        c.distance = float(self.distance)
+        c.field_length = float(self.field_length)
+        c.viewing_window = 1 if self.viewing_window else 0
+        c.n_channels = len(self.wavelengths)
+        for i, w in enumerate(self.wavelengths):
+            c.wave_length[i] = float(w)
+        return c
+
+    def xml(self) -> str:
+        """The flat <PointCloud> config the reference's readConfig parses
+        (ophgen/src/ophGen.cpp:221-358, ophgen/src/ophPointCloud.cpp:83-149)."""
+        lines = ["<PointCloud>"]
+        lines.append(f"  <ScaleX>{self.scale[0]!r}</ScaleX>")
+        lines.append(f"  <ScaleY>{self.scale[1]!r}</ScaleY>")
+        lines.append(f"  <ScaleZ>{self.scale[2]!r}</ScaleZ>")
+        lines.append(f"  <Distance>{self.distance!r}</Distance>")
+        lines.append(f"  <FieldLength>{self.field_length!r}</FieldLength>")
+        lines.append(f"  <SLM_PixelPitchX>{self.ppx!r}</SLM_PixelPitchX>")
+        lines.append(f"  <SLM_PixelPitchY>{self.ppy!r}</SLM_PixelPitchY>")
+        lines.append(f"  <SLM_PixelNumX>{self.pnx}</SLM_PixelNumX>")
+        lines.append(f"  <SLM_PixelNumY>{self.pny}</SLM_PixelNumY>")
+        lines.append(f"  <SLM_WaveNum>{len(self.wavelengths)}</SLM_WaveNum>")
+        for i, w in enumerate(self.wavelengths):
+            lines.append(f"  <SLM_WaveLength_{i + 1}>{float(w)!r}</SLM_WaveLength_{i + 1}>")
+        for k, v in self.extra_xml.items():
+            lines.append(f"  <{k}>{v}</{k}>")
+        lines.append("</PointCloud>")
+        return "\n".join(lines) + "\n"
+
+
+def _p(a: np.ndarray, t=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(t))
+
+
+def _load_oracle():
+    global _ora
+    with _lock:
+        if _ora is None:
+            if not os.path.exists(ORACLE_LIB):
+                build(with_reference=False)
+            lib = ctypes.CDLL(ORACLE_LIB)
+            lib.oracle_generate.argtypes = [ctypes.POINTER(OracleConfig), ctypes.POINTER(ctypes.c_double),
+                                            ctypes.c_int64, ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+            lib.oracle_generate.restype = ctypes.c_int
+            lib.oracle_field_at.argtypes = [ctypes.POINTER(OracleConfig), ctypes.POINTER(ctypes.c_double),
+                                            ctypes.c_int64, ctypes.c_int32, ctypes.c_int32,
+                                            ctypes.POINTER(ctypes.c_int64), ctypes.c_int64,
+                                            ctypes.POINTER(ctypes.c_double)]
+            lib.oracle_field_at.restype = ctypes.c_int
+            lib.oracle_encode.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int64, ctypes.c_int32,
+                                          ctypes.POINTER(ctypes.c_double)]
+            lib.oracle_encode.restype = ctypes.c_int
+            lib.oracle_normalize.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.c_int32, ctypes.c_int64,
+                                             ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_double),
+                                             ctypes.POINTER(ctypes.c_double)]
+            lib.oracle_normalize.restype = None
+            _ora = lib
+    return _ora
+
+
+def _vertices(v: np.ndarray) -> np.ndarray:
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    if v.ndim != 2 or v.shape[1] != 7:
+        raise ValueError("vertices must be an (n, 7) float64 array: pos[3], color[3], phase")
+    return v
+
+
+def generate(geom: Geometry, vertices: np.ndarray, diff_flag: int) -> np.ndarray:
+    """Full complex field [n_channels, pny, pnx] (complex128)."""
+    lib = _load_oracle()
+    v = _vertices(vertices)
+    out = np.empty((geom.n_channels, geom.pny, geom.pnx, 2), dtype=np.float64)
+    c = geom.to_c()
+    rc = lib.oracle_generate(ctypes.byref(c), _p(v), v.shape[0], diff_flag, _p(out))
+    if rc != 0:
+        raise ValueError("oracle_generate rejected its arguments")
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def field_at(geom: Geometry, vertices: np.ndarray, diff_flag: int, channel: int,
+             pixel_index: np.ndarray) -> np.ndarray:
+    """Complex field of one channel at flat pixel indices (y*pnx + x)."""
+    lib = _load_oracle()
+    v = _vertices(vertices)
+    idx = np.ascontiguousarray(pixel_index, dtype=np.int64)
+    out = np.empty((idx.shape[0], 2), dtype=np.float64)
+    c = geom.to_c()
+    rc = lib.oracle_field_at(ctypes.byref(c), _p(v), v.shape[0], diff_flag, channel,
+                             _p(idx, ctypes.c_int64), idx.shape[0], _p(out))
+    if rc != 0:
+        raise ValueError("oracle_field_at rejected its arguments")
+    return out[:, 0] + 1j * out[:, 1]
+
+
+def encode(field: np.ndarray, encode_flag: int) -> np.ndarray:
+    lib = _load_oracle()
+    f = np.ascontiguousarray(field, dtype=np.complex128)
+    flat = f.reshape(-1).view(np.float64)
+    out = np.empty(f.size, dtype=np.float64)
+    if lib.oracle_encode(_p(flat), f.size, encode_flag, _p(out)) != 0:
+        raise ValueError("oracle_encode rejected its arguments")
+    return out.reshape(f.shape)
+
+
+def normalize(encoded: np.ndarray):
+    """encoded: [n_channels, ...]; returns (uint8 codes, min, max)."""
+    lib = _load_oracle()
+    e = np.ascontiguousarray(encoded, dtype=np.float64)
+    nch = e.shape[0]
+    per = e.size // nch
+    out = np.empty(e.shape, dtype=np.uint8)
+    mn, mx = ctypes.c_double(), ctypes.c_double()
+    lib.oracle_normalize(_p(e), nch, per, _p(out, ctypes.c_uint8), ctypes.byref(mn), ctypes.byref(mx))
+    return out, mn.value, mx.value
+
+
+# ---------------------------------------------------------------- reference
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _load_ref():
+    global _ref
+    with _lock:
+        if _ref is None:
+            if not os.path.exists(REF_LIB):
+                raise FileNotFoundError("oracle/_ref/libophref.so is not built (make -C oracle ref)")
+            lib = ctypes.CDLL(REF_LIB)
+            lib.ophref_run.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong,
+                                       ctypes.c_int, ctypes.c_uint, ctypes.c_uint,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            lib.ophref_run.restype = ctypes.c_int
+            lib.ophref_query.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
+            lib.ophref_query.restype = ctypes.c_int
+            lib.ophref_load_ply.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong]
+            lib.ophref_load_ply.restype = ctypes.c_longlong
+            _ref = lib
+    return _ref
+
+
+def ref_load_ply(path: str) -> np.ndarray:
+    lib = _load_ref()
+    n = lib.ophref_load_ply(path.encode(), None, 0)
+    if n < 0:
+        raise ValueError(f"reference PLYparser failed on {path}")
+    out = np.zeros((n, 7), dtype=np.float64)
+    lib.ophref_load_ply(path.encode(), out.ctypes.data, n)
+    return out
+
+
+def ref_run(xml_path: str, vertices: Optional[np.ndarray] = None, ply_path: Optional[str] = None,
+            diff_flag: int = 0, encode_flag: int = 0, viewing_window: bool = False):
+    """Run the reference CPU path; returns (field, encoded, normalized, seconds).
+    encode_flag 2 encodes the same field as phase and then amplitude and
+    returns both stacked on a leading axis."""
+    lib = _load_ref()
+    pnx, pny, nch = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    if lib.ophref_query(xml_path.encode(), ctypes.byref(pnx), ctypes.byref(pny), ctypes.byref(nch)) != 0:
+        raise ValueError(f"reference readConfig failed on {xml_path}")
+    shape = (nch.value, pny.value, pnx.value)
+    field = np.zeros(shape + (2,), dtype=np.float64)
+    n_enc = 2 if encode_flag == 2 else 1
+    enc = np.zeros((n_enc,) + shape, dtype=np.float64)
+    nrm = np.zeros((n_enc,) + shape, dtype=np.uint8)
+    secs = ctypes.c_double()
+    v = None
+    n = 0
+    if ply_path is None:
+        v = _vertices(vertices)
+        n = v.shape[0]
+    rc = lib.ophref_run(xml_path.encode(), ply_path.encode() if ply_path else None,
+                        v.ctypes.data if v is not None else None, n, 1 if viewing_window else 0,
+                        diff_flag, encode_flag, field.ctypes.data, enc.ctypes.data, nrm.ctypes.data,
+                        ctypes.byref(secs))
+    if rc != 0:
+        raise RuntimeError(f"ophref_run failed ({rc})")
+    if n_enc == 1:
+        enc, nrm = enc[0], nrm[0]
+    return field[..., 0] + 1j * field[..., 1], enc, nrm, secs.value

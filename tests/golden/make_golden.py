@@ -1,0 +1,166 @@
+"""Generates the golden vectors in tests/golden/ from the reference itself.
+
+Runs the reference's own CPU path (oracle/_ref/libophref.so, compiled from
+the reference sources by ``make -C oracle ref``) through its public API
+(readConfig -> setPointCloudModel | loadPointCloud -> SetMode(MODE_CPU) ->
+generateHologram -> encoding -> normalize; Example/examPointCloud/
+examPointCloud.cpp:54-132) on small seeded inputs, and stores the complex
+field, the encoded buffer and the 8-bit codes. The PLY cases write PLY files
+in the reference's own point-cloud format (ASCII and binary_little_endian,
+with and without the `color channel` element) and record the Vertex arrays
+the reference PLYparser returns for them.
+
+The reference does not exist where the GPU tests run; only these committed
+fixtures travel. Re-run with:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import struct
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle  # noqa: E402
+
+
+def box(n, xy, z, seed):
+    rng = np.random.default_rng(seed)
+    v = np.zeros((n, 7))
+    v[:, 0] = rng.uniform(-xy[0], xy[0], n)
+    v[:, 1] = rng.uniform(-xy[1], xy[1], n)
+    v[:, 2] = rng.uniform(z[0], z[1], n)
+    v[:, 3:6] = 1.0 - rng.uniform(0.0, 1.0, (n, 3))
+    v[:, 6] = rng.uniform(0, 2 * np.pi, n)
+    return v
+
+
+# name: (geometry, vertices, diff_flag, viewing_window)
+FIELD_CASES = {
+    "rs_window_1ch": (oracle.Geometry(pnx=96, pny=64, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                      box(300, (4e-4, 3e-4), (0.002, 0.01), 101), 0, False),
+    "fresnel_window_1ch": (oracle.Geometry(pnx=96, pny=64, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                           box(300, (4e-4, 3e-4), (0.002, 0.01), 102), 1, False),
+    "rs_3ch_vw": (oracle.Geometry(pnx=80, pny=48, ppx=6.4e-6, ppy=7.1e-6, wavelengths=[638e-9, 532e-9, 473e-9],
+                                  scale=(0.01, 0.01, 0.01), distance=0.1, field_length=1.0,
+                                  viewing_window=True),
+                  box(250, (0.05, 0.05), (-0.2, 0.2), 103), 0, True),
+    "fresnel_3ch": (oracle.Geometry(pnx=80, pny=48, ppx=6.4e-6, ppy=7.1e-6,
+                                    wavelengths=[638e-9, 532e-9, 473e-9], scale=(0.5, 0.5, 2.0), distance=0.05),
+                    box(250, (1e-3, 1e-3), (0.05, 0.2), 104), 1, False),
+}
+
+
+def rs_1k_crop():
+    """The rs_1k distribution (x, y ~ U(+-2 mm), z ~ U[0.45, 0.55] m, amplitude
+    U(0, 1], seed 0) on a 256x256 crop of its SLM with 500 points."""
+    rng = np.random.default_rng(0)
+    n = 500
+    v = np.zeros((n, 7))
+    v[:, 0] = rng.uniform(-2e-3, 2e-3, n)
+    v[:, 1] = rng.uniform(-2e-3, 2e-3, n)
+    v[:, 2] = rng.uniform(0.45, 0.55, n)
+    amp = 1.0 - rng.uniform(0.0, 1.0, n)
+    v[:, 3:6] = amp[:, None]
+    return oracle.Geometry(pnx=256, pny=256, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]), v
+
+
+def write_ply_ascii(path, xyz, rgb, phase, with_channel=True):
+    n = xyz.shape[0]
+    with open(path, "w") as f:
+        f.write("ply\nformat ascii 1.0\ncomment synthetic point cloud\n")
+        if with_channel:
+            f.write("element color 1\nproperty int channel\n")
+        f.write(f"element vertex {n}\nproperty float x\nproperty float y\nproperty float z\n")
+        f.write("property uchar red\nproperty uchar green\nproperty uchar blue\nproperty double phase\n")
+        f.write("end_header\n")
+        if with_channel:
+            f.write("3\n")
+        for i in range(n):
+            f.write(f"{xyz[i, 0]:.6f} {xyz[i, 1]:.6f} {xyz[i, 2]:.6f} {rgb[i, 0]} {rgb[i, 1]} {rgb[i, 2]} "
+                    f"{phase[i]:.6f}\n")
+
+
+def write_ply_binary(path, xyz, rgb, phase, with_channel=True):
+    n = xyz.shape[0]
+    hdr = "ply\nformat binary_little_endian 1.0\ncomment synthetic point cloud\n"
+    if with_channel:
+        hdr += "element color 1\nproperty int channel\n"
+    hdr += (f"element vertex {n}\nproperty float x\nproperty float y\nproperty float z\n"
+            "property uchar red\nproperty uchar green\nproperty uchar blue\nproperty float phase\nend_header\n")
+    with open(path, "wb") as f:
+        f.write(hdr.encode())
+        if with_channel:
+            f.write(struct.pack("<i", 3))
+        for i in range(n):
+            f.write(struct.pack("<fffBBBf", xyz[i, 0], xyz[i, 1], xyz[i, 2], int(rgb[i, 0]), int(rgb[i, 1]),
+                                int(rgb[i, 2]), phase[i]))
+
+
+def main():
+    if not oracle.ref_available():
+        oracle.build(with_reference=True)
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        xml = os.path.join(d, "cfg.xml")
+        for name, (g, v, diff, vw) in FIELD_CASES.items():
+            with open(xml, "w") as f:
+                f.write(g.xml())
+            field, enc, codes, _ = oracle.ref_run(xml, vertices=v, diff_flag=diff, encode_flag=2,
+                                                  viewing_window=vw)
+            enc_p, enc_a, codes_p, codes_a = enc[0], enc[1], codes[0], codes[1]
+            np.savez_compressed(os.path.join(HERE, f"{name}.npz"), vertices=v, field=field, enc_phase=enc_p,
+                                codes_phase=codes_p, enc_amp=enc_a, codes_amp=codes_a, diff_flag=diff,
+                                xml=g.xml(), viewing_window=vw)
+            out[name] = field.shape
+        # rs_1k crop: codes in full, the field at sampled pixels
+        g, v = rs_1k_crop()
+        with open(xml, "w") as f:
+            f.write(g.xml())
+        field, _, codes, _ = oracle.ref_run(xml, vertices=v, diff_flag=0, encode_flag=2)
+        codes_p, codes_a = codes[0], codes[1]
+        rng = np.random.default_rng(7)
+        idx = np.sort(rng.choice(256 * 256, 2048, replace=False))
+        np.savez_compressed(os.path.join(HERE, "rs_1k_crop.npz"), vertices=v, pixel_index=idx,
+                            field_at=field[0].reshape(-1)[idx], codes_phase=codes_p, codes_amp=codes_a,
+                            xml=g.xml())
+        out["rs_1k_crop"] = codes_p.shape
+
+        # PLY: files in the reference's format + what PLYparser makes of them
+        rng = np.random.default_rng(9)
+        n = 64
+        xyz = np.round(rng.uniform(-0.5, 0.5, (n, 3)), 6)
+        rgb = rng.integers(0, 256, (n, 3))
+        phase = np.round(rng.uniform(0, 6.28, n), 6)
+        plys = {
+            "ply_ascii_channel.ply": (write_ply_ascii, True),
+            "ply_ascii_nochannel.ply": (write_ply_ascii, False),
+            "ply_binary_channel.ply": (write_ply_binary, True),
+        }
+        ply_vertices = {}
+        for fname, (writer, ch) in plys.items():
+            path = os.path.join(HERE, fname)
+            writer(path, xyz, rgb, phase, ch)
+            ply_vertices[fname.replace(".ply", "")] = oracle.ref_load_ply(path)
+        np.savez_compressed(os.path.join(HERE, "ply_vertices.npz"), **ply_vertices)
+
+        # A PLY-driven generate: the reference's loadPointCloud path end to end
+        g = oracle.Geometry(pnx=72, pny=40, ppx=4.3e-6, ppy=4.3e-6, wavelengths=[638e-9, 532e-9, 473e-9],
+                            scale=(0.01, 0.01, 0.01), distance=0.1)
+        with open(xml, "w") as f:
+            f.write(g.xml())
+        field, _, codes_p, _ = oracle.ref_run(xml, ply_path=os.path.join(HERE, "ply_ascii_channel.ply"),
+                                             diff_flag=0, encode_flag=0)
+        np.savez_compressed(os.path.join(HERE, "ply_generate_rs.npz"), field=field, codes_phase=codes_p,
+                            xml=g.xml())
+    for k, v in out.items():
+        print(k, v)
+
+
+if __name__ == "__main__":
+    main()

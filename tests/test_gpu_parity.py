@@ -1,0 +1,153 @@
+"""GPU parity: libophpc (through the C ABI) against the CPU oracle.
+
+Tolerances (spec bar, stated here): complex field relative L2 error
+<= 1e-4 against the FP64 oracle, and the 8-bit encoded hologram exact on
+>= 99.9% of pixels and within +-1 LSB elsewhere (phase codes compared
+circularly, 255 and 0 being neighbours). The oracle restates the reference CPU
+path (ophgen/src/ophGen.cpp:361-514, 654-687, 1843-1864) and is pinned to the
+reference itself by tests/test_oracle.py.
+"""
+import numpy as np
+import pytest
+
+from tests._util import code_agreement, rel_l2, run_encode, run_generate
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-4
+CODE_EXACT = 0.999
+
+
+def _box(n, xy, z, seed, amp_lo=0.0):
+    rng = np.random.default_rng(seed)
+    v = np.zeros((n, 7))
+    v[:, 0] = rng.uniform(-xy[0], xy[0], n)
+    v[:, 1] = rng.uniform(-xy[1], xy[1], n)
+    v[:, 2] = rng.uniform(z[0], z[1], n)
+    v[:, 3:6] = 1.0 - rng.uniform(amp_lo, 1.0, (n, 3))
+    v[:, 6] = rng.uniform(0, 2 * np.pi, n)
+    return v
+
+
+CASES = {
+    # full aperture, the benchmark regime
+    "rs_full": (dict(pnx=256, pny=192, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                _box(1500, (1e-3, 1e-3), (0.3, 0.5), 11), 0, {}),
+    "fresnel_full": (dict(pnx=256, pny=192, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                     _box(1500, (1e-3, 1e-3), (0.3, 0.5), 12), 1, {}),
+    # points close to the SLM: windows of ~20 px cut most tiles (EXACT class)
+    "rs_window": (dict(pnx=200, pny=120, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                  _box(600, (6e-4, 4e-4), (0.002, 0.01), 13), 0, {}),
+    "fresnel_window": (dict(pnx=200, pny=120, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                       _box(600, (6e-4, 4e-4), (0.002, 0.01), 14), 1, {}),
+    # three channels, non-square pitch, odd sizes, scale and distance
+    "rs_3ch_odd": (dict(pnx=130, pny=77, ppx=6.4e-6, ppy=7.1e-6, wavelengths=[638e-9, 532e-9, 473e-9],
+                        scale=(0.5, 0.5, 2.0), distance=0.05),
+                   _box(700, (1e-3, 1e-3), (0.05, 0.2), 15), 0, {}),
+    "fresnel_3ch_odd": (dict(pnx=130, pny=77, ppx=6.4e-6, ppy=7.1e-6, wavelengths=[638e-9, 532e-9, 473e-9],
+                             scale=(0.5, 0.5, 2.0), distance=0.05),
+                        _box(700, (1e-3, 1e-3), (0.05, 0.2), 16), 1, {}),
+    # start offset and the viewing-window transform
+    "rs_offset_vw": (dict(pnx=96, pny=160, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9], scale=(0.01, 0.01, 0.01),
+                          distance=0.1),
+                     _box(400, (0.05, 0.05), (-0.2, 0.2), 17), 0,
+                     dict(offset=(3, -2), viewing_window=True, field_length=1.0)),
+    "fresnel_offset_vw": (dict(pnx=96, pny=160, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9],
+                               scale=(0.01, 0.01, 0.01), distance=0.1),
+                          _box(400, (0.05, 0.05), (-0.2, 0.2), 18), 1,
+                          dict(offset=(3, -2), viewing_window=True, field_length=1.0)),
+}
+
+
+def _oracle_field(oracle_mod, gk, v, diff, extra):
+    g = oracle_mod.Geometry(**{k: gk[k] for k in ("pnx", "pny", "ppx", "ppy", "wavelengths")},
+                            scale=gk.get("scale", (1.0, 1.0, 1.0)), distance=gk.get("distance", 0.0),
+                            offset=extra.get("offset", (0, 0)), field_length=extra.get("field_length", 0.0),
+                            viewing_window=extra.get("viewing_window", False))
+    return oracle_mod.generate(g, v, diff)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_field_and_codes(gpu_ctx, oracle_mod, name):
+    gk, v, diff, extra = CASES[name]
+    ref = _oracle_field(oracle_mod, gk, v, diff, extra)
+    got = run_generate(gpu_ctx, gk, v, diff, **extra)
+    assert got.shape == ref.shape
+    err = rel_l2(got, ref)
+    print(f"{name}: relL2 = {err:.3e}")
+    assert err <= FIELD_TOL, f"{name}: relL2 {err:.3e} above {FIELD_TOL}"
+    for flag, circ in ((0, True), (1, False)):
+        enc_ref = oracle_mod.encode(ref, flag)
+        codes_ref, _, _ = oracle_mod.normalize(enc_ref)
+        enc, codes = run_encode(gpu_ctx, got, flag)
+        exact, maxd = code_agreement(codes, codes_ref, circ)
+        print(f"  encode {flag}: exact {exact:.5f}, max |d| {maxd}")
+        assert exact >= CODE_EXACT and maxd <= 1
+
+
+def test_encode_bit_exact_on_identical_field(gpu_ctx, oracle_mod):
+    """Same field in -> the device encoder reproduces the reference's
+    encode + normalise byte for byte (FP64, no contraction)."""
+    rng = np.random.default_rng(5)
+    f = (rng.normal(size=(3, 64, 80)) + 1j * rng.normal(size=(3, 64, 80))) * 1e3
+    f[1, 3, 4] = 0.0
+    for flag in (0, 1, 2, 3):
+        enc, codes = run_encode(gpu_ctx, f, flag)
+        if flag <= 1:
+            enc_ref = oracle_mod.encode(f, flag)
+        else:
+            enc_ref = f.real.copy() if flag == 2 else f.imag.copy()
+        codes_ref, _, _ = oracle_mod.normalize(enc_ref)
+        assert np.max(np.abs(enc - enc_ref)) <= 4e-16 * max(1.0, np.abs(enc_ref).max())
+        assert np.array_equal(codes, codes_ref), f"flag {flag}"
+
+
+def test_zero_points_gives_zero_field(gpu_ctx):
+    gk = dict(pnx=70, pny=33, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9, 473e-9])
+    got = run_generate(gpu_ctx, gk, np.zeros((0, 7)), 0)
+    assert got.shape == (2, 33, 70) and not np.any(got)
+
+
+def test_single_point_known_answer(gpu_ctx):
+    """One on-axis point: the analytic RS term at the pixel nearest the axis."""
+    gk = dict(pnx=64, pny=64, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    v = np.array([[0.0, 0.0, 0.25, 0.8, 0.8, 0.8, 0.0]])
+    got = run_generate(gpu_ctx, gk, v, 0)[0]
+    lam, pp, pn = 532e-9, 8e-6, 64
+    for yi, xi in ((0, 0), (32, 33), (63, 63), (10, 50)):
+        X = -pn * pp / 2 + (xi - 1) * pp
+        Y = -pn * pp / 2 + (pn - yi) * pp
+        r = np.sqrt(X * X + Y * Y + 0.25 ** 2)
+        a = 0.8 * 0.25 / (lam * r * r)
+        k = 2 * np.pi / lam
+        want = a * np.sin(k * r) - 1j * a * np.cos(k * r)
+        assert abs(got[yi, xi] - want) <= 2e-5 * abs(want)
+
+
+def test_amplitude_linearity(gpu_ctx):
+    gk = dict(pnx=128, pny=96, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    v = _box(800, (1e-3, 1e-3), (0.2, 0.4), 21)
+    for diff in (0, 1):
+        a = run_generate(gpu_ctx, gk, v, diff)
+        v2 = v.copy()
+        v2[:, 3:6] *= 2.5
+        b = run_generate(gpu_ctx, gk, v2, diff)
+        assert rel_l2(b, 2.5 * a) <= 1e-6
+
+
+def test_additivity_over_point_subsets(gpu_ctx):
+    gk = dict(pnx=128, pny=96, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9, 638e-9])
+    v = _box(900, (1e-3, 1e-3), (0.2, 0.4), 22)
+    for diff in (0, 1):
+        whole = run_generate(gpu_ctx, gk, v, diff)
+        parts = run_generate(gpu_ctx, gk, v[:400], diff) + run_generate(gpu_ctx, gk, v[400:], diff)
+        assert rel_l2(parts, whole) <= 5e-6
+
+
+def test_deterministic(gpu_ctx):
+    gk = dict(pnx=300, pny=200, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    v = _box(3000, (1e-3, 1e-3), (0.2, 0.4), 23)
+    for diff in (0, 1):
+        a = run_generate(gpu_ctx, gk, v, diff)
+        b = run_generate(gpu_ctx, gk, v, diff)
+        assert np.array_equal(a, b)
