@@ -1,0 +1,369 @@
+"""Benchmark of the point-cloud hologram path on GB300.
+
+Workload (default): the full-HD three-colour sphere — 1920x1080 SLM at
+8.0 um pitch, 638/532/473 nm channels, 100,000 points on a randomly
+perturbed sphere of radius 3 mm at z = 0.5 m (seeded synthetic data; the
+reference ships no dataset). One step = generateHologram(PC_DIFF_RS) for all
+three channels + phase encoding + 8-bit normalisation over all channels.
+
+The headline `value` is RS point x pixel interactions per second over the
+device-timed steps (inputs resident in HBM, L2 flushed between steps);
+`e2e` is the same metric through the host-facing C ABI with host buffers,
+host->device copy of the vertices and device->host copy of the complex
+field and the 8-bit codes inside every timed step. Fresnel (plain FP32
+kernel) is timed the same way and reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+For N > 1 (torchrun) every rank generates its own hologram of the workload
+(independent jobs, no data-path collective: weak scaling); `value` is the
+sum over ranks divided by the slowest rank's time.
+
+`--impl reference` times the reference's CPU point-cloud path on the host
+cores instead: the reference's own sources (oracle/_ref) where they were
+compiled, else the C restatement of that path (oracle/), each step a
+bounded sample (a subset of the points at full resolution) of the same
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "pt*px/s RS & Fresnel at relL2<=1e-4 vs FP64; serving p50/p99 ms vs plain"
+UNIT = "interactions/s"
+WORKLOAD = "sphere_fhd"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--cpu-points", type=int, default=0, help="points in the CPU sample (0 = auto)")
+    return ap.parse_args()
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_model() -> str:
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part", "hardware")):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.machine()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except Exception:
+            return out
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, r[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=max(mx), reasons=sorted(reasons), samples=len(sm))
+        return out
+
+
+# ------------------------------------------------------------------ CPU arm
+
+def cpu_sample_run(w, n_points: int, diff_flag: int):
+    """Times the CPU point-cloud path on `n_points` of the workload at full
+    resolution with all host threads. Returns (interactions/s, seconds,
+    kind, field)."""
+    import oracle
+    sub = w.subset(n_points)
+    g = oracle.Geometry(pnx=sub.pnx, pny=sub.pny, ppx=sub.pp, ppy=sub.pp, wavelengths=list(sub.wavelengths))
+    if oracle.ref_available():
+        import tempfile
+        with tempfile.TemporaryDirectory() as d:
+            xml = os.path.join(d, "cfg.xml")
+            with open(xml, "w") as f:
+                f.write(g.xml())
+            # generateHologram's own elapsed time (ophgen/src/ophPointCloud.cpp:187-190)
+            field, _, _, secs = oracle.ref_run(xml, vertices=sub.vertices, diff_flag=diff_flag, encode_flag=3)
+        kind = "reference"
+    else:
+        t0 = time.perf_counter()
+        field = oracle.generate(g, sub.vertices, diff_flag)
+        secs = time.perf_counter() - t0
+        kind = "port"
+    return sub.interactions / secs, secs, kind, field
+
+
+def reference_arm(args, w):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    n = args.cpu_points or 60
+    for _ in range(max(0, args.warmup)):
+        cpu_sample_run(w, n, 0)
+    times = []
+    kind = "port"
+    for _ in range(args.steps):
+        _, secs, kind, _ = cpu_sample_run(w, n, 0)
+        times.append(secs)
+    t = sum(times) / len(times)
+    inter = w.subset(n).interactions
+    value = inter / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": w.name, "pnx": w.pnx, "pny": w.pny, "channels": w.n_channels,
+                   "n_points": w.n_points, "diff": "RS", "sample_points": n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": host_cores(), "kind": kind,
+                         "sample": f"{n} of {w.n_points} points, full {w.pnx}x{w.pny}, {w.n_channels} channels, "
+                                   f"RS; OpenMP over {host_cores()} threads ({cpu_model()})"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def gpu_arm(args, w):
+    import torch
+
+    import openholo_gb300 as oph
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    ctx = oph.Context(local)
+    lib = oph.lib()
+    cfg = oph.make_config(**w.geometry_kwargs())
+    nch, pnx, pny = w.n_channels, w.pnx, w.pny
+    npx = pnx * pny
+    s = torch.cuda.current_stream()
+    sp = s.cuda_stream
+    dv = torch.from_numpy(w.vertices).cuda()
+    field = torch.empty((nch, pny, pnx, 2), dtype=torch.float64, device="cuda")
+    codes = torch.empty((nch, npx), dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")   # > 129 MB L2
+
+    def step(diff):
+        ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, 0, field.data_ptr(), sp)
+        ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        """Per-step CUDA events on the launching stream, L2 flushed between steps."""
+        evs = []
+        for _ in range(steps):
+            flush.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            fn()
+            b.record(s)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) / 1e3 for a, b in evs]
+
+    # warm-up
+    for _ in range(max(3, args.warmup)):
+        step(oph.DIFF_RS)
+    torch.cuda.synchronize()
+
+    # --- headline: device-resident RS step ---------------------------------
+    barrier()
+    l0 = lib.ophpc_kernel_launches()
+    wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        step_times = timed(lambda: step(oph.DIFF_RS), args.steps)
+    barrier()
+    wall = time.perf_counter() - wall0
+    launches = lib.ophpc_kernel_launches() - l0
+    t_step = sum(step_times) / len(step_times)
+    if dist is not None:
+        tt = torch.tensor([t_step], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step = float(tt.item())
+    inter = w.interactions
+    value = inter * world / t_step
+
+    # --- dominant kernel alone (generate = prep + rs kernel) for the roofline
+    gen_rs = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_RS, 0, field.data_ptr(), sp), 3)
+    t_rs = sum(gen_rs) / len(gen_rs)
+    gen_fr = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_FRESNEL, 0, field.data_ptr(), sp),
+                   max(3, args.steps // 2))
+    t_fr = sum(gen_fr) / len(gen_fr)
+
+    # --- end to end through the host-facing ABI ------------------------------
+    hv = torch.from_numpy(w.vertices).pin_memory()
+    hfield = torch.empty((nch, pny, pnx, 2), dtype=torch.float64).pin_memory()
+    hcodes = torch.empty((nch, npx), dtype=torch.uint8).pin_memory()
+    dv2 = torch.empty_like(dv)
+
+    def e2e_step():
+        dv2.copy_(hv, non_blocking=True)
+        ctx.generate(cfg, dv2.data_ptr(), w.n_points, oph.DIFF_RS, 0, field.data_ptr(), sp)
+        ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
+        hfield.copy_(field, non_blocking=True)
+        hcodes.copy_(codes, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e2e_times = timed(e2e_step, max(3, args.steps // 2))
+    t_e2e = sum(e2e_times) / len(e2e_times)
+    e2e_value = inter * world / t_e2e
+    h2d = hv.numel() * 8
+    d2h = hfield.numel() * 8 + hcodes.numel()
+
+    clocks = clk.summary()
+    sm_mhz = clocks["sm_mhz"] or 1995.0
+    props = torch.cuda.get_device_properties(local)
+    sms = props.multi_processor_count
+    # SFU roofline: every interaction needs one sin and one cos (2 MUFU ops);
+    # 16 MUFU results per clock per SM.
+    peak_rs = sms * 16 / 2 * sm_mhz * 1e6
+    achieved_rs = inter / t_rs
+
+    line = None
+    if rank == 0:
+        cpu = None
+        rel = None
+        if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
+            # cpu_baseline leg: the CPU point-cloud path on a bounded sample of
+            # the same workload, and the GPU result on that sample checked
+            # against it (relative L2 error, FP64 CPU result as reference).
+            n_cpu = args.cpu_points or 300
+            rate, secs, kind, ref_field = cpu_sample_run(w, n_cpu, 0)
+            sub = w.subset(n_cpu)
+            dsub = torch.from_numpy(sub.vertices).cuda()
+            fsub = torch.empty_like(field)
+            ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, 0, fsub.data_ptr(), sp)
+            torch.cuda.synchronize()
+            g = fsub.cpu().numpy()
+            got = g[..., 0] + 1j * g[..., 1]
+            rel = float(np.linalg.norm(got - ref_field) / np.linalg.norm(ref_field))
+            cpu = {"value": rate, "unit": UNIT, "cores": host_cores(), "kind": kind,
+                   "sample": f"{n_cpu} of {w.n_points} points at full {w.pnx}x{w.pny}, {w.n_channels} channels, RS "
+                             f"({secs:.1f} s, OpenMP, {cpu_model()})",
+                   "relL2_gpu_vs_cpu_on_sample": rel}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": w.name, "pnx": pnx, "pny": pny, "pixel_pitch_m": w.pp,
+                       "wavelengths_m": list(w.wavelengths), "n_points": w.n_points, "diff": "RS",
+                       "step": "generateHologram(RS, 3 channels) + phase encode + normalise",
+                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
+            "relL2": rel,
+            "roofline": {"bound": "sfu", "kernel": "rs_kernel", "achieved": achieved_rs, "peak": peak_rs,
+                         "unit": "interactions/s", "frac": achieved_rs / peak_rs, "traffic": None,
+                         "peak_basis": f"{sms} SMs x 16 MUFU/clk / 2 MUFU (sin, cos) per interaction x "
+                                       f"{sm_mhz:.0f} MHz median SM clock under load"},
+            "fresnel": {"value": inter * world / t_fr, "unit": UNIT, "ms_per_generate": t_fr * 1e3,
+                        "kernel": "fresnel_kernel (FP32 cores, separable)"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": t_e2e * 1e3},
+            "gpu_launches": int(launches),
+            "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"],
+                       "reasons": clocks["reasons"], "samples": clocks["samples"]},
+            "wall_s_timed_region": wall,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    ctx.close()
+    return line
+
+
+def main():
+    args = parse()
+    from openholo_gb300 import workloads
+    w = workloads.BY_NAME[args.workload]()
+    if args.impl == "reference":
+        reference_arm(args, w)
+    else:
+        gpu_arm(args, w)
+
+
+if __name__ == "__main__":
+    main()

@@ -96,6 +96,10 @@ typedef struct ophpc_context ophpc_context;
 /* Version of this header's ABI. */
 int32_t ophpc_api_version(void);
 
+/* Number of CUDA kernels this library has launched since it was loaded
+ * (instrumentation; no reference counterpart). */
+uint64_t ophpc_kernel_launches(void);
+
 /* Human-readable text of a status code (static storage). */
 const char* ophpc_status_string(ophpc_status status);
 
@@ -137,6 +141,12 @@ ophpc_status ophpc_generate_host(ophpc_context* ctx, const ophpc_config* cfg,
 ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_channels,
                           uint64_t n_pixels, uint32_t encode_flag, double* d_encoded,
                           uint8_t* d_normalized, void* stream);
+
+/* ophGen::normalize alone on device: min/max over all channels of
+ * d_encoded ([n_channels][n_pixels] doubles) and the 8-bit codes into
+ * d_normalized. Asynchronous on `stream`. */
+ophpc_status ophpc_normalize(ophpc_context* ctx, const double* d_encoded, uint32_t n_channels,
+                             uint64_t n_pixels, uint8_t* d_normalized, void* stream);
 
 #ifdef __cplusplus
 }

@@ -79,6 +79,7 @@ def lib_path() -> str:
 def _declare(L: ctypes.CDLL) -> None:
     vp, u32, u64, i32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int32
     L.ophpc_api_version.restype = i32
+    L.ophpc_kernel_launches.restype = u64
     L.ophpc_status_string.argtypes = [ctypes.c_int]
     L.ophpc_status_string.restype = ctypes.c_char_p
     L.ophpc_last_error.argtypes = [vp]

@@ -12,6 +12,7 @@
 #include "pc_common.cuh"
 #include "pc_tc.cuh"
 
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -20,6 +21,12 @@
 #include <string>
 
 using namespace ophpc;
+
+namespace ophpc {
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace ophpc
 
 struct ophpc_context {
     int device = 0;
@@ -224,6 +231,8 @@ extern "C" {
 
 int32_t ophpc_api_version(void) { return OPHPC_API_VERSION; }
 
+uint64_t ophpc_kernel_launches(void) { return launches_so_far(); }
+
 const char* ophpc_status_string(ophpc_status st) {
     switch (st) {
         case OPHPC_SUCCESS: return "success";
@@ -395,6 +404,30 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
     e = cudaGetLastError();
     cudaFreeAsync(d_mm, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "encode launch");
+    return OPHPC_SUCCESS;
+}
+
+ophpc_status ophpc_normalize(ophpc_context* ctx, const double* d_encoded, uint32_t n_channels, uint64_t n_pixels,
+                             uint8_t* d_normalized, void* stream) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    if (n_channels < 1 || n_channels > OPHPC_MAX_CHANNELS)
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "n_channels must be 1..3");
+    if (n_pixels == 0) return OPHPC_SUCCESS;
+    DeviceGuard guard(ctx->device);
+    if (!d_encoded || !is_device_ptr(d_encoded))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded must be device memory");
+    if (!d_normalized || !is_device_ptr(d_normalized))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_normalized must be device memory");
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long* d_mm = nullptr;
+    cudaError_t e = pool_alloc(ctx, &d_mm, 2 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation (min/max)");
+    launch_normalize(d_encoded, (int)n_channels, (int64_t)n_pixels, d_normalized, d_mm, s);
+    e = cudaGetLastError();
+    cudaFreeAsync(d_mm, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "normalize launch");
     return OPHPC_SUCCESS;
 }
 

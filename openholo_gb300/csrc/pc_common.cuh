@@ -71,6 +71,11 @@ __device__ __forceinline__ float reduce_turns(float t) {
     return __fsub_rn(t, r);
 }
 
+// Count of kernels this library has launched (all contexts, all threads);
+// read through ophpc_kernel_launches().
+void count_launches(unsigned n);
+uint64_t launches_so_far();
+
 // Launchers (defined in the .cu files).
 void launch_prep(const void* d_vertices, int64_t n_points, const double* scale, double distance,
                  double field_length, int viewing_window, int diff_flag, const JobGeom& jg,
@@ -84,6 +89,8 @@ void launch_sum_partials(const JobGeom& jg, double2* d_field, const double2* d_p
 void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int encode_flag,
                    double* d_encoded, uint8_t* d_normalized, unsigned long long* d_minmax,
                    cudaStream_t stream);
+void launch_normalize(const double* d_encoded, int n_channels, int64_t n_pixels, uint8_t* d_normalized,
+                      unsigned long long* d_minmax, cudaStream_t stream);
 int rs_blocks_per_sm();
 int fresnel_blocks_per_sm();
 

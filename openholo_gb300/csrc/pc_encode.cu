@@ -82,6 +82,38 @@ __global__ void __launch_bounds__(256) encode_minmax_kernel(const double2* __res
     }
 }
 
+// min/max of an already encoded buffer (normalize() on its own)
+__global__ void __launch_bounds__(256) minmax_kernel(const double* __restrict__ encoded, int64_t n,
+                                                     unsigned long long* __restrict__ minmax) {
+    double mn = kMaxDouble, mx = kMinDouble;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double e = encoded[i];
+        if (e < mn) mn = e;
+        if (e > mx) mx = e;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    __shared__ double s_mn[8], s_mx[8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_mn[w] = mn;
+        s_mx[w] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            mn = fmin(mn, s_mn[k]);
+            mx = fmax(mx, s_mx[k]);
+        }
+        atomicMin(&minmax[0], ordered_bits(mn));
+        atomicMax(&minmax[1], ordered_bits(mx));
+    }
+}
+
 __device__ __forceinline__ double from_ordered(unsigned long long b) {
     b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
     return __longlong_as_double((long long)b);
@@ -111,17 +143,34 @@ __global__ void init_minmax_kernel(unsigned long long* minmax) {
 
 }  // namespace
 
+namespace {
+int grid_for(int64_t n, int threads) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t want = (n + threads - 1) / threads;
+    return (int)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
+}
+}  // namespace
+
+void launch_normalize(const double* d_encoded, int n_channels, int64_t n_pixels, uint8_t* d_normalized,
+                      unsigned long long* d_minmax, cudaStream_t stream) {
+    const int64_t n = (int64_t)n_channels * n_pixels;
+    if (n <= 0) return;
+    const int threads = 256, blocks = grid_for(n, threads);
+    count_launches(3);
+    init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
+    minmax_kernel<<<blocks, threads, 0, stream>>>(d_encoded, n, d_minmax);
+    normalize_kernel<<<blocks, threads, 0, stream>>>(nullptr, d_encoded, n, 0, d_minmax, d_normalized);
+}
+
 void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int encode_flag,
                    double* d_encoded, uint8_t* d_normalized, unsigned long long* d_minmax,
                    cudaStream_t stream) {
     const int64_t n = (int64_t)n_channels * n_pixels;
     if (n <= 0) return;
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int threads = 256;
-    int64_t want = (n + threads - 1) / threads;
-    const int blocks = (int)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
+    const int threads = 256, blocks = grid_for(n, threads);
+    count_launches(d_normalized ? 3 : 2);
     init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
     encode_minmax_kernel<<<blocks, threads, 0, stream>>>(d_field, n, encode_flag, d_encoded, d_minmax);
     if (d_normalized)

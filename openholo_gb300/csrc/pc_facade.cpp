@@ -1,0 +1,424 @@
+// ophPointCloud façade (include/ophPointCloud.h) and its C ABI
+// (include/ophpc_pointcloud.h).
+//
+// Mirrors the reference object's state and call sequence
+// (ophgen/src/ophPointCloud.cpp, ophgen/src/ophGen.cpp:146-219,654-849):
+// host buffers complex_H / m_lpEncoded / m_lpNormalized per channel, filled
+// by generateHologram / encoding / normalize; the arithmetic runs in
+// libophpc's kernels. Every call that reads a host buffer uploads it first,
+// so a caller that edits getComplexField() or getEncodedBuffer() between
+// calls sees the same result as with the reference.
+#include "ophPointCloud.h"
+#include "ophpc_pointcloud.h"
+
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#define OPH_LOG(...) std::printf(__VA_ARGS__)
+
+namespace {
+constexpr double kPi = 3.14159265358979323846;
+}
+
+ophPointCloud::ophPointCloud(void) { context_.wave_length = wave_length_; }
+
+ophPointCloud::ophPointCloud(const char* pc_file, const char* cfg_file) : ophPointCloud() {
+    if (loadPointCloud(pc_file) == -1) OPH_LOG("<FAILED> Load point cloud data file('%s')", pc_file);
+    if (!readConfig(cfg_file)) OPH_LOG("<FAILED> Load config specification data file('%s')", cfg_file);
+}
+
+ophPointCloud::~ophPointCloud(void) {
+    freeBuffers();
+    delete[] vertices_;
+    vertices_ = nullptr;
+    if (d_vertices_) cudaFree(d_vertices_);
+    if (d_field_) cudaFree(d_field_);
+    if (d_encoded_) cudaFree(d_encoded_);
+    if (d_codes_) cudaFree(d_codes_);
+    if (gpu_) ophpc_destroy(gpu_);
+}
+
+void ophPointCloud::release(void) { delete this; }
+
+void ophPointCloud::freeBuffers() {
+    for (uint c = 0; c < n_old_channels_; ++c) {
+        if (complex_H_) delete[] complex_H_[c];
+        if (encoded_) delete[] encoded_[c];
+        if (normalized_) delete[] normalized_[c];
+    }
+    delete[] complex_H_;
+    delete[] encoded_;
+    delete[] normalized_;
+    complex_H_ = nullptr;
+    encoded_ = nullptr;
+    normalized_ = nullptr;
+    n_old_channels_ = 0;
+    buffer_pixels_ = 0;
+}
+
+bool ophPointCloud::initialize() {
+    freeBuffers();
+    const uint nch = context_.waveNum;
+    const long long n = (long long)context_.pixel_number[_X] * context_.pixel_number[_Y];
+    if (nch < 1 || nch > OPHPC_MAX_CHANNELS || n <= 0) return false;
+    complex_H_ = new Complex<Real>*[nch];
+    encoded_ = new Real*[nch];
+    normalized_ = new uchar*[nch];
+    for (uint c = 0; c < nch; ++c) {
+        complex_H_[c] = new Complex<Real>[n];
+        encoded_[c] = new Real[n]();
+        normalized_[c] = new uchar[n]();
+    }
+    n_old_channels_ = nch;
+    buffer_pixels_ = n;
+    return true;
+}
+
+void ophPointCloud::setPixelNumber(int nx, int ny) {
+    context_.pixel_number[_X] = nx;
+    context_.pixel_number[_Y] = ny;
+    context_.ss[_X] = nx * context_.pixel_pitch[_X];
+    context_.ss[_Y] = ny * context_.pixel_pitch[_Y];
+    initialize();
+}
+
+void ophPointCloud::setPixelPitch(Real px, Real py) {
+    context_.pixel_pitch[_X] = px;
+    context_.pixel_pitch[_Y] = py;
+    context_.ss[_X] = context_.pixel_number[_X] * px;
+    context_.ss[_Y] = context_.pixel_number[_Y] * py;
+}
+
+void ophPointCloud::setWaveNum(uint n) {
+    context_.waveNum = n > OPHPC_MAX_CHANNELS ? OPHPC_MAX_CHANNELS : n;
+    initialize();
+}
+
+void ophPointCloud::setWaveLength(Real w, uint idx) {
+    if (idx < OPHPC_MAX_CHANNELS) wave_length_[idx] = w;
+}
+
+bool ophPointCloud::readConfig(const char* cfg_file) {
+    ophpc_config c;
+    ophpc_image_config img;
+    std::memset(&img, 0, sizeof(img));
+    const ophpc_status st = ophpc_read_config(cfg_file, &c, &img);
+    if (st == OPHPC_ERROR_IO || st == OPHPC_ERROR_INVALID_ARGUMENT) {
+        OPH_LOG("<FAILED> Loading file\n");
+        last_error_ = "cannot read config file";
+        return false;
+    }
+    context_.waveNum = c.n_channels;
+    for (uint i = 0; i < OPHPC_MAX_CHANNELS; ++i) wave_length_[i] = c.wave_length[i];
+    context_.pixel_number[_X] = c.pixel_number[0];
+    context_.pixel_number[_Y] = c.pixel_number[1];
+    context_.pixel_pitch[_X] = c.pixel_pitch[0];
+    context_.pixel_pitch[_Y] = c.pixel_pitch[1];
+    context_.ss[_X] = context_.pixel_number[_X] * context_.pixel_pitch[_X];
+    context_.ss[_Y] = context_.pixel_number[_Y] * context_.pixel_pitch[_Y];
+    context_.bUseDP = img.double_precision != 0;
+    for (int i = 0; i < 3; ++i) context_.shift[i] = img.shift[i];
+    img_ = img;
+    field_length_ = c.field_length;
+    scale_[0] = c.scale[0];
+    scale_[1] = c.scale[1];
+    scale_[2] = c.scale[2];
+    distance_ = c.distance;
+    if (st != OPHPC_SUCCESS) {
+        last_error_ = "config key missing or malformed";
+        // the reference initialises only once the common keys were read
+        if (c.pixel_number[0] > 0 && c.pixel_number[1] > 0 && c.pixel_pitch[0] > 0 && c.pixel_pitch[1] > 0)
+            initialize();
+        return false;
+    }
+    if (!initialize()) {
+        last_error_ = "invalid pixel number or channel count";
+        return false;
+    }
+    return true;
+}
+
+int ophPointCloud::loadPointCloud(const char* pc_file) {
+    const int64_t n = ophpc_load_ply(pc_file, nullptr, 0);
+    if (n < 0) {
+        OPH_LOG("<FAILED> Loading ply file.\n");
+        last_error_ = "cannot load point cloud";
+        return -1;
+    }
+    delete[] vertices_;
+    vertices_ = new Vertex[n > 0 ? n : 1];
+    ophpc_load_ply(pc_file, reinterpret_cast<ophpc_vertex*>(vertices_), (uint64_t)n);
+    n_points_ = (ulonglong)n;
+    return (int)n;
+}
+
+void ophPointCloud::setPointCloudModel(Vertex* vertex) {
+    if (n_points_ < 1 || !vertex) return;
+    delete[] vertices_;
+    vertices_ = new Vertex[n_points_];
+    std::memcpy(vertices_, vertex, sizeof(Vertex) * n_points_);
+}
+
+void ophPointCloud::fillConfig(ophpc_config* c) const {
+    std::memset(c, 0, sizeof(*c));
+    c->pixel_number[0] = context_.pixel_number[_X];
+    c->pixel_number[1] = context_.pixel_number[_Y];
+    c->offset[0] = context_.offset[_X];
+    c->offset[1] = context_.offset[_Y];
+    c->pixel_pitch[0] = context_.pixel_pitch[_X];
+    c->pixel_pitch[1] = context_.pixel_pitch[_Y];
+    for (int i = 0; i < 3; ++i) c->scale[i] = scale_[i];
+    c->distance = distance_;
+    c->field_length = field_length_;
+    c->viewing_window = viewing_window_ ? 1 : 0;
+    c->n_channels = context_.waveNum;
+    for (uint i = 0; i < OPHPC_MAX_CHANNELS; ++i) c->wave_length[i] = wave_length_[i];
+}
+
+bool ophPointCloud::ensureGpu() {
+    if (gpu_) return true;
+    const ophpc_status st = ophpc_create(0, &gpu_);
+    if (st != OPHPC_SUCCESS) {
+        gpu_ = nullptr;
+        last_error_ = std::string("no GPU context: ") + ophpc_status_string(st);
+        OPH_LOG("<FAILED> %s\n", last_error_.c_str());
+        return false;
+    }
+    return true;
+}
+
+bool ophPointCloud::ensureDevice(size_t bv, size_t bf, size_t be, size_t bc) {
+    auto grow = [&](void** p, size_t* cap, size_t want) {
+        if (want <= *cap) return true;
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        *cap = 0;
+        if (cudaMalloc(p, want) != cudaSuccess) {
+            cudaGetLastError();
+            *p = nullptr;
+            return false;
+        }
+        *cap = want;
+        return true;
+    };
+    if (!grow(&d_vertices_, &cap_v_, bv) || !grow(&d_field_, &cap_f_, bf) || !grow(&d_encoded_, &cap_e_, be) ||
+        !grow(&d_codes_, &cap_c_, bc)) {
+        last_error_ = "device allocation failed";
+        return false;
+    }
+    return true;
+}
+
+Real ophPointCloud::generateHologram(uint diff_flag) {
+    const auto begin = std::chrono::steady_clock::now();
+    if (diff_flag != PC_DIFF_RS && diff_flag != PC_DIFF_FRESNEL) {
+        OPH_LOG("<FAILED> Wrong parameters.");
+        return 0.0;
+    }
+    if (!complex_H_) {
+        last_error_ = "readConfig must succeed before generateHologram";
+        return 0.0;
+    }
+    // resetBuffer (ophGen.cpp:801-814)
+    for (uint c = 0; c < context_.waveNum; ++c) {
+        std::memset(encoded_[c], 0, sizeof(Real) * buffer_pixels_);
+        std::memset(normalized_[c], 0, (size_t)buffer_pixels_);
+    }
+    encoded_valid_ = false;
+    if (!ensureGpu()) return 0.0;
+    if (n_points_ > 0 && !vertices_) {
+        last_error_ = "no point cloud";
+        return 0.0;
+    }
+    ophpc_config c;
+    fillConfig(&c);
+    const size_t plane = (size_t)buffer_pixels_;
+    const uint nch = context_.waveNum;
+    if (!ensureDevice(sizeof(Vertex) * (n_points_ ? n_points_ : 1), sizeof(double) * 2 * plane * nch,
+                      sizeof(double) * plane * nch, plane * nch))
+        return 0.0;
+    if (n_points_ && cudaMemcpy(d_vertices_, vertices_, sizeof(Vertex) * n_points_, cudaMemcpyHostToDevice) != cudaSuccess) {
+        last_error_ = "vertex upload failed";
+        return 0.0;
+    }
+    const ophpc_status st = ophpc_generate(gpu_, &c, reinterpret_cast<const ophpc_vertex*>(d_vertices_), n_points_,
+                                           diff_flag, mode_, (double*)d_field_, nullptr);
+    if (st != OPHPC_SUCCESS) {
+        last_error_ = std::string("generate: ") + ophpc_last_error(gpu_);
+        return 0.0;
+    }
+    for (uint ch = 0; ch < nch; ++ch) {
+        if (cudaMemcpy(complex_H_[ch], (double*)d_field_ + 2 * plane * ch, sizeof(double) * 2 * plane,
+                       cudaMemcpyDeviceToHost) != cudaSuccess) {
+            last_error_ = "field download failed";
+            return 0.0;
+        }
+    }
+    context_.k = (2 * kPi) / wave_length_[nch - 1];
+    progress_ = 0;
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - begin).count();
+}
+
+void ophPointCloud::encoding(unsigned int flag) {
+    if (flag > ENCODE_IMAGINARY) {
+        OPH_LOG("<FAILED> WRONG PARAMETERS.\n");
+        return;
+    }
+    if (!complex_H_ || !ensureGpu()) return;
+    const size_t plane = (size_t)buffer_pixels_;
+    const uint nch = context_.waveNum;
+    if (!ensureDevice(cap_v_ ? cap_v_ : 1, sizeof(double) * 2 * plane * nch, sizeof(double) * plane * nch, plane * nch))
+        return;
+    for (uint ch = 0; ch < nch; ++ch)
+        cudaMemcpy((double*)d_field_ + 2 * plane * ch, complex_H_[ch], sizeof(double) * 2 * plane, cudaMemcpyHostToDevice);
+    if (ophpc_encode(gpu_, (const double*)d_field_, nch, plane, flag, (double*)d_encoded_, nullptr, nullptr) !=
+        OPHPC_SUCCESS) {
+        last_error_ = std::string("encode: ") + ophpc_last_error(gpu_);
+        return;
+    }
+    for (uint ch = 0; ch < nch; ++ch)
+        cudaMemcpy(encoded_[ch], (double*)d_encoded_ + plane * ch, sizeof(double) * plane, cudaMemcpyDeviceToHost);
+    encoded_valid_ = true;
+}
+
+void ophPointCloud::normalize(void) {
+    if (!encoded_ || !ensureGpu()) return;
+    const size_t plane = (size_t)buffer_pixels_;
+    const uint nch = context_.waveNum;
+    if (!ensureDevice(cap_v_ ? cap_v_ : 1, cap_f_ ? cap_f_ : 1, sizeof(double) * plane * nch, plane * nch)) return;
+    for (uint ch = 0; ch < nch; ++ch)
+        cudaMemcpy((double*)d_encoded_ + plane * ch, encoded_[ch], sizeof(double) * plane, cudaMemcpyHostToDevice);
+    if (ophpc_normalize(gpu_, (const double*)d_encoded_, nch, plane, (uint8_t*)d_codes_, nullptr) != OPHPC_SUCCESS) {
+        last_error_ = std::string("normalize: ") + ophpc_last_error(gpu_);
+        return;
+    }
+    for (uint ch = 0; ch < nch; ++ch)
+        cudaMemcpy(normalized_[ch], (uint8_t*)d_codes_ + plane * ch, plane, cudaMemcpyDeviceToHost);
+}
+
+bool ophPointCloud::save(const char* fname, uint8_t bitsperpixel, uchar* src, uint px, uint py) {
+    if (fname == nullptr) return false;
+    int w = (int)px, h = (int)py;
+    if (px == 0 && py == 0) {
+        w = context_.pixel_number[_X];
+        h = context_.pixel_number[_Y];
+    }
+    // ophGen::save (ophgen/src/ophGen.cpp:689-769): '\\' -> '/', ".bmp"
+    // appended when the path has no '.'
+    std::string file = fname;
+    for (auto& ch : file)
+        if (ch == '\\') ch = '/';
+    const size_t slash = file.find_last_of('/');
+    const std::string dir = slash == std::string::npos ? "" : file.substr(0, slash + 1);
+    std::string name = slash == std::string::npos ? file : file.substr(slash + 1);
+    if (file.rfind('.') == std::string::npos) name += ".bmp";
+    const std::string full = dir + name;
+    if (src) return ophpc_save_bmp(full.c_str(), src, w, h, bitsperpixel, img_.flip, img_.rotate) == OPHPC_SUCCESS;
+    if (!normalized_) return false;
+    const uint nch = context_.waveNum;
+    if (nch == 1)
+        return ophpc_save_bmp(full.c_str(), normalized_[0], w, h, 8, img_.flip, img_.rotate) == OPHPC_SUCCESS;
+    if (nch != 3) return false;
+    if (img_.merge) {
+        // mergeColor (Openholo/src/Openholo.cpp:103-117): channel i -> byte 2-i
+        std::vector<uint8_t> rgb((size_t)w * h * 3);
+        for (uint c = 0; c < 3; ++c)
+            for (size_t i = 0; i < (size_t)w * h; ++i) rgb[i * 3 + (2 - c)] = normalized_[c][i];
+        return ophpc_save_bmp(full.c_str(), rgb.data(), w, h, 24, img_.flip, img_.rotate) == OPHPC_SUCCESS;
+    }
+    bool ok = true;
+    for (uint c = 0; c < 3; ++c) {
+        const std::string path = dir + std::to_string(c) + "_" + name;
+        ok = ophpc_save_bmp(path.c_str(), normalized_[c], w, h, 8, img_.flip, img_.rotate) == OPHPC_SUCCESS && ok;
+    }
+    return ok;
+}
+
+// ------------------------------------------------------------------ C ABI
+
+struct ophpc_pc {
+    ophPointCloud* obj;
+};
+
+extern "C" {
+
+ophpc_pc* ophpc_pc_create(void) {
+    auto* h = new (std::nothrow) ophpc_pc;
+    if (!h) return nullptr;
+    h->obj = new (std::nothrow) ophPointCloud();
+    if (!h->obj) {
+        delete h;
+        return nullptr;
+    }
+    return h;
+}
+
+void ophpc_pc_release(ophpc_pc* h) {
+    if (!h) return;
+    h->obj->release();
+    delete h;
+}
+
+int32_t ophpc_pc_read_config(ophpc_pc* h, const char* path) { return h && h->obj->readConfig(path) ? 1 : 0; }
+
+int64_t ophpc_pc_load_point_cloud(ophpc_pc* h, const char* path) { return h ? h->obj->loadPointCloud(path) : -1; }
+
+void ophpc_pc_set_point_cloud(ophpc_pc* h, const ophpc_vertex* v, uint64_t n) {
+    if (!h) return;
+    h->obj->setNumberOfPoints(n);
+    h->obj->setPointCloudModel(reinterpret_cast<Vertex*>(const_cast<ophpc_vertex*>(v)));
+}
+
+void ophpc_pc_set_mode(ophpc_pc* h, uint32_t mode) { if (h) h->obj->SetMode(mode); }
+void ophpc_pc_set_viewing_window(ophpc_pc* h, int32_t on) { if (h) h->obj->setViewingWindow(on != 0); }
+void ophpc_pc_set_scale(ophpc_pc* h, double sx, double sy, double sz) { if (h) h->obj->setScale(sx, sy, sz); }
+void ophpc_pc_set_distance(ophpc_pc* h, double d) { if (h) h->obj->setDistance(d); }
+void ophpc_pc_set_offset(ophpc_pc* h, int32_t ox, int32_t oy) { if (h) h->obj->setOffset(ox, oy); }
+
+double ophpc_pc_generate_hologram(ophpc_pc* h, uint32_t diff_flag) {
+    return h ? h->obj->generateHologram(diff_flag) : 0.0;
+}
+
+void ophpc_pc_encoding(ophpc_pc* h, uint32_t flag) { if (h) h->obj->encoding(flag); }
+void ophpc_pc_normalize(ophpc_pc* h) { if (h) h->obj->normalize(); }
+
+int32_t ophpc_pc_save(ophpc_pc* h, const char* path, uint8_t bits_per_pixel) {
+    return h && h->obj->save(path, bits_per_pixel) ? 1 : 0;
+}
+
+int32_t ophpc_pc_get_config(ophpc_pc* h, ophpc_config* out) {
+    if (!h || !out) return 0;
+    h->obj->fillConfig(out);
+    return 1;
+}
+
+uint64_t ophpc_pc_number_of_points(ophpc_pc* h) { return h ? h->obj->getNumberOfPoints() : 0; }
+
+const ophpc_vertex* ophpc_pc_point_cloud(ophpc_pc* h) {
+    return h ? reinterpret_cast<const ophpc_vertex*>(h->obj->getPointCloudModel()) : nullptr;
+}
+
+const double* ophpc_pc_complex_field(ophpc_pc* h, uint32_t ch) {
+    if (!h || !h->obj->getComplexField() || ch >= h->obj->getContext().waveNum) return nullptr;
+    return reinterpret_cast<const double*>(h->obj->getComplexField()[ch]);
+}
+
+const double* ophpc_pc_encoded(ophpc_pc* h, uint32_t ch) {
+    if (!h || !h->obj->getEncodedBuffer() || ch >= h->obj->getContext().waveNum) return nullptr;
+    return h->obj->getEncodedBuffer()[ch];
+}
+
+const uint8_t* ophpc_pc_normalized(ophpc_pc* h, uint32_t ch) {
+    if (!h || !h->obj->getNormalizedBuffer() || ch >= h->obj->getContext().waveNum) return nullptr;
+    return h->obj->getNormalizedBuffer()[ch];
+}
+
+const char* ophpc_pc_last_error(ophpc_pc* h) { return h ? h->obj->lastError() : ""; }
+
+}  // extern "C"

@@ -219,6 +219,7 @@ int fresnel_blocks_per_sm() {
 void launch_fresnel(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
                     cudaStream_t stream) {
     dim3 grid((unsigned)jg.tiles_x, (unsigned)jg.tiles_y, (unsigned)(jg.n_channels * jg.ksplit));
+    count_launches(1);
     fresnel_kernel<<<grid, kThreads, kFresnelSmem, stream>>>(d_recs, jg, d_field, d_partials);
 }
 
@@ -227,6 +228,7 @@ void launch_sum_partials(const JobGeom& jg, double2* d_field, const double2* d_p
     if (jg.ksplit <= 1) return;
     const int64_t n = (int64_t)jg.n_channels * jg.ch[0].pnX * (int64_t)jg.ch[0].pnY;
     const int threads = 256;
+    count_launches(1);
     sum_partials_kernel<<<(unsigned)((n + threads - 1) / threads), threads, 0, stream>>>(
         d_field, d_partials, n, jg.ksplit - 1);
 }

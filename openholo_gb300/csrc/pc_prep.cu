@@ -111,6 +111,7 @@ void launch_prep(const void* d_vertices, int64_t n_points, const double* scale, 
     a.viewing_window = viewing_window;
     a.diff_flag = diff_flag;
     dim3 grid((unsigned)((n_points + 255) / 256), (unsigned)jg.n_channels);
+    count_launches(1);
     prep_points_kernel<<<grid, 256, 0, stream>>>((const double*)d_vertices, n_points, a, jg, d_recs);
 }
 

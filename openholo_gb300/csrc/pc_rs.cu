@@ -326,6 +326,7 @@ int rs_blocks_per_sm() {
 void launch_rs(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
                cudaStream_t stream) {
     dim3 grid((unsigned)jg.tiles_x, (unsigned)jg.tiles_y, (unsigned)(jg.n_channels * jg.ksplit));
+    count_launches(1);
     rs_kernel<<<grid, kThreads, kRsSmem, stream>>>(d_recs, jg, d_field, d_partials);
 }
 

@@ -224,20 +224,57 @@ def _load_ref():
             lib.ophref_query.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
                                          ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
             lib.ophref_query.restype = ctypes.c_int
+            lib.ophref_run_save.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_uint,
+                                            ctypes.c_uint, ctypes.c_char_p, ctypes.c_int]
+            lib.ophref_run_save.restype = ctypes.c_int
             lib.ophref_load_ply.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong]
             lib.ophref_load_ply.restype = ctypes.c_longlong
             _ref = lib
     return _ref
 
 
+class _QuietStdout:
+    """Silences the reference's printf logging (LOG, Openholo/src/sys.h) by
+    pointing file descriptor 1 at /dev/null for the duration of a call."""
+
+    def __enter__(self):
+        import sys
+        sys.stdout.flush()
+        self._libc = ctypes.CDLL(None)
+        self._saved = os.dup(1)
+        self._null = os.open(os.devnull, os.O_WRONLY)
+        os.dup2(self._null, 1)
+        return self
+
+    def __exit__(self, *a):
+        self._libc.fflush(None)
+        os.dup2(self._saved, 1)
+        os.close(self._saved)
+        os.close(self._null)
+
+
 def ref_load_ply(path: str) -> np.ndarray:
     lib = _load_ref()
-    n = lib.ophref_load_ply(path.encode(), None, 0)
+    with _QuietStdout():
+        n = lib.ophref_load_ply(path.encode(), None, 0)
     if n < 0:
         raise ValueError(f"reference PLYparser failed on {path}")
     out = np.zeros((n, 7), dtype=np.float64)
-    lib.ophref_load_ply(path.encode(), out.ctypes.data, n)
+    with _QuietStdout():
+        lib.ophref_load_ply(path.encode(), out.ctypes.data, n)
     return out
+
+
+def ref_run_save(xml_path: str, vertices: np.ndarray, diff_flag: int, encode_flag: int, bmp_path: str,
+                 bits_per_pixel: int = 8) -> None:
+    """Reference generate -> encoding -> normalize -> save(bmp_path)."""
+    lib = _load_ref()
+    v = _vertices(vertices)
+    with _QuietStdout():
+        rc = lib.ophref_run_save(xml_path.encode(), v.ctypes.data, v.shape[0], diff_flag, encode_flag,
+                                 bmp_path.encode(), bits_per_pixel)
+    if rc != 0:
+        raise RuntimeError(f"ophref_run_save failed ({rc})")
 
 
 def ref_run(xml_path: str, vertices: Optional[np.ndarray] = None, ply_path: Optional[str] = None,
@@ -247,7 +284,9 @@ def ref_run(xml_path: str, vertices: Optional[np.ndarray] = None, ply_path: Opti
     returns both stacked on a leading axis."""
     lib = _load_ref()
     pnx, pny, nch = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    if lib.ophref_query(xml_path.encode(), ctypes.byref(pnx), ctypes.byref(pny), ctypes.byref(nch)) != 0:
+    with _QuietStdout():
+        q = lib.ophref_query(xml_path.encode(), ctypes.byref(pnx), ctypes.byref(pny), ctypes.byref(nch))
+    if q != 0:
         raise ValueError(f"reference readConfig failed on {xml_path}")
     shape = (nch.value, pny.value, pnx.value)
     field = np.zeros(shape + (2,), dtype=np.float64)
@@ -260,10 +299,11 @@ def ref_run(xml_path: str, vertices: Optional[np.ndarray] = None, ply_path: Opti
     if ply_path is None:
         v = _vertices(vertices)
         n = v.shape[0]
-    rc = lib.ophref_run(xml_path.encode(), ply_path.encode() if ply_path else None,
-                        v.ctypes.data if v is not None else None, n, 1 if viewing_window else 0,
-                        diff_flag, encode_flag, field.ctypes.data, enc.ctypes.data, nrm.ctypes.data,
-                        ctypes.byref(secs))
+    with _QuietStdout():
+        rc = lib.ophref_run(xml_path.encode(), ply_path.encode() if ply_path else None,
+                            v.ctypes.data if v is not None else None, n, 1 if viewing_window else 0,
+                            diff_flag, encode_flag, field.ctypes.data, enc.ctypes.data, nrm.ctypes.data,
+                            ctypes.byref(secs))
     if rc != 0:
         raise RuntimeError(f"ophref_run failed ({rc})")
     if n_enc == 1:

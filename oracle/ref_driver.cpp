@@ -112,4 +112,22 @@ int ophref_run(const char* xml_path, const char* ply_path, const void* vertices,
     return 0;
 }
 
+// Runs the reference path (as ophref_run, phase encoding) and saves the
+// hologram through ophGen::save (ophgen/src/ophGen.cpp:689-769) with
+// `bits_per_pixel`. Returns 0 on success.
+int ophref_run_save(const char* xml_path, const void* vertices, unsigned long long n_points,
+                    unsigned diff_flag, unsigned encode_flag, const char* bmp_path, int bits_per_pixel)
+{
+    Holder h;
+    h.pc = new ophPointCloud();
+    if (!h.pc->readConfig(xml_path)) return -1;
+    h.pc->setNumberOfPoints(n_points);
+    h.pc->setPointCloudModel((Vertex*)vertices);
+    h.pc->SetMode(MODE_CPU);
+    h.pc->generateHologram(diff_flag);
+    h.pc->encoding(encode_flag == 1 ? ophGen::ENCODE_AMPLITUDE : ophGen::ENCODE_PHASE);
+    h.pc->normalize();
+    return h.pc->save(bmp_path, (uint8_t)bits_per_pixel) ? 0 : -3;
+}
+
 }  // extern "C"

@@ -158,6 +158,25 @@ def main():
                                              diff_flag=0, encode_flag=0)
         np.savez_compressed(os.path.join(HERE, "ply_generate_rs.npz"), field=field, codes_phase=codes_p,
                             xml=g.xml())
+        # BMP output of ophGen::save: one channel (row width a multiple of 4
+        # and not), and three channels merged into 24-bit BGR.
+        bmp_cases = {
+            "bmp_1ch_w96": (FIELD_CASES["rs_window_1ch"][0], FIELD_CASES["rs_window_1ch"][1], 8, {}),
+            "bmp_1ch_w90": (oracle.Geometry(pnx=90, pny=50, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                            box(120, (3e-4, 2e-4), (0.01, 0.03), 105), 8, {}),
+            "bmp_3ch_merge": (oracle.Geometry(pnx=80, pny=48, ppx=6.4e-6, ppy=7.1e-6,
+                                              wavelengths=[638e-9, 532e-9, 473e-9], scale=(0.5, 0.5, 2.0),
+                                              distance=0.05, extra_xml={"IMG_Merge": 1}),
+                              box(150, (1e-3, 1e-3), (0.05, 0.2), 106), 24, {}),
+        }
+        for name, (g, v, bpp, _) in bmp_cases.items():
+            with open(xml, "w") as f:
+                f.write(g.xml())
+            bmp = os.path.join(HERE, name + ".bmp")
+            oracle.ref_run_save(xml, v, 0, 0, bmp, bpp)
+            field, _, codes, _ = oracle.ref_run(xml, vertices=v, diff_flag=0, encode_flag=0)
+            np.savez_compressed(os.path.join(HERE, name + ".npz"), vertices=v, xml=g.xml(), bpp=bpp)
+            out[name] = os.path.getsize(bmp)
     for k, v in out.items():
         print(k, v)
 

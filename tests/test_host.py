@@ -1,0 +1,114 @@
+"""Host-side checks of the C ABI library (no compute calls, no GPU needed)."""
+import ctypes
+import glob
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import openholo_gb300 as oph
+from openholo_gb300 import pointcloud as P
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_c_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        # C declarations only: skip the C++ façade class header
+        if "class ophPointCloud" in text:
+            continue
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b((?:ophpc|cudaPointCloud|sum)_?\w*)\s*\(", text, re.M):
+            if not m.group(0).lstrip().startswith("#"):
+                names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol():
+    decl = _declared_c_functions()
+    assert len(decl) >= 20
+    out = subprocess.run(["nm", "-D", "--defined-only", oph.lib_path()], capture_output=True, text=True).stdout
+    exported = {ln.split()[-1] for ln in out.splitlines() if ln.strip()}
+    missing = [d for d in decl if d not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    L = oph.lib()
+    for d in decl:
+        getattr(L, d)   # resolvable through the loader too
+
+
+def test_abi_basics_without_compute():
+    L = oph.lib()
+    assert L.ophpc_api_version() == 1
+    assert L.ophpc_status_string(0) == b"success"
+    assert L.ophpc_status_string(10) == b"no CUDA device"
+    assert ctypes.sizeof(oph.OphpcConfig) == 2 * 4 + 2 * 4 + 2 * 8 + 3 * 8 + 8 + 8 + 4 + 4 + 3 * 8
+
+
+def test_null_context_is_rejected():
+    L = oph.lib()
+    cfg = oph.make_config(64, 64, 8e-6, 8e-6, [532e-9])
+    assert L.ophpc_generate(None, ctypes.byref(cfg), None, 0, 0, 0, None, None) == 1
+    assert L.ophpc_encode(None, None, 1, 1, 0, None, None, None) == 1
+    assert L.ophpc_destroy(None) == 1
+
+
+def _gpu_visible():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_gpu_visible(), reason="checks the no-GPU error path")
+def test_create_without_gpu_reports_no_device():
+    L = oph.lib()
+    h = ctypes.c_void_p()
+    assert L.ophpc_create(0, ctypes.byref(h)) == 10
+    with pytest.raises(oph.OphpcError):
+        oph.Context(0)
+
+
+@pytest.mark.skipif(_gpu_visible(), reason="checks the no-GPU error path")
+def test_facade_without_gpu_fails_loudly(tmp_path):
+    """No CPU fallback: generateHologram returns 0.0 and says why."""
+    x = tmp_path / "c.xml"
+    x.write_text("<PointCloud><ScaleX>1</ScaleX><ScaleY>1</ScaleY><ScaleZ>1</ScaleZ><Distance>0</Distance>"
+                 "<SLM_PixelPitchX>8e-6</SLM_PixelPitchX><SLM_PixelPitchY>8e-6</SLM_PixelPitchY>"
+                 "<SLM_PixelNumX>32</SLM_PixelNumX><SLM_PixelNumY>16</SLM_PixelNumY>"
+                 "<SLM_WaveNum>1</SLM_WaveNum><SLM_WaveLength_1>532e-9</SLM_WaveLength_1></PointCloud>")
+    with P.PointCloud() as h:
+        assert h.readConfig(str(x))
+        h.setPointCloudModel(np.array([[0, 0, 0.3, 1, 1, 1, 0]], dtype=np.float64))
+        assert h.getNumberOfPoints() == 1
+        assert h.generateHologram(0) == 0.0
+        assert "GPU" in h.lastError()
+
+
+def test_facade_config_and_model_state(tmp_path):
+    x = tmp_path / "c.xml"
+    x.write_text("<PointCloud><ScaleX>0.5</ScaleX><ScaleY>0.25</ScaleY><ScaleZ>2</ScaleZ><Distance>0.1</Distance>"
+                 "<SLM_PixelPitchX>8e-6</SLM_PixelPitchX><SLM_PixelPitchY>6e-6</SLM_PixelPitchY>"
+                 "<SLM_PixelNumX>40</SLM_PixelNumX><SLM_PixelNumY>24</SLM_PixelNumY>"
+                 "<SLM_WaveNum>2</SLM_WaveNum><SLM_WaveLength_1>532e-9</SLM_WaveLength_1>"
+                 "<SLM_WaveLength_2>638e-9</SLM_WaveLength_2></PointCloud>")
+    with P.PointCloud() as h:
+        assert h.readConfig(str(x))
+        c = h.getConfig()
+        assert (c.pixel_number[0], c.pixel_number[1], c.n_channels) == (40, 24, 2)
+        assert list(c.scale) == [0.5, 0.25, 2.0] and c.distance == 0.1
+        h.setScale(1, 2, 3)
+        h.setDistance(0.2)
+        h.setOffset(3, -1)
+        c = h.getConfig()
+        assert list(c.scale) == [1, 2, 3] and c.distance == 0.2 and list(c.offset) == [3, -1]
+        v = np.random.default_rng(0).normal(size=(10, 7))
+        h.setPointCloudModel(v)
+        assert np.array_equal(h.getPointCloudModel(), v)
+        assert h.getComplexField().shape == (2, 24, 40)
+        assert h.generateHologram(7) == 0.0    # bad flag -> 0.0, as the reference
+        assert not h.readConfig(str(tmp_path / "missing.xml"))

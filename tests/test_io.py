@@ -1,0 +1,152 @@
+"""Host-side files of the path (no GPU): PLY loader, XML config reader, BMP
+writer, each against what the reference itself produced (tests/golden/)."""
+import os
+import struct
+
+import numpy as np
+import pytest
+
+from openholo_gb300 import pointcloud as P
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.mark.parametrize("name", ["ply_ascii_channel", "ply_ascii_nochannel", "ply_binary_channel"])
+def test_ply_matches_reference_parser(name):
+    want = np.load(os.path.join(GOLD, "ply_vertices.npz"))[name]
+    got = P.load_ply(os.path.join(GOLD, name + ".ply"))
+    assert got.shape == want.shape
+    assert np.array_equal(got, want)
+
+
+def test_ply_appends_extension_and_fails_cleanly(tmp_path):
+    got = P.load_ply(os.path.join(GOLD, "ply_ascii_channel"))   # ".ply" appended
+    assert got.shape[0] == 64
+    with pytest.raises(Exception):
+        P.load_ply(str(tmp_path / "missing.ply"))
+    bad = tmp_path / "bad.ply"
+    bad.write_text("not a ply\n")
+    with pytest.raises(Exception):
+        P.load_ply(str(bad))
+
+
+def test_ply_big_endian_roundtrip(tmp_path):
+    """binary_big_endian is byte-swapped (the reference reads it unswapped)."""
+    n = 5
+    rng = np.random.default_rng(0)
+    xyz = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    rgb = rng.integers(0, 256, (n, 3))
+    hdr = ("ply\nformat binary_big_endian 1.0\nelement color 1\nproperty int channel\n"
+           f"element vertex {n}\nproperty float x\nproperty float y\nproperty float z\n"
+           "property uchar red\nproperty uchar green\nproperty uchar blue\nend_header\n")
+    p = tmp_path / "be.ply"
+    with open(p, "wb") as f:
+        f.write(hdr.encode())
+        f.write(struct.pack(">i", 3))
+        for i in range(n):
+            f.write(struct.pack(">fffBBB", *xyz[i], *[int(c) for c in rgb[i]]))
+    got = P.load_ply(str(p))
+    assert np.array_equal(got[:, :3], xyz.astype(np.float64))
+    assert np.array_equal(got[:, 3:6], (rgb.astype(np.float32) / np.float32(255.0)).astype(np.float64))
+
+
+def _write(tmp_path, name, text):
+    p = tmp_path / name
+    p.write_text(text)
+    return str(p)
+
+
+DICE_STYLE = """<PointCloud>
+  <!-- About points -->
+  <FieldLength>1000e-3</FieldLength> <!-- Double Type -->
+  <ScaleX>0.01</ScaleX> <!-- Double Type -->
+  <ScaleY>0.01</ScaleY>
+  <ScaleZ>0.01</ScaleZ>
+  <Distance>0.1</Distance>
+  <IMG_Rotation>0</IMG_Rotation>
+  <IMG_Merge>1</IMG_Merge>
+  <DoublePrecision>1</DoublePrecision>
+  <SLM_PixelPitchX>4.3e-6</SLM_PixelPitchX>
+  <SLM_PixelPitchY> 4.3e-6</SLM_PixelPitchY>
+  <SLM_PixelNumX>1920</SLM_PixelNumX>
+  <SLM_PixelNumY>1080</SLM_PixelNumY>
+  <SLM_WaveNum>3</SLM_WaveNum>
+  <SLM_WaveLength_1>638e-9</SLM_WaveLength_1>
+  <SLM_WaveLength_2>520e-9</SLM_WaveLength_2>
+  <SLM_WaveLength_3>450e-9</SLM_WaveLength_3>
+  <NumOfStream>0</NumOfStream>
+</PointCloud>
+"""
+
+
+def test_config_reader_dice_style(tmp_path):
+    st, c, img = P.read_config(_write(tmp_path, "a.xml", DICE_STYLE))
+    assert st == 0
+    assert (c.pixel_number[0], c.pixel_number[1]) == (1920, 1080)
+    assert (c.pixel_pitch[0], c.pixel_pitch[1]) == (4.3e-6, 4.3e-6)
+    assert c.n_channels == 3 and list(c.wave_length) == [638e-9, 520e-9, 450e-9]
+    assert list(c.scale) == [0.01, 0.01, 0.01] and c.distance == 0.1 and c.field_length == 1.0
+    assert img.merge == 1 and img.rotate == 0 and img.flip == 0 and img.double_precision == 1
+    assert img.num_of_stream == 0 and list(img.shift) == [0, 0, 0]
+
+
+def test_config_reader_golden_xml(tmp_path):
+    for name in ["rs_window_1ch", "rs_3ch_vw", "fresnel_3ch"]:
+        d = np.load(os.path.join(GOLD, name + ".npz"))
+        st, c, _ = P.read_config(_write(tmp_path, name + ".xml", str(d["xml"])))
+        assert st == 0
+
+
+def test_config_reader_errors(tmp_path):
+    # wrong extension / unreadable -> I/O error
+    assert P.read_config(_write(tmp_path, "a.txt", DICE_STYLE))[0] == 4
+    assert P.read_config(str(tmp_path / "missing.xml"))[0] == 4
+    # the reference reads keys under xml_doc.FirstChild(): a declaration
+    # first makes every key missing -> no usable document
+    assert P.read_config(_write(tmp_path, "b.xml", '<?xml version="1.0"?>\n' + DICE_STYLE))[0] == 4
+    # missing required key -> config error, other keys still read
+    st, c, _ = P.read_config(_write(tmp_path, "c.xml", DICE_STYLE.replace("<SLM_PixelNumY>1080</SLM_PixelNumY>", "")))
+    assert st == 5 and c.pixel_number[0] == 1920
+    # malformed number -> config error
+    st, _, _ = P.read_config(_write(tmp_path, "d.xml", DICE_STYLE.replace("0.01</ScaleX>", "abc</ScaleX>")))
+    assert st == 5
+    # more than three wavelengths: Vertex carries three colours
+    st, _, _ = P.read_config(_write(tmp_path, "e.xml", DICE_STYLE.replace("<SLM_WaveNum>3", "<SLM_WaveNum>4")))
+    assert st == 5
+
+
+def test_config_reader_tinyxml_value_rules(tmp_path):
+    x = DICE_STYLE.replace("<IMG_Rotation>0</IMG_Rotation>", "<IMG_Rotation>true</IMG_Rotation>")
+    x = x.replace("<SLM_PixelNumX>1920</SLM_PixelNumX>", "<SLM_PixelNumX>0x780</SLM_PixelNumX>")
+    st, c, img = P.read_config(_write(tmp_path, "f.xml", x))
+    assert st == 0 and img.rotate == 1 and c.pixel_number[0] == 1920
+
+
+def _bmp_pixels(raw: bytes):
+    off = struct.unpack_from("<I", raw, 10)[0]
+    w, h = struct.unpack_from("<ii", raw, 18)
+    bpp = struct.unpack_from("<H", raw, 28)[0]
+    ch = bpp // 8
+    stride = (w * ch + 3) & ~3
+    rows = [raw[off + y * stride: off + y * stride + w * ch] for y in range(h)]
+    return np.frombuffer(b"".join(rows), dtype=np.uint8).reshape(h, w * ch), w, h, bpp
+
+
+@pytest.mark.parametrize("name", ["bmp_1ch_w96", "bmp_1ch_w90", "bmp_3ch_merge"])
+def test_bmp_writer_byte_identical(tmp_path, name):
+    ref = open(os.path.join(GOLD, name + ".bmp"), "rb").read()
+    pix, w, h, bpp = _bmp_pixels(ref)
+    out = tmp_path / "o.bmp"
+    P.save_bmp(str(out), pix.reshape(h, w, bpp // 8) if bpp == 24 else pix, bits_per_pixel=bpp)
+    assert open(out, "rb").read() == ref
+
+
+def test_bmp_flip_and_rotate(tmp_path):
+    pix = np.arange(12, dtype=np.uint8).reshape(3, 4)
+    for flip, want in ((1, pix[::-1]), (2, pix[:, ::-1]), (3, pix[::-1, ::-1])):
+        P.save_bmp(str(tmp_path / "f.bmp"), pix, 8, flip=flip)
+        got, _, _, _ = _bmp_pixels(open(tmp_path / "f.bmp", "rb").read())
+        assert np.array_equal(got, want)
+    P.save_bmp(str(tmp_path / "r.bmp"), pix, 8, rotate=True)
+    got, _, _, _ = _bmp_pixels(open(tmp_path / "r.bmp", "rb").read())
+    assert np.array_equal(got, pix[::-1, ::-1])
