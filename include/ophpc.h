@@ -142,6 +142,31 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
                           uint64_t n_pixels, uint32_t encode_flag, double* d_encoded,
                           uint8_t* d_normalized, void* stream);
 
+/* Largest n_points * n_channels that ophpc_generate_static_scratch accepts:
+ * its scratch is a fixed 32 MiB device array of 64-byte point records. */
+#define OPHPC_STATIC_SCRATCH_RECORDS 524288u
+
+/* Allocation-free generate; this entry point has no counterpart in the
+ * reference. For callers that cannot allocate device memory — a host
+ * application that owns all device memory through its own allocator under a
+ * fixed budget, or a real-time loop that must never enter cudaMalloc /
+ * cudaFree, which can synchronise the whole device. Same arguments and
+ * result as ophpc_generate (plain RS and Fresnel kernels; tensor modes return
+ * OPHPC_ERROR_UNSUPPORTED), but no context: it runs on the calling thread's
+ * current device, and its scratch is one file-scope 32 MiB device array that
+ * every GPU loading the library holds until the process exits. It allocates
+ * nothing. The first call on a device does a one-time set-up on that device
+ * (looks up the array's device address); make that first call before any
+ * stream capture. n_points * n_channels above OPHPC_STATIC_SCRATCH_RECORDS is
+ * rejected with OPHPC_ERROR_INVALID_ARGUMENT before any work is queued. All
+ * calls on a device share the array and it keeps the last call's contents;
+ * nothing in it needs to start at zero, but calls whose GPU work overlaps
+ * (other streams, unsynchronised threads) race on it. Asynchronous on
+ * `stream`. */
+ophpc_status ophpc_generate_static_scratch(const ophpc_config* cfg, const ophpc_vertex* d_vertices,
+                                           uint64_t n_points, uint32_t diff_flag, uint32_t mode,
+                                           double* d_field, void* stream);
+
 /* ophGen::normalize alone on device: min/max over all channels of
  * d_encoded ([n_channels][n_pixels] doubles) and the 8-bit codes into
  * d_normalized. Asynchronous on `stream`. */
