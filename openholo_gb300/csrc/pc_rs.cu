@@ -29,8 +29,9 @@ namespace ophpc {
 namespace {
 
 struct __align__(16) RsSRec {
-    float P, Q, h, g;        // FAST: 2dxc/rc2, 2dyc/rc2, 1/rc2, rc/lambda. EXACT: 2dxc, 2dyc, rc2, rc
-    float fc, ac, dxc, dyc;  // frac(rc/lambda) in [-.5,.5]; FAST: coef/rc2, EXACT: coef
+    float P, Q, h, g;        // FAST: 2dxc/rc2, 2dyc/rc2, 1/rc2, rc/(2 lambda). EXACT: 2dxc, 2dyc, rc2, rc
+    float fc, ac, dxc, dyc;  // frac(rc/lambda) in [-.5,.5]; FAST: coef/rc2, -rc/(8 lambda), -
+                             // EXACT: coef, dxc, dyc
     float zz, mabs;          // EXACT: z^2, absolute margin of the FP32 cone test
     int32_t idx;             // EXACT: point index (FP64 fallback)
     int32_t xl, xh, yl, yh;  // EXACT: window rectangle relative to the tile origin
@@ -41,8 +42,8 @@ static_assert(sizeof(RsSRec) == 64, "RsSRec size");
 constexpr float kTwoPi = 6.283185307179586f;
 // FAST requires (rc/lambda) * |w|^3 / 16 below this many turns (series error)
 // and |w| below kMaxW (the dropped amplitude term is w^2).
-constexpr double kSeriesTol = 2e-8;
-constexpr double kMaxW = 1e-3;
+constexpr float kSeriesTol = 2e-8f;
+constexpr float kMaxW = 1e-3f;
 
 __device__ __forceinline__ int warp_prefix(unsigned ballot) {
     return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
@@ -64,11 +65,11 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
     const int vx1 = min(X0 + kTileW, g.pnX), vy1 = min(Y0 + kTileH, g.pnY);
     const int xc = X0 + kTileW / 2, yc = Y0 + kTileH / 2;
     const double Xc = pixel_x(g, xc), Yc = pixel_y(g, yc);
-    // valid-pixel coordinate ranges of this tile (X grows with the column,
-    // Y falls with the row)
-    const double Xmin = pixel_x(g, X0), Xmax = pixel_x(g, vx1 - 1);
-    const double Ymax = pixel_y(g, Y0), Ymin = pixel_y(g, vy1 - 1);
-    const double umax = (kTileW / 2) * g.ppX, vmax = (kTileH / 2) * g.ppY;
+    // offsets of the tile's valid pixels from its centre pixel: u = X - Xc
+    // (grows with the column), v = Y - Yc (falls with the row)
+    const float umin_f = (float)((double)(X0 - xc) * g.ppX), umax_f = (float)((double)(vx1 - 1 - xc) * g.ppX);
+    const float vmax_f = (float)((double)(yc - Y0) * g.ppY), vmin_f = (float)((double)(yc - (vy1 - 1)) * g.ppY);
+    const float uext_f = (float)((kTileW / 2) * g.ppX), vext_f = (float)((kTileH / 2) * g.ppY);
 
     const int tx = threadIdx.x % kThreadsX, ty = threadIdx.x / kThreadsX;
     const int warp = threadIdx.x >> 5;
@@ -107,47 +108,57 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                 const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
                 const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
                 if (ix0 < ix1 && iy0 < iy1) {
+                    // FP64: only frac(r_c / lambda). sqrt from an FP32 seed
+                    // refined by two Newton steps (relative error < 1e-20).
                     const double dxc = Xc - p.x, dyc = Yc - p.y;
-                    const double zz = p.aux;
-                    const double rc2 = dxc * dxc + dyc * dyc + zz;
-                    const double rc = sqrt(rc2);
+                    const double rc2 = fma(dxc, dxc, fma(dyc, dyc, p.aux));
+                    const double y0 = (double)rsqrtf((float)rc2);
+                    const double hy = 0.5 * y0;
+                    double rc = rc2 * y0;
+                    rc = fma(hy, fma(-rc, rc, rc2), rc);
+                    rc = fma(hy, fma(-rc, rc, rc2), rc);
                     const double tc = rc * g.inv_lambda;
-                    const double fc = tc - rint(tc);
+                    const float fc = (float)(tc - rint(tc));
+                    // FP32: classification (conservative margins) and the record
+                    const float dxf = (float)dxc, dyf = (float)dyc, zzf = (float)p.aux;
+                    const float rc2f = (float)rc2, rcf = (float)rc, tcf = (float)tc;
+                    const float hf = 1.0f / rc2f;
                     const bool rect_full = p.x_lo <= X0 && p.x_hi >= vx1 && p.y_lo <= Y0 && p.y_hi >= vy1;
-                    // conservative cone test over the whole tile
-                    const double ax0 = fabs(Xmin - p.x), ax1 = fabs(Xmax - p.x);
-                    const double ay0 = fabs(Ymin - p.y), ay1 = fabs(Ymax - p.y);
-                    const double maxdx = fmax(ax0, ax1), maxdy = fmax(ay0, ay1);
-                    const double mindx = (p.x >= Xmin && p.x <= Xmax) ? 0.0 : fmin(ax0, ax1);
-                    const double mindy = (p.y >= Ymin && p.y <= Ymax) ? 0.0 : fmin(ay0, ay1);
-                    const bool cone_full =
-                        maxdx < g.detx * sqrt(mindy * mindy + zz) * (1.0 - 1e-9) &&
-                        maxdy < g.dety * sqrt(mindx * mindx + zz) * (1.0 - 1e-9);
-                    const double nmax = 2.0 * fabs(dxc) * umax + umax * umax + 2.0 * fabs(dyc) * vmax + vmax * vmax;
-                    const double wmax = nmax / rc2;
-                    const bool series_ok = wmax < kMaxW && tc * wmax * wmax * wmax * (1.0 / 16.0) < kSeriesTol;
+                    const float xa = dxf + umin_f, xb = dxf + umax_f;   // X - x over the tile
+                    const float ya = dyf + vmin_f, yb = dyf + vmax_f;   // Y - y over the tile
+                    const float slack = 1e-6f * (fabsf(dxf) + fabsf(dyf) + uext_f + vext_f);
+                    const float maxdx = fmaxf(fabsf(xa), fabsf(xb)) + slack;
+                    const float maxdy = fmaxf(fabsf(ya), fabsf(yb)) + slack;
+                    const float mindx = fmaxf(((xa <= 0.f && xb >= 0.f) ? 0.f : fminf(fabsf(xa), fabsf(xb))) - slack, 0.f);
+                    const float mindy = fmaxf(((ya <= 0.f && yb >= 0.f) ? 0.f : fminf(fabsf(ya), fabsf(yb))) - slack, 0.f);
+                    const bool cone_full = maxdx < detx_f * sqrtf(fmaf(mindy, mindy, zzf)) * (1.f - 1e-5f) &&
+                                           maxdy < dety_f * sqrtf(fmaf(mindx, mindx, zzf)) * (1.f - 1e-5f);
+                    const float nmax = fmaf(2.f * fabsf(dxf), uext_f, uext_f * uext_f) +
+                                       fmaf(2.f * fabsf(dyf), vext_f, vext_f * vext_f);
+                    const float wmax = nmax * hf;
+                    const bool series_ok = wmax < kMaxW && tcf * wmax * wmax * wmax * (1.f / 16.f) < kSeriesTol;
                     RsSRec& t = tmp[q];
-                    t.fc = (float)fc;
+                    t.fc = fc;
                     if (rect_full && cone_full && series_ok) {
                         cls[q] = 1;
-                        const double h = 1.0 / rc2;
-                        t.P = (float)(2.0 * dxc * h);
-                        t.Q = (float)(2.0 * dyc * h);
-                        t.h = (float)h;
-                        t.g = (float)tc;
-                        t.ac = (float)(p.coef * h);
+                        t.P = 2.f * dxf * hf;
+                        t.Q = 2.f * dyf * hf;
+                        t.h = hf;
+                        t.g = 0.5f * tcf;           // phase = fc + (tc/2) w - (tc/8) w^2
+                        t.dxc = -0.125f * tcf;
+                        t.ac = (float)p.coef * hf;
                     } else {
                         cls[q] = 2;
-                        t.P = (float)(2.0 * dxc);
-                        t.Q = (float)(2.0 * dyc);
-                        t.h = (float)rc2;
-                        t.g = (float)rc;
+                        t.P = 2.f * dxf;
+                        t.Q = 2.f * dyf;
+                        t.h = rc2f;
+                        t.g = rcf;
                         t.ac = (float)p.coef;
-                        t.dxc = (float)dxc;
-                        t.dyc = (float)dyc;
-                        t.zz = (float)zz;
-                        t.mabs = (float)(1e-6 * (fabs(dxc) + fabs(dyc) + umax + vmax + sqrt(zz)) *
-                                         (1.0 + g.detx + g.dety));
+                        t.dxc = dxf;
+                        t.dyc = dyf;
+                        t.zz = zzf;
+                        t.mabs = 1e-6f * (fabsf(dxf) + fabsf(dyf) + uext_f + vext_f + sqrtf(zzf)) *
+                                 (1.f + detx_f + dety_f);
                         t.idx = (int32_t)idx;
                         t.xl = p.x_lo - X0;
                         t.xh = p.x_hi - X0;
@@ -196,8 +207,8 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
         for (int k = 0; k < kPixH * kPixW; ++k) sr[k] = si[k] = 0.f;
 #pragma unroll 1
         for (int j = 0; j < n_fast; ++j) {
-            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);
-            const float2 b = *reinterpret_cast<const float2*>(&s_rec[j].fc);
+            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);    // P, Q, h, tc/2
+            const float4 b = *reinterpret_cast<const float4*>(&s_rec[j].fc);   // fc, ac, -tc/8, -
             float A[kPixW], B[kPixH];
 #pragma unroll
             for (int c = 0; c < kPixW; ++c) A[c] = fmaf(a.x, u[c], a.z * uu[c]);
@@ -208,8 +219,7 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
 #pragma unroll
                 for (int c = 0; c < kPixW; ++c) {
                     const float w = A[c] + B[r];
-                    const float q = fmaf(w, -0.125f, 0.5f);
-                    float t = fmaf(a.w * w, q, b.x);
+                    float t = fmaf(w, fmaf(w, b.z, a.w), b.x);
                     t = reduce_turns(t);
                     float s, co;
                     __sincosf(t * kTwoPi, &s, &co);
