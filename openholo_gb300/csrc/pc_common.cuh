@@ -71,6 +71,47 @@ __device__ __forceinline__ float reduce_turns(float t) {
     return __fsub_rn(t, r);
 }
 
+// Packed FP32 pairs (sm_100+ .f32x2 arithmetic): one instruction issues two
+// FP32 operations, halving issue slots in the per-pixel loops. A pair lives
+// in a 64-bit register (low half = first element).
+namespace f2 {
+typedef unsigned long long v2;
+__device__ __forceinline__ v2 pack(float lo, float hi) {
+    v2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ v2 splat(float x) { return pack(x, x); }
+__device__ __forceinline__ void unpack(v2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ v2 add(v2 a, v2 b) {
+    v2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ v2 sub(v2 a, v2 b) {
+    v2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ v2 mul(v2 a, v2 b) {
+    v2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ v2 fma(v2 a, v2 b, v2 c) {
+    v2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+// t - rint(t) on both halves (1.5*2^23 round-to-nearest constant)
+__device__ __forceinline__ v2 reduce_turns(v2 t) {
+    const v2 m = splat(12582912.0f);
+    return sub(t, sub(add(t, m), m));
+}
+}  // namespace f2
+
 // Count of kernels this library has launched (all contexts, all threads);
 // read through ophpc_kernel_launches().
 void count_launches(unsigned n);

@@ -20,14 +20,17 @@ namespace ophpc {
 
 namespace {
 
+// Values duplicated into pairs for the packed FP32 arithmetic.
 struct __align__(16) FrSRec {
-    float P, Q, s, fc;       // 2 dxc s, 2 dyc s, s, frac(tau_c)
+    float2 P, Q;             // 2 dxc s, 2 dyc s
+    float2 s, fc;            // s, frac(tau_c)
     float ac;                // amp / (lambda z)
     int32_t xl, xh;          // window columns relative to the tile origin
-    int32_t yl, yh;          // window rows relative to the tile origin
+    int32_t yl;              // window rows relative to the tile origin
+    int32_t yh;
     int32_t pad[3];
 };
-static_assert(sizeof(FrSRec) == 48, "FrSRec size");
+static_assert(sizeof(FrSRec) == 64, "FrSRec size");
 
 constexpr float kTwoPi = 6.283185307179586f;
 
@@ -65,6 +68,18 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
         vv[r] = v[r] * v[r];
     }
 
+    f2::v2 up[kPixW / 2], uup[kPixW / 2], vp[kPixH / 2], vvp[kPixH / 2];
+#pragma unroll
+    for (int p = 0; p < kPixW / 2; ++p) {
+        up[p] = f2::pack(u[2 * p], u[2 * p + 1]);
+        uup[p] = f2::pack(uu[2 * p], uu[2 * p + 1]);
+    }
+#pragma unroll
+    for (int p = 0; p < kPixH / 2; ++p) {
+        vp[p] = f2::pack(v[2 * p], v[2 * p + 1]);
+        vvp[p] = f2::pack(vv[2 * p], vv[2 * p + 1]);
+    }
+
 #pragma unroll
     for (int k = 0; k < kPixH * kPixW; ++k) s_acc[k * kThreads + threadIdx.x] = make_double2(0.0, 0.0);
 
@@ -90,10 +105,12 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
                     const double s = p.aux;   // 1 / (2 z lambda)
                     const double tc = (dxc * dxc + dyc * dyc + 2.0 * p.z * p.z) * s;
                     FrSRec& t = tmp[q];
-                    t.P = (float)(2.0 * dxc * s);
-                    t.Q = (float)(2.0 * dyc * s);
-                    t.s = (float)s;
-                    t.fc = (float)(tc - rint(tc));
+                    const float P = (float)(2.0 * dxc * s), Q = (float)(2.0 * dyc * s), sf = (float)s;
+                    const float fc = (float)(tc - rint(tc));
+                    t.P = make_float2(P, P);
+                    t.Q = make_float2(Q, Q);
+                    t.s = make_float2(sf, sf);
+                    t.fc = make_float2(fc, fc);
                     t.ac = (float)p.coef;
                     t.xl = p.x_lo - X0;
                     t.xh = p.x_hi - X0;
@@ -123,47 +140,68 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
             if (keep[q]) s_rec[off[q] + warp_prefix(bk[q])] = tmp[q];
         __syncthreads();
 
-        float sr[kPixH * kPixW], si[kPixH * kPixW];
+        // accumulators: one packed (re, im) pair per pixel
+        f2::v2 acc[kPixH * kPixW];
 #pragma unroll
-        for (int k = 0; k < kPixH * kPixW; ++k) sr[k] = si[k] = 0.f;
+        for (int k = 0; k < kPixH * kPixW; ++k) acc[k] = 0ull;
+        const f2::v2 two_pi = f2::splat(kTwoPi);
 #pragma unroll 1
         for (int j = 0; j < n_keep; ++j) {
-            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);
+            const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&s_rec[j]);
+            const ulonglong2 r0 = R[0], r1 = R[1];
+            const f2::v2 P = r0.x, Q = r0.y, sp = r1.x, fc = r1.y;
             const float ac = s_rec[j].ac;
             const int4 wb = *reinterpret_cast<const int4*>(&s_rec[j].xl);
-            float exr[kPixW], exi[kPixW], eyr[kPixH], eyi[kPixH];
+            // column factors ac*e^{i 2pi alpha_c}, broadcast into pairs
+            f2::v2 ca[kPixW], cb[kPixW];
 #pragma unroll
-            for (int c = 0; c < kPixW; ++c) {
-                const int cl = tx * kPixW + c;
-                float t = fmaf(a.x, u[c], a.z * uu[c]) + a.w;
-                t = reduce_turns(t);
-                float s, co;
-                __sincosf(t * kTwoPi, &s, &co);
-                const float m = (cl >= wb.x && cl < wb.y) ? ac : 0.f;
-                exr[c] = m * co;
-                exi[c] = m * s;
+            for (int p = 0; p < kPixW / 2; ++p) {
+                f2::v2 t = f2::fma(P, up[p], f2::fma(sp, uup[p], fc));
+                t = f2::mul(f2::reduce_turns(t), two_pi);
+                float x[2];
+                f2::unpack(t, x[0], x[1]);
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int c = 2 * p + k;
+                    const int cl = tx * kPixW + c;
+                    float sn, cs;
+                    __sincosf(x[k], &sn, &cs);
+                    const float m = (cl >= wb.x && cl < wb.y) ? ac : 0.f;
+                    ca[c] = f2::splat(m * cs);
+                    cb[c] = f2::splat(m * sn);
+                }
             }
+            // row factors e^{i 2pi beta_r} as (c, d) and (-d, c)
+            f2::v2 r1p[kPixH], r2p[kPixH];
 #pragma unroll
-            for (int r = 0; r < kPixH; ++r) {
-                const int rl = ty * kPixH + r;
-                float t = fmaf(a.y, v[r], a.z * vv[r]);
-                t = reduce_turns(t);
-                float s, co;
-                __sincosf(t * kTwoPi, &s, &co);
-                const bool m = rl >= wb.z && rl < wb.w;
-                eyr[r] = m ? co : 0.f;
-                eyi[r] = m ? s : 0.f;
+            for (int p = 0; p < kPixH / 2; ++p) {
+                f2::v2 t = f2::fma(Q, vp[p], f2::mul(sp, vvp[p]));
+                t = f2::mul(f2::reduce_turns(t), two_pi);
+                float x[2];
+                f2::unpack(t, x[0], x[1]);
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int r = 2 * p + k;
+                    const int rl = ty * kPixH + r;
+                    float sn, cs;
+                    __sincosf(x[k], &sn, &cs);
+                    const float m = (rl >= wb.z && rl < wb.w) ? 1.f : 0.f;
+                    r1p[r] = f2::pack(m * cs, m * sn);
+                    r2p[r] = f2::pack(-m * sn, m * cs);
+                }
             }
 #pragma unroll
             for (int r = 0; r < kPixH; ++r) {
 #pragma unroll
                 for (int c = 0; c < kPixW; ++c) {
                     const int k = r * kPixW + c;
-                    sr[k] = fmaf(exr[c], eyr[r], fmaf(-exi[c], eyi[r], sr[k]));
-                    si[k] = fmaf(exr[c], eyi[r], fmaf(exi[c], eyr[r], si[k]));
+                    acc[k] = f2::fma(ca[c], r1p[r], f2::fma(cb[c], r2p[r], acc[k]));
                 }
             }
         }
+        float sr[kPixH * kPixW], si[kPixH * kPixW];
+#pragma unroll
+        for (int k = 0; k < kPixH * kPixW; ++k) f2::unpack(acc[k], sr[k], si[k]);
 #pragma unroll
         for (int k = 0; k < kPixH * kPixW; ++k) {
             double2 a = s_acc[k * kThreads + threadIdx.x];
