@@ -272,6 +272,37 @@ def gpu_arm(args, w):
                    max(3, args.steps // 2))
     t_fr = sum(gen_fr) / len(gen_fr)
 
+    # --- tensor-core Fresnel (tcgen05): FP16 and split-BF16, relL2 against the
+    # plain FP32 Fresnel field (itself within ~1e-6 of FP64)
+    def tensor_leg(wl, d_vert, cfg_l, out, steps):
+        res = {}
+        plain = torch.empty_like(out)
+        t_plain = None
+        gen_p = timed(lambda: ctx.generate(cfg_l, d_vert.data_ptr(), wl.n_points, oph.DIFF_FRESNEL, 0,
+                                           plain.data_ptr(), sp), 1)
+        t_plain = gen_p[0]
+        for name, mode in (("fp16", oph.MODE_TENSOR_FP16), ("bf16x3", oph.MODE_TENSOR_BF16X3)):
+            ctx.generate(cfg_l, d_vert.data_ptr(), wl.n_points, oph.DIFF_FRESNEL, mode, out.data_ptr(), sp)
+            torch.cuda.synchronize()
+            ts = timed(lambda: ctx.generate(cfg_l, d_vert.data_ptr(), wl.n_points, oph.DIFF_FRESNEL, mode,
+                                            out.data_ptr(), sp), steps)
+            t = sum(ts) / len(ts)
+            rel = float(torch.linalg.vector_norm(out - plain) / torch.linalg.vector_norm(plain))
+            res[name] = {"value": wl.interactions / t, "unit": UNIT, "ms_per_generate": t * 1e3,
+                         "relL2_vs_plain_fp32": rel, "speedup_vs_plain_fresnel": t_plain / t}
+        res["plain_fresnel_ms"] = t_plain * 1e3
+        return res
+
+    tensor = {"sphere_fhd": tensor_leg(w, dv, cfg, field, max(3, args.steps // 2))}
+    if os.environ.get("OPHPC_BENCH_SKIP_4K") != "1":
+        from openholo_gb300 import workloads as W
+        w4 = W.box_4k()
+        cfg4 = oph.make_config(**w4.geometry_kwargs())
+        dv4 = torch.from_numpy(w4.vertices).cuda()
+        f4 = torch.empty((1, w4.pny, w4.pnx, 2), dtype=torch.float64, device="cuda")
+        tensor["box_4k"] = tensor_leg(w4, dv4, cfg4, f4, 2)
+        del dv4, f4
+
     # --- end to end through the host-facing ABI ------------------------------
     hv = torch.from_numpy(w.vertices).pin_memory()
     hfield = torch.empty((nch, pny, pnx, 2), dtype=torch.float64).pin_memory()
@@ -339,6 +370,7 @@ def gpu_arm(args, w):
                                        f"{sm_mhz:.0f} MHz median SM clock under load"},
             "fresnel": {"value": inter * world / t_fr, "unit": UNIT, "ms_per_generate": t_fr * 1e3,
                         "kernel": "fresnel_kernel (FP32 cores, separable)"},
+            "tensor_fresnel": tensor,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": t_e2e * 1e3},
             "gpu_launches": int(launches),

@@ -1,0 +1,95 @@
+"""Tensor-core Fresnel (tcgen05) against the FP64 oracle.
+
+Tolerances, stated per precision:
+  split-BF16 (hi/lo, three products, FP32 accumulation): relL2 <= 1e-4, the
+      spec bar, and the 8-bit phase encoding exact on >= 99.9% of pixels
+      within +-1 LSB;
+  FP16 (one product): relL2 <= 1e-3 — an 11-bit significand leaves ~1e-4 per
+      table entry, so FP16 cannot reach 1e-4 and the measured error is
+      reported beside every FP16 number instead.
+"""
+import numpy as np
+import pytest
+
+from tests._util import code_agreement, rel_l2, run_encode, run_generate
+
+pytestmark = pytest.mark.gpu
+
+MODE_FP16 = 0x100
+MODE_BF16X3 = 0x200
+
+
+def _box(n, xy, z, seed):
+    rng = np.random.default_rng(seed)
+    v = np.zeros((n, 7))
+    v[:, 0] = rng.uniform(-xy[0], xy[0], n)
+    v[:, 1] = rng.uniform(-xy[1], xy[1], n)
+    v[:, 2] = rng.uniform(z[0], z[1], n)
+    v[:, 3:6] = 1.0 - rng.uniform(0.0, 1.0, (n, 3))
+    return v
+
+
+CASES = {
+    "full_aperture": (dict(pnx=256, pny=256, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                      _box(3000, (1e-3, 1e-3), (0.3, 0.5), 31)),
+    "window_cut_odd": (dict(pnx=200, pny=120, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                       _box(700, (6e-4, 4e-4), (0.002, 0.01), 32)),
+    "three_channels": (dict(pnx=130, pny=77, ppx=6.4e-6, ppy=7.1e-6, wavelengths=[638e-9, 532e-9, 473e-9],
+                            scale=(0.5, 0.5, 2.0), distance=0.05),
+                       _box(900, (1e-3, 1e-3), (0.05, 0.2), 33)),
+}
+
+
+def _oracle(oracle_mod, gk, v):
+    g = oracle_mod.Geometry(**{k: gk[k] for k in ("pnx", "pny", "ppx", "ppy", "wavelengths")},
+                            scale=gk.get("scale", (1.0, 1.0, 1.0)), distance=gk.get("distance", 0.0))
+    return oracle_mod.generate(g, v, 1)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_bf16x3_meets_the_bar(gpu_ctx, oracle_mod, name):
+    gk, v = CASES[name]
+    ref = _oracle(oracle_mod, gk, v)
+    got = run_generate(gpu_ctx, gk, v, 1, MODE_BF16X3)
+    err = rel_l2(got, ref)
+    print(f"{name}: split-BF16 relL2 = {err:.3e}")
+    assert err <= 1e-4
+    _, codes = run_encode(gpu_ctx, got, 0)
+    codes_ref, _, _ = oracle_mod.normalize(oracle_mod.encode(ref, 0))
+    exact, maxd = code_agreement(codes, codes_ref, True)
+    print(f"  phase codes exact {exact:.5f} max|d| {maxd}")
+    assert exact >= 0.999 and maxd <= 1
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp16_error_reported(gpu_ctx, oracle_mod, name):
+    gk, v = CASES[name]
+    ref = _oracle(oracle_mod, gk, v)
+    got = run_generate(gpu_ctx, gk, v, 1, MODE_FP16)
+    err = rel_l2(got, ref)
+    print(f"{name}: FP16 relL2 = {err:.3e}")
+    assert err <= 1e-3
+
+
+def test_tensor_modes_match_plain_kernel_on_many_points(gpu_ctx):
+    """More points than one table chunk holds at this width, so the FP64 sums
+    across chunks are exercised; the plain FP32 kernel is within 1e-6 of
+    FP64 and serves as the reference here."""
+    gk = dict(pnx=1024, pny=512, ppx=3.74e-6, ppy=3.74e-6, wavelengths=[532e-9])
+    v = _box(70000, (2e-3, 2e-3), (0.29, 0.31), 34)
+    plain = run_generate(gpu_ctx, gk, v, 1, 0)
+    bf = run_generate(gpu_ctx, gk, v, 1, MODE_BF16X3)
+    fp = run_generate(gpu_ctx, gk, v, 1, MODE_FP16)
+    e_bf, e_fp = rel_l2(bf, plain), rel_l2(fp, plain)
+    print(f"vs plain: split-BF16 {e_bf:.3e}, FP16 {e_fp:.3e}")
+    assert e_bf <= 1e-4 and e_fp <= 1e-3
+
+
+def test_tensor_zero_points_and_determinism(gpu_ctx):
+    gk = dict(pnx=150, pny=100, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    z = run_generate(gpu_ctx, gk, np.zeros((0, 7)), 1, MODE_BF16X3)
+    assert not np.any(z)
+    v = _box(500, (1e-3, 1e-3), (0.2, 0.3), 35)
+    a = run_generate(gpu_ctx, gk, v, 1, MODE_BF16X3)
+    b = run_generate(gpu_ctx, gk, v, 1, MODE_BF16X3)
+    assert np.array_equal(a, b)
