@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-points", type=int, default=0, help="points in the CPU sample (0 = auto)")
+    ap.add_argument("--serving-jobs", type=int, default=64, help="jobs in the serving stream (512 = full)")
+    ap.add_argument("--serving-max-points", type=int, default=100_000,
+                    help="largest point count of a serving job (500000 = full)")
     return ap.parse_args()
 
 
@@ -194,6 +197,69 @@ def reference_arm(args, w):
     print(json.dumps(line), flush=True)
 
 
+# ------------------------------------------------------------------ serving
+
+def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int = 4):
+    """Mixed hologram jobs with Poisson arrivals through the serving engine.
+
+    Every job is first run alone (isolated latency = its service time); the
+    mean isolated service time sets the arrival rate of each offered load.
+    Latency = completion - arrival (server clock). Jobs return their 8-bit
+    phase holograms (the field stays on the device)."""
+    import threading
+
+    import torch
+
+    from openholo_gb300 import make_config, workloads
+    from openholo_gb300.serving import Server
+
+    jobs = workloads.serving_stream(n_jobs, rate_per_s=1.0, seed=seed, max_points=max_points)
+    prepared = []
+    for jb in jobs:
+        w = jb.workload
+        hv = torch.from_numpy(w.vertices).pin_memory()
+        hc = torch.empty((w.n_channels, w.pny, w.pnx), dtype=torch.uint8).pin_memory()
+        prepared.append((make_config(**w.geometry_kwargs()), hv, hc, w.n_points, jb.diff_flag, w.interactions))
+    out = {"jobs": n_jobs, "max_points": max_points, "loads": {}}
+    with Server(0, max_in_flight=6, step_ms=2.0) as srv:
+        iso = []
+        for cfg, hv, hc, n, d, _ in prepared:
+            r = srv.wait_stats(srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0))
+            iso.append(r.t_done - r.t_submit)
+        iso = np.array(iso)
+        mean_s = float(iso.mean())
+        out["isolated_ms"] = {"p50": float(np.percentile(iso, 50) * 1e3), "p99": float(np.percentile(iso, 99) * 1e3),
+                              "mean": mean_s * 1e3}
+        rng = np.random.default_rng(seed + 1)
+        gaps = rng.exponential(1.0, n_jobs)
+        for load in loads:
+            arrivals = np.cumsum(gaps) * mean_s / load
+            tickets = [None] * n_jobs
+
+            def feeder():
+                t0 = time.perf_counter()
+                for i, (cfg, hv, hc, n, d, _) in enumerate(prepared):
+                    dt = arrivals[i] - (time.perf_counter() - t0)
+                    if dt > 0:
+                        time.sleep(dt)
+                    tickets[i] = srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0)
+
+            th = threading.Thread(target=feeder)
+            th.start()
+            th.join()
+            res = [srv.wait_stats(t) for t in tickets]
+            lat = np.array([r.t_done - r.t_submit for r in res])
+            span = max(r.t_done for r in res) - min(r.t_submit for r in res)
+            slow = lat / iso
+            out["loads"][f"{load:.2f}"] = {
+                "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "p99_over_isolated_p99": float(np.percentile(lat, 99) / np.percentile(iso, 99)),
+                "slowdown_p50": float(np.percentile(slow, 50)), "slowdown_p99": float(np.percentile(slow, 99)),
+                "throughput_interactions_per_s": float(sum(p[5] for p in prepared) / span),
+                "jobs_per_s": n_jobs / span}
+    return out
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def gpu_arm(args, w):
@@ -303,6 +369,10 @@ def gpu_arm(args, w):
         tensor["box_4k"] = tensor_leg(w4, dv4, cfg4, f4, 2)
         del dv4, f4
 
+    serving = None
+    if os.environ.get("OPHPC_BENCH_SKIP_SERVING") != "1" and world == 1:
+        serving = serving_leg(args.serving_jobs, args.serving_max_points)
+
     # --- end to end through the host-facing ABI ------------------------------
     hv = torch.from_numpy(w.vertices).pin_memory()
     hfield = torch.empty((nch, pny, pnx, 2), dtype=torch.float64).pin_memory()
@@ -371,6 +441,7 @@ def gpu_arm(args, w):
             "fresnel": {"value": inter * world / t_fr, "unit": UNIT, "ms_per_generate": t_fr * 1e3,
                         "kernel": "fresnel_kernel (FP32 cores, separable)"},
             "tensor_fresnel": tensor,
+            "serving": serving,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": t_e2e * 1e3},
             "gpu_launches": int(launches),

@@ -52,6 +52,12 @@ struct JobGeom {
     int32_t ksplit;         // point-range splits per tile
     int64_t n_points;
     int64_t points_per_split;
+    // Point range of this launch, [p0, p1); p1 == 0 means all n_points.
+    // With accumulate != 0 the kernels add into the field instead of
+    // overwriting it (a job computed as several point-range launches).
+    int64_t p0, p1;
+    int32_t accumulate;
+    int32_t pad;
 };
 
 // Pixel-centre coordinates, exactly as the reference forms them

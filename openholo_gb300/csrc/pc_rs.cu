@@ -91,8 +91,9 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
     for (int k = 0; k < kPixH * kPixW; ++k) s_acc[k * kThreads + threadIdx.x] = make_double2(0.0, 0.0);
 
     const int64_t n = jg.n_points;
-    const int64_t p_beg = (int64_t)part * jg.points_per_split;
-    const int64_t p_end = min(n, p_beg + jg.points_per_split);
+    const int64_t range_end = jg.p1 > 0 ? min(jg.p1, n) : n;
+    const int64_t p_beg = jg.p0 + (int64_t)part * jg.points_per_split;
+    const int64_t p_end = min(range_end, p_beg + jg.points_per_split);
     const PointRec* chrec = recs + (int64_t)ch * n;
 
     for (int64_t cb = p_beg; cb < p_end; cb += kChunk) {
@@ -317,7 +318,13 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
             const int col = X0 + tx * kPixW + c;
             if (col >= g.pnX) continue;
             const double2 a = s_acc[(r * kPixW + c) * kThreads + threadIdx.x];
-            dst[(int64_t)row * g.pnX + col] = make_double2(a.x, -a.y);
+            double2* o = dst + (int64_t)row * g.pnX + col;
+            if (jg.accumulate && part == 0) {
+                const double2 prev = *o;
+                *o = make_double2(prev.x + a.x, prev.y - a.y);
+            } else {
+                *o = make_double2(a.x, -a.y);
+            }
         }
     }
 }
