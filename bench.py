@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-points", type=int, default=0, help="points in the CPU sample (0 = auto)")
     ap.add_argument("--serving-jobs", type=int, default=64, help="jobs in the serving stream (512 = full)")
+    ap.add_argument("--profile-case", default=None,
+                    help="run one small fixed case for a profiler and exit: rs_1k, fresnel_1k, tc_fp16_4k, "
+                         "tc_bf16x3_4k (box_4k distribution, 131,072 points)")
     ap.add_argument("--serving-max-points", type=int, default=100_000,
                     help="largest point count of a serving job (500000 = full)")
     return ap.parse_args()
@@ -221,7 +224,7 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
         hc = torch.empty((w.n_channels, w.pny, w.pnx), dtype=torch.uint8).pin_memory()
         prepared.append((make_config(**w.geometry_kwargs()), hv, hc, w.n_points, jb.diff_flag, w.interactions))
     out = {"jobs": n_jobs, "max_points": max_points, "loads": {}}
-    with Server(0, max_in_flight=6, step_ms=2.0) as srv:
+    with Server(0, max_in_flight=16, step_ms=2.0) as srv:
         iso = []
         for cfg, hv, hc, n, d, _ in prepared:
             r = srv.wait_stats(srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0))
@@ -458,8 +461,36 @@ def gpu_arm(args, w):
     return line
 
 
+def profile_case(name: str) -> None:
+    """One call of one path on a small fixed case (for ncu captures): no
+    timing, no CPU work, a few GB of device memory at most."""
+    import torch
+
+    import openholo_gb300 as oph
+    from openholo_gb300 import workloads
+    if name in ("rs_1k", "fresnel_1k"):
+        w, diff, mode = workloads.rs_1k(), (0 if name == "rs_1k" else 1), 0
+    elif name in ("tc_fp16_4k", "tc_bf16x3_4k"):
+        w = workloads.box_4k(n_points=131_072)
+        diff = 1
+        mode = oph.MODE_TENSOR_FP16 if name == "tc_fp16_4k" else oph.MODE_TENSOR_BF16X3
+    else:
+        raise SystemExit(f"unknown profile case {name}")
+    ctx = oph.Context(0)
+    cfg = oph.make_config(**w.geometry_kwargs())
+    dv = torch.from_numpy(w.vertices).cuda()
+    f = torch.empty((w.n_channels, w.pny, w.pnx, 2), dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    print(f"profile case {name}: done")
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     from openholo_gb300 import workloads
     w = workloads.BY_NAME[args.workload]()
     if args.impl == "reference":

@@ -30,7 +30,7 @@ extern "C" {
 typedef struct ophpc_server ophpc_server;
 
 typedef struct ophpc_server_options {
-    uint32_t max_in_flight;    /* admitted jobs at once (0 = 6) */
+    uint32_t max_in_flight;    /* admitted jobs at once (0 = 16) */
     uint32_t pad;
     uint64_t memory_budget;    /* bytes of device memory for jobs (0 = half the free memory) */
     uint64_t reserve_bytes;    /* free device memory always left untouched (0 = 512 MiB) */

@@ -37,7 +37,7 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 
-constexpr int kPrioLevels = 3;
+constexpr int kPrioLevels = 6;   // CUDA exposes six stream priorities on this GPU family
 
 struct ServeJob {
     uint64_t ticket = 0;
@@ -283,8 +283,9 @@ void worker_main(ophpc_server* s) {
             std::sort(ranked.begin(), ranked.end(),
                       [](const ServeJob* a, const ServeJob* b) { return a->remaining < b->remaining; });
             for (ServeJob* j : idle) {
+                // rank among admitted jobs by remaining work -> priority bucket
                 const size_t r = (size_t)(std::find(ranked.begin(), ranked.end(), j) - ranked.begin());
-                const int prio = r == 0 ? 0 : (r < ranked.size() / 2 + 1 ? 1 : 2);
+                const int prio = (int)(r * kPrioLevels / ranked.size());
                 enqueue_step(s, j, std::min(prio, kPrioLevels - 1));
             }
             progressed = true;
@@ -318,7 +319,7 @@ ophpc_status ophpc_server_create(int32_t device, const ophpc_server_options* opt
     std::unique_ptr<ophpc_server> s(new ophpc_server());
     s->device = device;
     if (options) s->opt = *options;
-    if (s->opt.max_in_flight == 0) s->opt.max_in_flight = 6;
+    if (s->opt.max_in_flight == 0) s->opt.max_in_flight = 16;
     if (s->opt.step_ms <= 0) s->opt.step_ms = 2.0;
     if (s->opt.reserve_bytes == 0) s->opt.reserve_bytes = (size_t)512 << 20;
     if (s->opt.memory_budget == 0) {

@@ -63,7 +63,7 @@ class Result:
 class Server:
     """Continuous-batching hologram server on one GPU."""
 
-    def __init__(self, device: int = 0, max_in_flight: int = 6, memory_budget: int = 0, step_ms: float = 2.0,
+    def __init__(self, device: int = 0, max_in_flight: int = 16, memory_budget: int = 0, step_ms: float = 2.0,
                  reserve_bytes: int = 0):
         self._L = _L()
         o = ServerOptions(max_in_flight=max_in_flight, memory_budget=memory_budget, reserve_bytes=reserve_bytes,
