@@ -138,6 +138,12 @@ public:
     void encoding(unsigned int ENCODE_FLAG);
     void normalize(void);
     bool save(const char* fname, uint8_t bitsperpixel = 8, uchar* src = nullptr, uint px = 0, uint py = 0);
+    /* Openholo::saveAsOhc / loadAsOhc (Openholo/src/Openholo.cpp:252-319):
+     * the complex field with its pitch and wavelengths. loadAsOhc replaces
+     * the pixel number, pitch and wavelengths of the context and the
+     * complex field; the encoded and normalized buffers restart at zero. */
+    bool saveAsOhc(const char* fname);
+    bool loadAsOhc(const char* fname);
 
     Complex<Real>** getComplexField(void) { return complex_H_; }
     Real** getEncodedBuffer(void) { return encoded_; }

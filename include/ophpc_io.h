@@ -57,6 +57,29 @@ int64_t ophpc_load_ply(const char* path, ophpc_vertex* out, uint64_t capacity);
 ophpc_status ophpc_save_bmp(const char* path, const uint8_t* pixels, int32_t width, int32_t height,
                             int32_t bits_per_pixel, int32_t flip, int32_t rotate);
 
+/* Openholo complex-field file (.ohc; Openholo/src/ImgCodecDefine.h:53-210,
+ * Openholo/src/ImgCodecOhc.cpp): writes the field as the reference's
+ * Openholo::saveAsOhc does (Openholo/src/Openholo.cpp:252-279) — version
+ * 3.0, real/imaginary float64, one plane per channel, metres — byte for
+ * byte. field: [n_channels][pnY][pnX][re, im] doubles. ".ohc" is appended
+ * when the name does not end in it. */
+ophpc_status ophpc_save_ohc(const char* path, const double* field, int32_t pnx, int32_t pny, double ppx,
+                            double ppy, uint32_t n_channels, const double* wavelengths);
+
+/* Reads a .ohc (Openholo::loadAsOhc, Openholo/src/Openholo.cpp:280-319;
+ * ImgDecoderOhc::decodeFieldData, Openholo/src/ImgCodecOhc.cpp:434-600):
+ * real/imaginary float32 or float64, one plane per channel or channels
+ * interleaved per pixel; pitch and wavelengths returned as stored, as the
+ * reference does. Amplitude/phase files are converted to real/imaginary
+ * (the reference leaves its complex field zero for them). Fills the shape
+ * (any pointer may be NULL) and, when field is non-NULL and
+ * capacity_doubles suffices (2 * n_channels * pnX * pnY), the field in the
+ * layout of ophpc_save_ohc. More than OPHPC_MAX_CHANNELS wavelengths,
+ * linked-file storage or amplitude-only / phase-only coding is
+ * OPHPC_ERROR_UNSUPPORTED. */
+ophpc_status ophpc_load_ohc(const char* path, int32_t* pnx, int32_t* pny, double* ppx, double* ppy,
+                            uint32_t* n_channels, double* wavelengths, double* field, uint64_t capacity_doubles);
+
 #ifdef __cplusplus
 }
 #endif

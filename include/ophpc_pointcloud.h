@@ -16,6 +16,7 @@
  *   ophpc_pc_encoding                 encoding          (ophPointCloud.cpp:242-245)
  *   ophpc_pc_normalize                normalize         (ophGen.cpp:654-687)
  *   ophpc_pc_save                     save              (ophGen.cpp:689-769)
+ *   ophpc_pc_save_ohc / _load_ohc     Openholo::saveAsOhc / loadAsOhc (Openholo.cpp:252-319)
  *   ophpc_pc_complex_field / _encoded / _normalized
  *                                     getComplexField()[ch] / getEncodedBuffer()[ch] /
  *                                     getNormalizedBuffer()[ch] (ophGen.h:117-124, Openholo.h:490)
@@ -47,6 +48,8 @@ double ophpc_pc_generate_hologram(ophpc_pc* h, uint32_t diff_flag);
 void ophpc_pc_encoding(ophpc_pc* h, uint32_t encode_flag);
 void ophpc_pc_normalize(ophpc_pc* h);
 int32_t ophpc_pc_save(ophpc_pc* h, const char* path, uint8_t bits_per_pixel);
+int32_t ophpc_pc_save_ohc(ophpc_pc* h, const char* path);
+int32_t ophpc_pc_load_ohc(ophpc_pc* h, const char* path);
 int32_t ophpc_pc_get_config(ophpc_pc* h, ophpc_config* out);
 uint64_t ophpc_pc_number_of_points(ophpc_pc* h);
 const ophpc_vertex* ophpc_pc_point_cloud(ophpc_pc* h);

@@ -340,6 +340,60 @@ bool ophPointCloud::save(const char* fname, uint8_t bitsperpixel, uchar* src, ui
     return ok;
 }
 
+bool ophPointCloud::saveAsOhc(const char* fname) {
+    if (fname == nullptr || !complex_H_) return false;
+    const uint nch = context_.waveNum;
+    const size_t plane = (size_t)buffer_pixels_;
+    std::vector<double> field(2 * plane * nch);
+    for (uint c = 0; c < nch; ++c)
+        std::memcpy(field.data() + 2 * plane * c, complex_H_[c], sizeof(double) * 2 * plane);
+    const ophpc_status st = ophpc_save_ohc(fname, field.data(), context_.pixel_number[_X], context_.pixel_number[_Y],
+                                           context_.pixel_pitch[_X], context_.pixel_pitch[_Y], nch, wave_length_);
+    if (st != OPHPC_SUCCESS) {
+        last_error_ = std::string("saveAsOhc: ") + ophpc_status_string(st);
+        return false;
+    }
+    return true;
+}
+
+bool ophPointCloud::loadAsOhc(const char* fname) {
+    if (fname == nullptr) return false;
+    int32_t pnx = 0, pny = 0;
+    double ppx = 0, ppy = 0, wl[OPHPC_MAX_CHANNELS] = {0, 0, 0};
+    uint32_t nch = 0;
+    ophpc_status st = ophpc_load_ohc(fname, &pnx, &pny, &ppx, &ppy, &nch, wl, nullptr, 0);
+    if (st != OPHPC_SUCCESS) {
+        OPH_LOG("<FAILED> Load ohc : %s\n", fname);
+        last_error_ = std::string("loadAsOhc: ") + ophpc_status_string(st);
+        return false;
+    }
+    const size_t plane = (size_t)pnx * (size_t)pny;
+    std::vector<double> field(2 * plane * nch);
+    st = ophpc_load_ohc(fname, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, field.data(), field.size());
+    if (st != OPHPC_SUCCESS) {
+        OPH_LOG("<FAILED> Load ohc : %s\n", fname);
+        last_error_ = std::string("loadAsOhc: ") + ophpc_status_string(st);
+        return false;
+    }
+    context_.waveNum = nch;
+    for (uint i = 0; i < OPHPC_MAX_CHANNELS; ++i) wave_length_[i] = i < nch ? wl[i] : 0.0;
+    context_.pixel_number[_X] = pnx;
+    context_.pixel_number[_Y] = pny;
+    context_.pixel_pitch[_X] = ppx;
+    context_.pixel_pitch[_Y] = ppy;
+    context_.ss[_X] = pnx * ppx;
+    context_.ss[_Y] = pny * ppy;
+    context_.k = (2 * kPi) / wave_length_[0];
+    if (!initialize()) {
+        last_error_ = "loadAsOhc: invalid pixel number or channel count";
+        return false;
+    }
+    for (uint c = 0; c < nch; ++c)
+        std::memcpy(complex_H_[c], field.data() + 2 * plane * c, sizeof(double) * 2 * plane);
+    encoded_valid_ = false;
+    return true;
+}
+
 // ------------------------------------------------------------------ C ABI
 
 struct ophpc_pc {
@@ -391,6 +445,9 @@ void ophpc_pc_normalize(ophpc_pc* h) { if (h) h->obj->normalize(); }
 int32_t ophpc_pc_save(ophpc_pc* h, const char* path, uint8_t bits_per_pixel) {
     return h && h->obj->save(path, bits_per_pixel) ? 1 : 0;
 }
+
+int32_t ophpc_pc_save_ohc(ophpc_pc* h, const char* path) { return h && h->obj->saveAsOhc(path) ? 1 : 0; }
+int32_t ophpc_pc_load_ohc(ophpc_pc* h, const char* path) { return h && h->obj->loadAsOhc(path) ? 1 : 0; }
 
 int32_t ophpc_pc_get_config(ophpc_pc* h, ophpc_config* out) {
     if (!h || !out) return 0;

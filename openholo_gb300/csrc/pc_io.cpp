@@ -366,9 +366,144 @@ void put32(std::vector<uint8_t>& b, size_t at, uint32_t v) {
     for (int i = 0; i < 4; ++i) b[at + i] = (uint8_t)(v >> (8 * i));
 }
 
+// ------------------------------------------------------------------ OHC
+
+// Field-info header of the .ohc format (65 bytes, packed, little-endian).
+#pragma pack(push, 1)
+struct OhcFileHeader {
+    char signature[2];
+    uint64_t file_size;
+    uint8_t version_major, version_minor;
+    uint32_t reserved1, reserved2;
+    uint32_t off_bytes;
+};
+struct OhcFieldInfo {
+    uint32_t header_size;
+    uint32_t px_x, px_y;
+    double pitch_x, pitch_y;
+    uint8_t pitch_unit;
+    uint32_t n_wavelengths;
+    uint8_t color_type, color_arrange, wavelength_unit, data_type, store, code_type, phase_coded;
+    double phase_min, phase_max;
+    uint64_t field_bytes;
+    uint8_t compression;
+};
+#pragma pack(pop)
+static_assert(sizeof(OhcFileHeader) == 24, "ohc file header");
+static_assert(sizeof(OhcFieldInfo) == 65, "ohc field info header");
+
+std::string ohc_path(const char* p) {
+    std::string s = p;
+    if (!ends_with(s, ".ohc")) s += ".ohc";
+    return s;
+}
+
 }  // namespace
 
 extern "C" {
+
+ophpc_status ophpc_save_ohc(const char* path, const double* field, int32_t pnx, int32_t pny, double ppx, double ppy,
+                            uint32_t nch, const double* wavelengths) {
+    if (!path || !field || !wavelengths || pnx <= 0 || pny <= 0 || nch < 1 || nch > OPHPC_MAX_CHANNELS)
+        return OPHPC_ERROR_INVALID_ARGUMENT;
+    const uint64_t npx = (uint64_t)pnx * (uint64_t)pny;
+    OhcFieldInfo fi;
+    std::memset(&fi, 0, sizeof(fi));
+    fi.header_size = (uint32_t)(sizeof(OhcFieldInfo) + 8 * nch);
+    fi.px_x = (uint32_t)pnx;
+    fi.px_y = (uint32_t)pny;
+    fi.pitch_x = ppx;
+    fi.pitch_y = ppy;
+    fi.pitch_unit = 1;           // metre
+    fi.n_wavelengths = nch;
+    fi.color_type = 2;           // multiple colours
+    fi.color_arrange = 2;        // one plane per channel
+    fi.wavelength_unit = 1;      // metre
+    fi.data_type = 10;           // float64
+    fi.store = 1;                // stored directly
+    fi.code_type = 2;            // real & imaginary
+    fi.phase_coded = 0;
+    fi.phase_min = -1.0;
+    fi.phase_max = 1.0;
+    fi.field_bytes = 16 * npx * nch;
+    fi.compression = 0;
+    OhcFileHeader fh;
+    fh.signature[0] = 'O';
+    fh.signature[1] = 'H';
+    fh.version_major = 3;
+    fh.version_minor = 0;
+    fh.reserved1 = fh.reserved2 = 0;
+    fh.off_bytes = (uint32_t)(sizeof(OhcFileHeader) + fi.header_size);
+    fh.file_size = fh.off_bytes + fi.field_bytes;
+    FILE* fp = std::fopen(ohc_path(path).c_str(), "wb");
+    if (!fp) return OPHPC_ERROR_IO;
+    bool ok = std::fwrite(&fh, sizeof(fh), 1, fp) == 1 && std::fwrite(&fi, sizeof(fi), 1, fp) == 1 &&
+              std::fwrite(wavelengths, sizeof(double), nch, fp) == nch;
+    std::vector<double> plane((size_t)npx);
+    for (int part = 0; part < 2 && ok; ++part)
+        for (uint32_t c = 0; c < nch && ok; ++c) {
+            const double* src = field + (size_t)c * npx * 2;
+            for (uint64_t i = 0; i < npx; ++i) plane[i] = src[2 * i + part];
+            ok = std::fwrite(plane.data(), sizeof(double), (size_t)npx, fp) == npx;
+        }
+    ok = (std::fclose(fp) == 0) && ok;
+    return ok ? OPHPC_SUCCESS : OPHPC_ERROR_IO;
+}
+
+ophpc_status ophpc_load_ohc(const char* path, int32_t* pnx, int32_t* pny, double* ppx, double* ppy, uint32_t* nch_out,
+                            double* wavelengths, double* field, uint64_t capacity) {
+    if (!path) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::ifstream f(ohc_path(path), std::ios::in | std::ios::binary);
+    if (!f.is_open()) return OPHPC_ERROR_IO;
+    OhcFileHeader fh;
+    OhcFieldInfo fi;
+    if (!f.read((char*)&fh, sizeof(fh)) || fh.signature[0] != 'O' || fh.signature[1] != 'H') return OPHPC_ERROR_IO;
+    if (!f.read((char*)&fi, sizeof(fi))) return OPHPC_ERROR_IO;
+    const uint32_t nch = fi.n_wavelengths;
+    if (nch < 1 || nch > OPHPC_MAX_CHANNELS || fi.px_x == 0 || fi.px_y == 0) return OPHPC_ERROR_UNSUPPORTED;
+    double wl[OPHPC_MAX_CHANNELS] = {0, 0, 0};
+    if (!f.read((char*)wl, sizeof(double) * nch)) return OPHPC_ERROR_IO;
+    // pitch and wavelengths as stored, whatever their unit field says
+    // (ImgDecoderOhc::getPixelPitch / getWavelength)
+    if (pnx) *pnx = (int32_t)fi.px_x;
+    if (pny) *pny = (int32_t)fi.px_y;
+    if (ppx) *ppx = fi.pitch_x;
+    if (ppy) *ppy = fi.pitch_y;
+    if (nch_out) *nch_out = nch;
+    if (wavelengths)
+        for (uint32_t c = 0; c < nch; ++c) wavelengths[c] = wl[c];
+    if (!field) return OPHPC_SUCCESS;
+    const uint64_t npx = (uint64_t)fi.px_x * fi.px_y;
+    if (capacity < 2 * npx * nch) return OPHPC_ERROR_INVALID_ARGUMENT;
+    if (fi.store != 1 || (fi.data_type != 9 && fi.data_type != 10)) return OPHPC_ERROR_UNSUPPORTED;
+    if (fi.code_type != 1 && fi.code_type != 2) return OPHPC_ERROR_UNSUPPORTED;   // AP or RI
+    f.seekg(fh.off_bytes, std::ios::beg);
+    const uint64_t nval = 2 * npx * nch;
+    std::vector<double> buf((size_t)nval);
+    if (fi.data_type == 10) {
+        if (!f.read((char*)buf.data(), (std::streamsize)(8 * nval))) return OPHPC_ERROR_IO;
+    } else {
+        std::vector<float> b32((size_t)nval);
+        if (!f.read((char*)b32.data(), (std::streamsize)(4 * nval))) return OPHPC_ERROR_IO;
+        for (uint64_t i = 0; i < nval; ++i) buf[i] = b32[i];
+    }
+    const uint64_t nf = npx * nch;   // values per part
+    for (uint32_t c = 0; c < nch; ++c)
+        for (uint64_t i = 0; i < npx; ++i) {
+            // colour arrangement: 2 = one plane per channel, 1 = channels interleaved per pixel
+            const uint64_t k = fi.color_arrange == 1 ? i * nch + c : c * npx + i;
+            double a = buf[k], b = buf[nf + k];
+            if (fi.code_type == 1) {   // amplitude, phase (the reference leaves the field zero here)
+                const double amp = a, ph = b;
+                a = amp * std::cos(ph);
+                b = amp * std::sin(ph);
+            }
+            field[2 * (c * npx + i) + 0] = a;
+            field[2 * (c * npx + i) + 1] = b;
+        }
+    return OPHPC_SUCCESS;
+}
+
 
 ophpc_status ophpc_read_config(const char* xml_path, ophpc_config* cfg, ophpc_image_config* img) {
     if (!xml_path || !cfg) return OPHPC_ERROR_INVALID_ARGUMENT;

@@ -14,7 +14,8 @@ meanings are the reference's (ophgen/src/ophPointCloud.h:547-698):
     h.save("hologram.bmp")
     h.release()
 
-The file helpers read_config / load_ply / save_bmp bind include/ophpc_io.h.
+The file helpers read_config / load_ply / save_bmp / save_ohc / load_ohc bind
+include/ophpc_io.h.
 """
 from __future__ import annotations
 
@@ -52,6 +53,14 @@ def _L():
         L.ophpc_load_ply.restype = ctypes.c_int64
         L.ophpc_save_bmp.argtypes = [ctypes.c_char_p, vp, i32, i32, i32, i32, i32]
         L.ophpc_save_bmp.restype = ctypes.c_int
+        L.ophpc_save_ohc.argtypes = [ctypes.c_char_p, vp, i32, i32, d, d, u32, vp]
+        L.ophpc_save_ohc.restype = ctypes.c_int
+        L.ophpc_load_ohc.argtypes = [ctypes.c_char_p, vp, vp, vp, vp, vp, vp, vp, u64]
+        L.ophpc_load_ohc.restype = ctypes.c_int
+        L.ophpc_pc_save_ohc.argtypes = [vp, ctypes.c_char_p]
+        L.ophpc_pc_save_ohc.restype = i32
+        L.ophpc_pc_load_ohc.argtypes = [vp, ctypes.c_char_p]
+        L.ophpc_pc_load_ohc.restype = i32
         L.ophpc_normalize.argtypes = [vp, vp, u32, u64, vp, vp]
         L.ophpc_normalize.restype = ctypes.c_int
         L.ophpc_pc_create.restype = vp
@@ -117,6 +126,41 @@ def save_bmp(path: str, pixels: np.ndarray, bits_per_pixel: int = 8, flip: int =
     st = _L().ophpc_save_bmp(path.encode(), p.ctypes.data, w, h, bits_per_pixel, flip, 1 if rotate else 0)
     if st != 0:
         raise OphpcError(st, f"cannot save {path}")
+
+
+def save_ohc(path: str, field: np.ndarray, pitch, wavelengths) -> None:
+    """field: complex [n_channels, pnY, pnX] (or [pnY, pnX]); written as the
+    reference's saveAsOhc writes it."""
+    f = np.asarray(field)
+    if f.ndim == 2:
+        f = f[None]
+    nch, pny, pnx = f.shape
+    buf = np.ascontiguousarray(np.stack([f.real, f.imag], axis=-1), dtype=np.float64)
+    wl = np.ascontiguousarray(np.asarray(wavelengths, dtype=np.float64).reshape(-1))
+    if wl.size != nch:
+        raise ValueError("one wavelength per channel")
+    st = _L().ophpc_save_ohc(path.encode(), buf.ctypes.data, pnx, pny, float(pitch[0]), float(pitch[1]), nch,
+                             wl.ctypes.data)
+    if st != 0:
+        raise OphpcError(st, f"cannot save {path}")
+
+
+def load_ohc(path: str):
+    """Returns (field complex [n_channels, pnY, pnX], pitch (x, y), wavelengths)."""
+    L = _L()
+    pnx, pny, nch = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint32()
+    ppx, ppy = ctypes.c_double(), ctypes.c_double()
+    wl = np.zeros(3)
+    args = [ctypes.byref(pnx), ctypes.byref(pny), ctypes.byref(ppx), ctypes.byref(ppy), ctypes.byref(nch),
+            wl.ctypes.data]
+    st = L.ophpc_load_ohc(path.encode(), *args, None, 0)
+    if st != 0:
+        raise OphpcError(st, f"cannot load {path}")
+    buf = np.zeros((nch.value, pny.value, pnx.value, 2))
+    st = L.ophpc_load_ohc(path.encode(), *args, buf.ctypes.data, buf.size)
+    if st != 0:
+        raise OphpcError(st, f"cannot load {path}")
+    return buf[..., 0] + 1j * buf[..., 1], (ppx.value, ppy.value), wl[:nch.value].copy()
 
 
 # ------------------------------------------------------------------ façade
@@ -212,6 +256,12 @@ class PointCloud:
 
     def save(self, path: str, bits_per_pixel: int = 8) -> bool:
         return bool(self._L.ophpc_pc_save(self._h, path.encode(), bits_per_pixel))
+
+    def saveAsOhc(self, path: str) -> bool:
+        return bool(self._L.ophpc_pc_save_ohc(self._h, path.encode()))
+
+    def loadAsOhc(self, path: str) -> bool:
+        return bool(self._L.ophpc_pc_load_ohc(self._h, path.encode()))
 
     def lastError(self) -> str:
         e = self._L.ophpc_pc_last_error(self._h)

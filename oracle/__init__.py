@@ -227,6 +227,12 @@ def _load_ref():
             lib.ophref_run_save.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_uint,
                                             ctypes.c_uint, ctypes.c_char_p, ctypes.c_int]
             lib.ophref_run_save.restype = ctypes.c_int
+            lib.ophref_run_save_ohc.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_uint,
+                                                ctypes.c_char_p]
+            lib.ophref_run_save_ohc.restype = ctypes.c_int
+            lib.ophref_load_ohc.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_ulonglong]
+            lib.ophref_load_ohc.restype = ctypes.c_int
             lib.ophref_load_ply.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong]
             lib.ophref_load_ply.restype = ctypes.c_longlong
             _ref = lib
@@ -275,6 +281,37 @@ def ref_run_save(xml_path: str, vertices: np.ndarray, diff_flag: int, encode_fla
                                  bmp_path.encode(), bits_per_pixel)
     if rc != 0:
         raise RuntimeError(f"ophref_run_save failed ({rc})")
+
+
+def ref_run_save_ohc(xml_path: str, vertices: np.ndarray, diff_flag: int, ohc_path: str) -> None:
+    """Reference generate -> saveAsOhc(ohc_path)."""
+    lib = _load_ref()
+    v = _vertices(vertices)
+    with _QuietStdout():
+        rc = lib.ophref_run_save_ohc(xml_path.encode(), v.ctypes.data, v.shape[0], diff_flag, ohc_path.encode())
+    if rc != 0:
+        raise RuntimeError(f"ophref_run_save_ohc failed ({rc})")
+
+
+def ref_load_ohc(ohc_path: str):
+    """Reference loadAsOhc -> (field [ch, pnY, pnX] complex, pitch[2], wavelengths[ch])."""
+    lib = _load_ref()
+    shape = np.zeros(3, dtype=np.int32)
+    pitch = np.zeros(2)
+    wl = np.zeros(3)
+    with _QuietStdout():
+        rc = lib.ophref_load_ohc(ohc_path.encode(), shape.ctypes.data, pitch.ctypes.data, wl.ctypes.data, None, 0)
+    if rc != 0:
+        raise RuntimeError(f"ophref_load_ohc failed ({rc})")
+    pnx, pny, nch = (int(x) for x in shape)
+    buf = np.zeros(2 * pnx * pny * nch)
+    with _QuietStdout():
+        rc = lib.ophref_load_ohc(ohc_path.encode(), shape.ctypes.data, pitch.ctypes.data, wl.ctypes.data,
+                                 buf.ctypes.data, buf.size)
+    if rc != 0:
+        raise RuntimeError(f"ophref_load_ohc failed ({rc})")
+    f = buf.reshape(nch, pny, pnx, 2)
+    return f[..., 0] + 1j * f[..., 1], pitch, wl[:nch]
 
 
 def ref_run(xml_path: str, vertices: Optional[np.ndarray] = None, ply_path: Optional[str] = None,

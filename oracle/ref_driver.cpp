@@ -130,4 +130,45 @@ int ophref_run_save(const char* xml_path, const void* vertices, unsigned long lo
     return h.pc->save(bmp_path, (uint8_t)bits_per_pixel) ? 0 : -3;
 }
 
+// Runs the reference generate and writes the complex field with
+// Openholo::saveAsOhc (Openholo/src/Openholo.cpp:252-279). Returns 0 on success.
+int ophref_run_save_ohc(const char* xml_path, const void* vertices, unsigned long long n_points,
+                        unsigned diff_flag, const char* ohc_path)
+{
+    Holder h;
+    h.pc = new ophPointCloud();
+    if (!h.pc->readConfig(xml_path)) return -1;
+    h.pc->setNumberOfPoints(n_points);
+    h.pc->setPointCloudModel((Vertex*)vertices);
+    h.pc->SetMode(MODE_CPU);
+    h.pc->generateHologram(diff_flag);
+    return h.pc->saveAsOhc(ohc_path) ? 0 : -3;
+}
+
+// Loads a .ohc with Openholo::loadAsOhc (Openholo/src/Openholo.cpp:280-319)
+// and copies out the shape (shape[0..2] = pnX, pnY, channels), pitch[2],
+// wavelengths[3] and, when field is non-NULL and cap_doubles suffices,
+// complex_H as [channel][re, im per pixel]. Returns 0 on success.
+int ophref_load_ohc(const char* ohc_path, int* shape, double* pitch, double* wavelengths, double* field,
+                    unsigned long long cap_doubles)
+{
+    Holder h;
+    h.pc = new ophPointCloud();
+    if (!h.pc->loadAsOhc(ohc_path)) return -1;
+    OphConfig& c = h.pc->getContext();
+    shape[0] = c.pixel_number[_X];
+    shape[1] = c.pixel_number[_Y];
+    shape[2] = (int)c.waveNum;
+    pitch[0] = c.pixel_pitch[_X];
+    pitch[1] = c.pixel_pitch[_Y];
+    for (unsigned i = 0; i < c.waveNum && i < 3; ++i) wavelengths[i] = c.wave_length[i];
+    const unsigned long long pnXY = (unsigned long long)shape[0] * shape[1];
+    if (field && cap_doubles >= 2 * pnXY * c.waveNum) {
+        Complex<Real>** H = h.pc->getComplexField();
+        for (unsigned ch = 0; ch < c.waveNum; ++ch)
+            std::memcpy(field + 2 * pnXY * ch, H[ch], sizeof(double) * 2 * pnXY);
+    }
+    return 0;
+}
+
 }  // extern "C"

@@ -102,6 +102,63 @@ def write_ply_binary(path, xyz, rgb, phase, with_channel=True):
                                 int(rgb[i, 2]), phase[i]))
 
 
+def write_ohc(path, field, pitch, wavelengths, arrange=2, dtype=10, code=2):
+    """A .ohc in the reference's layout (Openholo/src/ImgCodecDefine.h:53-210):
+    24-byte file header, 65-byte field-info header, wavelength table, then the
+    first part (real or amplitude) of every pixel of every channel, then the
+    second. arrange 2: one plane per channel; 1: channels interleaved per
+    pixel. dtype 10: float64, 9: float32. code 2: real/imaginary,
+    1: amplitude/phase."""
+    nch, pny, pnx = field.shape
+    if code == 2:
+        a, b = field.real, field.imag
+    else:
+        a, b = np.abs(field), np.angle(field)
+    if arrange == 2:
+        a, b = a.reshape(-1), b.reshape(-1)
+    else:
+        a, b = a.reshape(nch, -1).T.reshape(-1), b.reshape(nch, -1).T.reshape(-1)
+    np_t = np.float64 if dtype == 10 else np.float32
+    data = np.concatenate([a, b]).astype(np_t).tobytes()
+    info_size = 65 + 8 * nch
+    info = struct.pack("<IIIddBIBBBBBBBddQB", info_size, pnx, pny, pitch[0], pitch[1], 1, nch, 2 if nch > 1 else 1,
+                       arrange, 1, dtype, 1, code, 0, -1.0, 1.0, len(data), 0)
+    head = struct.pack("<2sQBBIII", b"OH", 24 + info_size + len(data), 3, 0, 0, 0, 24 + info_size)
+    with open(path, "wb") as f:
+        f.write(head + info + np.asarray(wavelengths, dtype=np.float64).tobytes() + data)
+
+
+def make_ohc(xml):
+    """OHC fixtures; xml is a scratch path for the config file."""
+    out = {}
+    # OHC: the reference's saveAsOhc output for a one- and a
+    # three-channel field, and what its loadAsOhc reads back from it.
+    ohc_cases = {"ohc_1ch_fresnel": "fresnel_window_1ch", "ohc_3ch_rs": "rs_3ch_vw"}
+    for name, case in ohc_cases.items():
+        g, v, diff, _ = FIELD_CASES[case]
+        small = oracle.Geometry(pnx=40, pny=24, ppx=g.ppx, ppy=g.ppy, wavelengths=g.wavelengths,
+                                scale=g.scale, distance=g.distance)
+        with open(xml, "w") as f:
+            f.write(small.xml())
+        path = os.path.join(HERE, name + ".ohc")
+        oracle.ref_run_save_ohc(xml, v, diff, path)
+        field, pitch, wl = oracle.ref_load_ohc(path)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), field=field, pitch=pitch, wavelengths=wl)
+        out[name] = os.path.getsize(path)
+    # Layouts the reference reads but does not write: channels
+    # interleaved per pixel, float32; the reference's reading of each.
+    rng = np.random.default_rng(11)
+    fld = rng.normal(size=(3, 6, 10)) + 1j * rng.normal(size=(3, 6, 10))
+    variants = {}
+    for vname, kw in {"seqt_f64": dict(arrange=1), "each_f32": dict(dtype=9),
+                      "seqt_f32": dict(arrange=1, dtype=9)}.items():
+        path = os.path.join(HERE, f"ohc_{vname}.ohc")
+        write_ohc(path, fld, (4e-6, 5e-6), [638e-9, 532e-9, 473e-9], **kw)
+        variants[vname] = oracle.ref_load_ohc(path)[0]
+    np.savez_compressed(os.path.join(HERE, "ohc_variants.npz"), source=fld, **variants)
+    return out
+
+
 def main():
     if not oracle.ref_available():
         oracle.build(with_reference=True)
@@ -177,9 +234,17 @@ def main():
             field, _, codes, _ = oracle.ref_run(xml, vertices=v, diff_flag=0, encode_flag=0)
             np.savez_compressed(os.path.join(HERE, name + ".npz"), vertices=v, xml=g.xml(), bpp=bpp)
             out[name] = os.path.getsize(bmp)
+
+        out.update(make_ohc(xml))
     for k, v in out.items():
         print(k, v)
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["ohc"]:   # only the OHC fixtures
+        if not oracle.ref_available():
+            oracle.build(with_reference=True)
+        with tempfile.TemporaryDirectory() as d:
+            print(make_ohc(os.path.join(d, "cfg.xml")))
+    else:
+        main()

@@ -150,3 +150,82 @@ def test_bmp_flip_and_rotate(tmp_path):
     P.save_bmp(str(tmp_path / "r.bmp"), pix, 8, rotate=True)
     got, _, _, _ = _bmp_pixels(open(tmp_path / "r.bmp", "rb").read())
     assert np.array_equal(got, pix[::-1, ::-1])
+
+
+# ------------------------------------------------------------------ OHC
+
+@pytest.mark.parametrize("name", ["ohc_1ch_fresnel", "ohc_3ch_rs"])
+def test_ohc_reader_matches_reference(name):
+    want = np.load(os.path.join(GOLD, name + ".npz"))
+    field, pitch, wl = P.load_ohc(os.path.join(GOLD, name + ".ohc"))
+    assert np.array_equal(field, want["field"])
+    assert np.array_equal(np.asarray(pitch), want["pitch"])
+    assert np.array_equal(wl, want["wavelengths"])
+
+
+@pytest.mark.parametrize("name", ["ohc_1ch_fresnel", "ohc_3ch_rs"])
+def test_ohc_writer_byte_identical(tmp_path, name):
+    """The reference's saveAsOhc file, rewritten from the field it holds."""
+    ref = open(os.path.join(GOLD, name + ".ohc"), "rb").read()
+    want = np.load(os.path.join(GOLD, name + ".npz"))
+    out = tmp_path / "o"                      # ".ohc" appended
+    P.save_ohc(str(out), want["field"], want["pitch"], want["wavelengths"])
+    assert open(str(out) + ".ohc", "rb").read() == ref
+
+
+@pytest.mark.parametrize("variant", ["seqt_f64", "each_f32", "seqt_f32"])
+def test_ohc_reader_layouts(variant):
+    """Channels interleaved per pixel and float32 data, read as the
+    reference's decoder reads them."""
+    z = np.load(os.path.join(GOLD, "ohc_variants.npz"))
+    field, pitch, wl = P.load_ohc(os.path.join(GOLD, f"ohc_{variant}.ohc"))
+    assert np.array_equal(field, z[variant])
+    assert pitch == (4e-6, 5e-6)
+    assert np.array_equal(wl, [638e-9, 532e-9, 473e-9])
+
+
+def _ohc_bytes(field, arrange=2, dtype=10, code=2, nwl=None):
+    nch = field.shape[0] if nwl is None else nwl
+    a, b = (field.real, field.imag) if code == 2 else (np.abs(field), np.angle(field))
+    data = np.concatenate([a.reshape(-1), b.reshape(-1)]).astype(np.float64 if dtype == 10 else np.float32)
+    info = struct.pack("<IIIddBIBBBBBBBddQB", 65 + 8 * nch, field.shape[2], field.shape[1], 1e-6, 1e-6, 1, nch, 2,
+                       arrange, 1, dtype, 1, code, 0, -1.0, 1.0, data.nbytes, 0)
+    head = struct.pack("<2sQBBIII", b"OH", 24 + len(info) + 8 * nch + data.nbytes, 3, 0, 0, 0,
+                       24 + len(info) + 8 * nch)
+    return head + info + np.full(nch, 5e-7).tobytes() + data.tobytes()
+
+
+def test_ohc_amplitude_phase_and_errors(tmp_path):
+    rng = np.random.default_rng(3)
+    f = rng.normal(size=(1, 4, 5)) + 1j * rng.normal(size=(1, 4, 5))
+    p = tmp_path / "ap.ohc"
+    p.write_bytes(_ohc_bytes(f, code=1))
+    got, _, _ = P.load_ohc(str(p))
+    assert np.allclose(got, f, rtol=0, atol=1e-12)
+    # amplitude-only coding, truncated data, bad signature, too many channels
+    bad = {"ae.ohc": _ohc_bytes(f, code=3), "short.ohc": _ohc_bytes(f)[:-8],
+           "sig.ohc": b"XX" + _ohc_bytes(f)[2:], "nch.ohc": _ohc_bytes(np.zeros((4, 2, 2)))}
+    for name, raw in bad.items():
+        (tmp_path / name).write_bytes(raw)
+        with pytest.raises(Exception):
+            P.load_ohc(str(tmp_path / name))
+    with pytest.raises(Exception):
+        P.load_ohc(str(tmp_path / "missing.ohc"))
+    with pytest.raises(Exception):
+        P.save_ohc(str(tmp_path / "x.ohc"), np.zeros((4, 2, 2)), (1e-6, 1e-6), [5e-7] * 4)
+
+
+def test_facade_ohc_roundtrip(tmp_path):
+    """PointCloud.loadAsOhc replaces the context and complex field;
+    saveAsOhc writes the reference's bytes back (no GPU needed)."""
+    src = os.path.join(GOLD, "ohc_3ch_rs.ohc")
+    want = np.load(os.path.join(GOLD, "ohc_3ch_rs.npz"))
+    with P.PointCloud() as h:
+        assert h.loadAsOhc(src)
+        c = h.getConfig()
+        assert (c.pixel_number[0], c.pixel_number[1], c.n_channels) == (40, 24, 3)
+        assert np.array_equal(list(c.wave_length), want["wavelengths"])
+        assert np.array_equal(h.getComplexField(), want["field"])
+        assert h.saveAsOhc(str(tmp_path / "back.ohc"))
+        assert not h.loadAsOhc(str(tmp_path / "missing"))
+    assert open(tmp_path / "back.ohc", "rb").read() == open(src, "rb").read()
