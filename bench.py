@@ -56,8 +56,8 @@ def parse():
     ap.add_argument("--cpu-points", type=int, default=0, help="points in the CPU sample (0 = auto)")
     ap.add_argument("--serving-jobs", type=int, default=64, help="jobs in the serving stream (512 = full)")
     ap.add_argument("--profile-case", default=None,
-                    help="run one small fixed case for a profiler and exit: rs_1k, fresnel_1k, tc_fp16_4k, "
-                         "tc_bf16x3_4k (box_4k distribution, 131,072 points)")
+                    help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
+                         "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points)")
     ap.add_argument("--serving-max-points", type=int, default=100_000,
                     help="largest point count of a serving job (500000 = full)")
     return ap.parse_args()
@@ -470,6 +470,8 @@ def profile_case(name: str) -> None:
     from openholo_gb300 import workloads
     if name in ("rs_1k", "fresnel_1k"):
         w, diff, mode = workloads.rs_1k(), (0 if name == "rs_1k" else 1), 0
+    elif name == "rs_fhd":   # the headline step's generate: ~110 MB on the device
+        w, diff, mode = workloads.sphere_fhd(), 0, 0
     elif name in ("tc_fp16_4k", "tc_bf16x3_4k"):
         w = workloads.box_4k(n_points=131_072)
         diff = 1

@@ -23,9 +23,11 @@
  *     output; OPHPC_MODE_TENSOR_* selects the tensor-core Fresnel kernel;
  *   - errors are reported through return values and lastError(), never by
  *     exiting the process;
- *   - encoding() supports ENCODE_PHASE, ENCODE_AMPLITUDE, ENCODE_REAL and
- *     ENCODE_IMAGINARY (the encoders of the point-cloud path); other flags
- *     log and do nothing, as an unknown flag does in the reference.
+ *   - encoding() supports ENCODE_PHASE, ENCODE_AMPLITUDE, ENCODE_REAL,
+ *     ENCODE_IMAGINARY, ENCODE_SIMPLENI, ENCODE_BURCKHARDT and
+ *     ENCODE_TWOPHASE on the GPU; the FFT-based SSB / off-axis and the
+ *     binary encoders log and do nothing, as an unknown flag does in the
+ *     reference.
  */
 #ifndef OPHPC_OPHPOINTCLOUD_H
 #define OPHPC_OPHPOINTCLOUD_H

@@ -68,6 +68,9 @@ typedef enum ophpc_status {
 #define OPHPC_ENCODE_AMPLITUDE 1u
 #define OPHPC_ENCODE_REAL 2u
 #define OPHPC_ENCODE_IMAGINARY 3u
+#define OPHPC_ENCODE_SIMPLENI 4u
+#define OPHPC_ENCODE_BURCKHARDT 5u
+#define OPHPC_ENCODE_TWOPHASE 6u
 
 /* Vertex (Openholo/src/struct.h:86-106): packed pos[3], color[3], phase —
  * 56 bytes, colour channels in [0, 1]; color[ch] is channel ch's amplitude. */
@@ -137,7 +140,14 @@ ophpc_status ophpc_generate_host(ophpc_context* ctx, const ophpc_config* cfg,
  * d_field: [n_channels][n_pixels][re, im] doubles. d_encoded (optional,
  * NULL to skip): [n_channels][n_pixels] doubles = m_lpEncoded.
  * d_normalized (optional): [n_channels][n_pixels] bytes = m_lpNormalized,
- * using the min/max over all channels. Asynchronous on `stream`. */
+ * using the min/max over all channels. encode_flag: PHASE, AMPLITUDE, REAL,
+ * IMAGINARY, SIMPLENI, BURCKHARDT or TWOPHASE (ophGen.cpp:1821-1974);
+ * the last three work per channel on the field divided by its largest
+ * sampled magnitude. BURCKHARDT writes two of every three entries and
+ * TWOPHASE the first 2*(n_pixels/2): the others keep what d_encoded held
+ * (as m_lpEncoded keeps an earlier encoding in the reference), or count as
+ * 0 when d_encoded is NULL. Other flags (SSB, off-axis, binary) are
+ * OPHPC_ERROR_UNSUPPORTED. Asynchronous on `stream`. */
 ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_channels,
                           uint64_t n_pixels, uint32_t encode_flag, double* d_encoded,
                           uint8_t* d_normalized, void* stream);

@@ -13,7 +13,8 @@ import os
 from typing import Optional, Sequence
 
 from ._abi import (  # noqa: F401
-    DIFF_FRESNEL, DIFF_RS, ENCODE_AMPLITUDE, ENCODE_IMAGINARY, ENCODE_PHASE, ENCODE_REAL, MODE_CPU,
+    DIFF_FRESNEL, DIFF_RS, ENCODE_AMPLITUDE, ENCODE_BURCKHARDT, ENCODE_IMAGINARY, ENCODE_PHASE, ENCODE_REAL,
+    ENCODE_SIMPLENI, ENCODE_TWOPHASE, MODE_CPU,
     MODE_DOUBLE, MODE_FASTMATH, MODE_FLOAT, MODE_GPU, MODE_TENSOR_BF16X3, MODE_TENSOR_FP16, OphpcConfig,
     OphpcError, STATUS, lib, lib_path, make_config,
 )
@@ -22,7 +23,7 @@ __all__ = [
     "Context", "OphpcConfig", "OphpcError", "make_config", "lib", "lib_path",
     "DIFF_RS", "DIFF_FRESNEL", "MODE_CPU", "MODE_GPU", "MODE_DOUBLE", "MODE_FLOAT", "MODE_FASTMATH",
     "MODE_TENSOR_FP16", "MODE_TENSOR_BF16X3", "ENCODE_PHASE", "ENCODE_AMPLITUDE", "ENCODE_REAL",
-    "ENCODE_IMAGINARY",
+    "ENCODE_IMAGINARY", "ENCODE_SIMPLENI", "ENCODE_BURCKHARDT", "ENCODE_TWOPHASE",
 ]
 
 

@@ -21,6 +21,9 @@ ENCODE_PHASE = 0
 ENCODE_AMPLITUDE = 1
 ENCODE_REAL = 2
 ENCODE_IMAGINARY = 3
+ENCODE_SIMPLENI = 4
+ENCODE_BURCKHARDT = 5
+ENCODE_TWOPHASE = 6
 
 STATUS = {
     0: "success", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "I/O error",

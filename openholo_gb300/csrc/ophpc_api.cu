@@ -384,8 +384,9 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
     if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->last_error.clear();
-    if (encode_flag > OPHPC_ENCODE_IMAGINARY)
-        return fail(ctx, OPHPC_ERROR_UNSUPPORTED, "encode_flag: phase, amplitude, real or imaginary only");
+    if (encode_flag > OPHPC_ENCODE_TWOPHASE)
+        return fail(ctx, OPHPC_ERROR_UNSUPPORTED,
+                    "encode_flag: phase, amplitude, real, imaginary, SimpleNI, Burckhardt or TwoPhase only");
     if (n_channels < 1 || n_channels > OPHPC_MAX_CHANNELS)
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "n_channels must be 1..3");
     if (n_pixels == 0) return OPHPC_SUCCESS;
@@ -397,11 +398,23 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_normalized must be device memory");
     cudaStream_t s = (cudaStream_t)stream;
     unsigned long long* d_mm = nullptr;
-    cudaError_t e = pool_alloc(ctx, &d_mm, 2 * sizeof(unsigned long long), s);
+    cudaError_t e = pool_alloc(ctx, &d_mm, 8 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation (min/max)");
-    launch_encode((const double2*)d_field, (int)n_channels, (int64_t)n_pixels, (int)encode_flag, d_encoded,
-                  d_normalized, d_mm, s);
+    double* d_tmp = nullptr;
+    if (encode_flag >= OPHPC_ENCODE_SIMPLENI && !d_encoded) {
+        const size_t bytes = sizeof(double) * (size_t)n_channels * (size_t)n_pixels;
+        e = pool_alloc(ctx, &d_tmp, bytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_tmp, 0, bytes, s);
+        if (e != cudaSuccess) {
+            if (d_tmp) cudaFreeAsync(d_tmp, s);
+            cudaFreeAsync(d_mm, s);
+            return cuda_fail(ctx, e, "scratch allocation (encoded)");
+        }
+    }
+    launch_encode((const double2*)d_field, (int)n_channels, (int64_t)n_pixels, (int)encode_flag,
+                  d_tmp ? d_tmp : d_encoded, d_normalized, d_mm, s);
     e = cudaGetLastError();
+    if (d_tmp) cudaFreeAsync(d_tmp, s);
     cudaFreeAsync(d_mm, s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "encode launch");
     return OPHPC_SUCCESS;

@@ -133,6 +133,9 @@ void launch_fresnel(const PointRec* d_recs, const JobGeom& jg, double2* d_field,
                     cudaStream_t stream);
 void launch_sum_partials(const JobGeom& jg, double2* d_field, const double2* d_partials,
                          cudaStream_t stream);
+// d_minmax: 5 words of device scratch (global min/max + per-channel |H|
+// maxima). For SIMPLENI, BURCKHARDT and TWOPHASE d_encoded is required and
+// in/out (entries the encoder skips keep their value).
 void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int encode_flag,
                    double* d_encoded, uint8_t* d_normalized, unsigned long long* d_minmax,
                    cudaStream_t stream);

@@ -17,6 +17,7 @@
 // All FP64 arithmetic uses explicit _rn operations (no FMA) to round exactly
 // as the x86-64 reference does.
 #include "pc_common.cuh"
+#include "ophpc.h"
 
 #include <cfloat>
 
@@ -135,10 +136,109 @@ __global__ void __launch_bounds__(256) normalize_kernel(const double2* __restric
     }
 }
 
-__global__ void init_minmax_kernel(unsigned long long* minmax) {
+// n_words 2: the global min/max; 5: also the per-channel |H| maxima of the
+// normalising encoders (words 2..4)
+__global__ void init_minmax_kernel(unsigned long long* minmax, int n_words) {
     // initial values MAX_DOUBLE / MIN_DOUBLE of minOfArr / maxOfArr
     minmax[0] = ordered_bits(kMaxDouble);
-    minmax[1] = ordered_bits(kMinDouble);
+    for (int k = 1; k < n_words; ++k) minmax[k] = ordered_bits(kMinDouble);
+}
+
+// ---------------------------------------------------------------------------
+// Encoders that normalise the field by its largest magnitude first, one
+// channel at a time as ophGen::encoding calls them (ophGen.cpp:845-847):
+//   SimpleNI   (ophGen.cpp:1955-1974): m = max |H|; e = |H + m|^2 for every
+//              pixel (the sqrt is squared again, as the reference does);
+//   Burckhardt (ophGen.cpp:1897-1953): every third pixel H[3i], i < n/3,
+//              divided by max |H[3i]|; its phase code p = (arg + pi)/(2 pi)
+//              (in [0, 1]) and magnitude a pick one of three 120-degree
+//              sectors compared in radians, so only the first is reached;
+//              two of the three entries 3i..3i+2 are written;
+//   TwoPhase   (ophGen.cpp:1866-1895): H[2i], i < n/2, divided by
+//              max |H[2i]|; e[2i] = (p + pi) + acos(a), e[2i+1] = (p + pi) - acos(a).
+// Entries an encoder does not write keep what the encoded buffer held.
+// Launches: absmax over the sampled pixels (grid.y = channel, atomicMax on
+// the ordered image of non-negative doubles), then the encoder; the 8-bit
+// codes come from the generic minmax + normalize pair over the buffer.
+
+__device__ __forceinline__ double mag_rn(double re, double im) {
+    return __dsqrt_rn(__dadd_rn(__dmul_rn(re, re), __dmul_rn(im, im)));
+}
+
+__device__ __forceinline__ int64_t sample_count(int64_t n, int flag) {
+    return flag == OPHPC_ENCODE_BURCKHARDT ? n / 3 : (flag == OPHPC_ENCODE_TWOPHASE ? n >> 1 : n);
+}
+
+__global__ void __launch_bounds__(256) chan_absmax_kernel(const double2* __restrict__ field, int64_t n_pixels,
+                                                          int flag, unsigned long long* __restrict__ absmax) {
+    const int c = blockIdx.y;
+    const int64_t count = sample_count(n_pixels, flag);
+    const int64_t stride = flag == OPHPC_ENCODE_BURCKHARDT ? 3 : (flag == OPHPC_ENCODE_TWOPHASE ? 2 : 1);
+    const double2* f = field + (int64_t)c * n_pixels;
+    double mx = kMinDouble;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 h = f[i * stride];
+        const double a = mag_rn(h.x, h.y);
+        if (a > mx) mx = a;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double s_mx[8];
+    if ((threadIdx.x & 31) == 0) s_mx[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) mx = fmax(mx, s_mx[k]);
+        atomicMax(&absmax[c], ordered_bits(mx));
+    }
+}
+
+__global__ void __launch_bounds__(256) encode_normalised_kernel(const double2* __restrict__ field, int64_t n_pixels,
+                                                                int flag,
+                                                                const unsigned long long* __restrict__ absmax,
+                                                                double* __restrict__ encoded) {
+    const int c = blockIdx.y;
+    const double m = from_ordered(absmax[c]);
+    const double2* f = field + (int64_t)c * n_pixels;
+    double* e = encoded + (int64_t)c * n_pixels;
+    const int64_t count = sample_count(n_pixels, flag);
+    const double pi2 = kPi * 2, sqrt3 = __dsqrt_rn(3.0);
+    const double third = __ddiv_rn(pi2, 3.0), two_thirds = __ddiv_rn(kPi * 4, 3.0);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (flag == OPHPC_ENCODE_SIMPLENI) {
+            const double2 h = f[i];
+            const double t = mag_rn(__dadd_rn(h.x, m), h.y);
+            e[i] = __dmul_rn(t, t);
+            continue;
+        }
+        const double2 h = f[flag == OPHPC_ENCODE_BURCKHARDT ? 3 * i : 2 * i];
+        const double re = __ddiv_rn(h.x, m), im = __ddiv_rn(h.y, m);
+        const double p = __ddiv_rn(__dadd_rn(atan2(im, re), kPi), pi2);
+        const double a = mag_rn(re, im);
+        if (flag == OPHPC_ENCODE_TWOPHASE) {
+            const double d = acos(a), base = __dadd_rn(p, kPi);
+            e[2 * i] = __dadd_rn(base, d);
+            e[2 * i + 1] = __dsub_rn(base, d);
+            continue;
+        }
+        // Burckhardt: a * (cos q + sin q / sqrt3) and 2 sin q / sqrt3 for the
+        // sector's q, into the sector's two entries
+        double q;
+        int lo, hi;
+        if (p >= 0 && p < third) {
+            q = p, lo = 0, hi = 1;
+        } else if (p >= third && p < two_thirds) {
+            q = __dsub_rn(p, third), lo = 1, hi = 2;
+        } else if (p >= two_thirds && p < pi2) {
+            q = __dsub_rn(p, two_thirds), lo = 2, hi = 0;
+        } else {
+            continue;
+        }
+        const double sq = sin(q), cq = cos(q);
+        e[3 * i + lo] = __dmul_rn(a, __dadd_rn(cq, __ddiv_rn(sq, sqrt3)));
+        e[3 * i + hi] = __ddiv_rn(__dmul_rn(2.0, sq), sqrt3);
+    }
 }
 
 }  // namespace
@@ -159,7 +259,7 @@ void launch_normalize(const double* d_encoded, int n_channels, int64_t n_pixels,
     if (n <= 0) return;
     const int threads = 256, blocks = grid_for(n, threads);
     count_launches(3);
-    init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
+    init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax, 2);
     minmax_kernel<<<blocks, threads, 0, stream>>>(d_encoded, n, d_minmax);
     normalize_kernel<<<blocks, threads, 0, stream>>>(nullptr, d_encoded, n, 0, d_minmax, d_normalized);
 }
@@ -170,8 +270,23 @@ void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int
     const int64_t n = (int64_t)n_channels * n_pixels;
     if (n <= 0) return;
     const int threads = 256, blocks = grid_for(n, threads);
+    if (encode_flag >= (int)OPHPC_ENCODE_SIMPLENI) {
+        // d_encoded is required (the caller provides scratch) and in/out
+        const int per = grid_for(n_pixels, threads);
+        const dim3 grid((unsigned)per, (unsigned)n_channels);
+        count_launches(d_normalized ? 5 : 3);
+        init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax, 5);
+        chan_absmax_kernel<<<grid, threads, 0, stream>>>(d_field, n_pixels, encode_flag, d_minmax + 2);
+        encode_normalised_kernel<<<grid, threads, 0, stream>>>(d_field, n_pixels, encode_flag, d_minmax + 2,
+                                                              d_encoded);
+        if (d_normalized) {
+            minmax_kernel<<<blocks, threads, 0, stream>>>(d_encoded, n, d_minmax);
+            normalize_kernel<<<blocks, threads, 0, stream>>>(nullptr, d_encoded, n, 0, d_minmax, d_normalized);
+        }
+        return;
+    }
     count_launches(d_normalized ? 3 : 2);
-    init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
+    init_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax, 2);
     encode_minmax_kernel<<<blocks, threads, 0, stream>>>(d_field, n, encode_flag, d_encoded, d_minmax);
     if (d_normalized)
         normalize_kernel<<<blocks, threads, 0, stream>>>(d_field, d_encoded, n, encode_flag, d_minmax,

@@ -266,7 +266,7 @@ Real ophPointCloud::generateHologram(uint diff_flag) {
 }
 
 void ophPointCloud::encoding(unsigned int flag) {
-    if (flag > ENCODE_IMAGINARY) {
+    if (flag > ENCODE_TWOPHASE) {
         OPH_LOG("<FAILED> WRONG PARAMETERS.\n");
         return;
     }
@@ -277,6 +277,10 @@ void ophPointCloud::encoding(unsigned int flag) {
         return;
     for (uint ch = 0; ch < nch; ++ch)
         cudaMemcpy((double*)d_field_ + 2 * plane * ch, complex_H_[ch], sizeof(double) * 2 * plane, cudaMemcpyHostToDevice);
+    // Burckhardt and TwoPhase leave some entries of m_lpEncoded as they were
+    if (flag == ENCODE_BURCKHARDT || flag == ENCODE_TWOPHASE)
+        for (uint ch = 0; ch < nch; ++ch)
+            cudaMemcpy((double*)d_encoded_ + plane * ch, encoded_[ch], sizeof(double) * plane, cudaMemcpyHostToDevice);
     if (ophpc_encode(gpu_, (const double*)d_field_, nch, plane, flag, (double*)d_encoded_, nullptr, nullptr) !=
         OPHPC_SUCCESS) {
         last_error_ = std::string("encode: ") + ophpc_last_error(gpu_);

@@ -29,6 +29,7 @@ from ._abi import OphpcConfig, OphpcError, lib
 PC_DIFF_RS = 0
 PC_DIFF_FRESNEL = 1
 ENCODE_PHASE, ENCODE_AMPLITUDE, ENCODE_REAL, ENCODE_IMAGINARY = 0, 1, 2, 3
+ENCODE_SIMPLENI, ENCODE_BURCKHARDT, ENCODE_TWOPHASE = 4, 5, 6
 
 
 class ImageConfig(ctypes.Structure):
@@ -173,6 +174,9 @@ class PointCloud:
     ENCODE_AMPLITUDE = ENCODE_AMPLITUDE
     ENCODE_REAL = ENCODE_REAL
     ENCODE_IMAGINARY = ENCODE_IMAGINARY
+    ENCODE_SIMPLENI = ENCODE_SIMPLENI
+    ENCODE_BURCKHARDT = ENCODE_BURCKHARDT
+    ENCODE_TWOPHASE = ENCODE_TWOPHASE
 
     def __init__(self, pc_file: Optional[str] = None, cfg_file: Optional[str] = None):
         self._L = _L()

@@ -182,13 +182,21 @@ def field_at(geom: Geometry, vertices: np.ndarray, diff_flag: int, channel: int,
     return out[:, 0] + 1j * out[:, 1]
 
 
-def encode(field: np.ndarray, encode_flag: int) -> np.ndarray:
+def encode(field: np.ndarray, encode_flag: int, prior: Optional[np.ndarray] = None) -> np.ndarray:
+    """field: [n_channels, ...] complex (or one channel). Each channel is
+    encoded on its own, as ophGen::encoding does; entries an encoder leaves
+    alone (Burckhardt, TwoPhase) keep `prior` (zeros by default)."""
     lib = _load_oracle()
     f = np.ascontiguousarray(field, dtype=np.complex128)
-    flat = f.reshape(-1).view(np.float64)
-    out = np.empty(f.size, dtype=np.float64)
-    if lib.oracle_encode(_p(flat), f.size, encode_flag, _p(out)) != 0:
-        raise ValueError("oracle_encode rejected its arguments")
+    chans = f.reshape(f.shape[0], -1) if f.ndim > 2 else f.reshape(1, -1)
+    out = np.zeros(chans.shape, dtype=np.float64) if prior is None else \
+        np.ascontiguousarray(prior, dtype=np.float64).reshape(chans.shape).copy()
+    for c in range(chans.shape[0]):
+        flat = np.ascontiguousarray(chans[c]).view(np.float64)
+        oc = np.ascontiguousarray(out[c])
+        if lib.oracle_encode(_p(flat), chans.shape[1], encode_flag, _p(oc)) != 0:
+            raise ValueError("oracle_encode rejected its arguments")
+        out[c] = oc
     return out.reshape(f.shape)
 
 
@@ -233,6 +241,9 @@ def _load_ref():
             lib.ophref_load_ohc.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                             ctypes.c_void_p, ctypes.c_ulonglong]
             lib.ophref_load_ohc.restype = ctypes.c_int
+            lib.ophref_encode_field.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_uint,
+                                                ctypes.c_void_p, ctypes.c_void_p]
+            lib.ophref_encode_field.restype = ctypes.c_int
             lib.ophref_load_ply.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong]
             lib.ophref_load_ply.restype = ctypes.c_longlong
             _ref = lib
@@ -291,6 +302,22 @@ def ref_run_save_ohc(xml_path: str, vertices: np.ndarray, diff_flag: int, ohc_pa
         rc = lib.ophref_run_save_ohc(xml_path.encode(), v.ctypes.data, v.shape[0], diff_flag, ohc_path.encode())
     if rc != 0:
         raise RuntimeError(f"ophref_run_save_ohc failed ({rc})")
+
+
+def ref_encode_field(xml_path: str, field: np.ndarray, encode_flag: int, pre_flag: int = -1):
+    """Reference encoding(encode_flag) + normalize of a given field
+    ([n_channels, pnY, pnX] complex; shape from the config) ->
+    (encoded [n_channels, pnY, pnX], codes uint8)."""
+    lib = _load_ref()
+    f = np.ascontiguousarray(field, dtype=np.complex128)
+    enc = np.zeros(f.shape, dtype=np.float64)
+    codes = np.zeros(f.shape, dtype=np.uint8)
+    with _QuietStdout():
+        rc = lib.ophref_encode_field(xml_path.encode(), f.ctypes.data, pre_flag, encode_flag, enc.ctypes.data,
+                                     codes.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"ophref_encode_field failed ({rc})")
+    return enc, codes
 
 
 def ref_load_ohc(ohc_path: str):

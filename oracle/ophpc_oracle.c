@@ -230,21 +230,83 @@ int oracle_field_at(const oracle_config* c, const double* vertices, int64_t n_po
     return 0;
 }
 
+/* |z| as Complex<T>::mag / oph::absCplx: sqrt(re*re + im*im). */
+static double ora_mag(double re, double im) { return sqrt(re * re + im * im); }
+
+/* oph::maxOfArr over |field[i * stride]|, i < count (function.h:93-99,
+ * 176-186): starts at MIN_DOUBLE, strict '>'. */
+static double ora_absmax(const double* field, int64_t count, int64_t stride)
+{
+    double mx = ORA_MIN_DOUBLE;
+    for (int64_t i = 0; i < count; ++i) {
+        const double a = ora_mag(field[2 * i * stride], field[2 * i * stride + 1]);
+        if (a > mx) mx = a;
+    }
+    return mx;
+}
+
 int oracle_encode(const double* field, int64_t n, int32_t encode_flag, double* encoded)
 {
     if (n > 0 && (!field || !encoded)) return -1;
-    if (encode_flag == 0) {
-        double pi2 = M_PI * 2;             /* ophGen.cpp:1846 */
+    const double pi2 = M_PI * 2;           /* ophGen.cpp:1846 */
+    switch (encode_flag) {
+    case 0:                                /* Phase, ophGen.cpp:1843-1853 */
 #pragma omp parallel for
         for (int64_t i = 0; i < n; ++i)
             encoded[i] = (atan2(field[2 * i + 1], field[2 * i]) + M_PI) / pi2;
-    } else if (encode_flag == 1) {
+        break;
+    case 1:                                /* Amplitude, ophGen.cpp:1855-1864 */
 #pragma omp parallel for
+        for (int64_t i = 0; i < n; ++i) encoded[i] = ora_mag(field[2 * i], field[2 * i + 1]);
+        break;
+    case 2:                                /* RealPart, ophGen.cpp:1821-1830 */
+        for (int64_t i = 0; i < n; ++i) encoded[i] = field[2 * i];
+        break;
+    case 3:                                /* ImaginaryPart, ophGen.cpp:1832-1841 */
+        for (int64_t i = 0; i < n; ++i) encoded[i] = field[2 * i + 1];
+        break;
+    case 4: {                              /* SimpleNI, ophGen.cpp:1955-1974 */
+        const double mx = ora_absmax(field, n, 1);
         for (int64_t i = 0; i < n; ++i) {
-            double re = field[2 * i], im = field[2 * i + 1];
-            encoded[i] = sqrt(re * re + im * im);
+            const double t = ora_mag(field[2 * i] + mx, field[2 * i + 1]);
+            encoded[i] = t * t;
         }
-    } else {
+        break;
+    }
+    case 5: {                              /* Burckhardt, ophGen.cpp:1897-1953 */
+        const int64_t m = n / 3;
+        const double mx = ora_absmax(field, m, 3);
+        const double sqrt3 = sqrt(3), p2 = 2 * M_PI, p4 = 4 * M_PI;
+        for (int64_t i = 0; i < m; ++i) {
+            const double re = field[6 * i] / mx, im = field[6 * i + 1] / mx;
+            const double ph = (atan2(im, re) + M_PI) / pi2;
+            const double am = ora_mag(re, im);
+            if (ph >= 0 && ph < (p2 / 3)) {
+                encoded[3 * i] = am * (cos(ph) + sin(ph) / sqrt3);
+                encoded[3 * i + 1] = 2 * sin(ph) / sqrt3;
+            } else if (ph >= (p2 / 3) && ph < (p4 / 3)) {
+                encoded[3 * i + 1] = am * (cos(ph - (p2 / 3)) + sin(ph - (p2 / 3)) / sqrt3);
+                encoded[3 * i + 2] = 2 * sin(ph - (p2 / 3)) / sqrt3;
+            } else if (ph >= (p4 / 3) && ph < (p2)) {
+                encoded[3 * i + 2] = am * (cos(ph - (p4 / 3)) + sin(ph - (p4 / 3)) / sqrt3);
+                encoded[3 * i] = 2 * sin(ph - (p4 / 3)) / sqrt3;
+            }
+        }
+        break;
+    }
+    case 6: {                              /* TwoPhase, ophGen.cpp:1866-1895 */
+        const int64_t m = n >> 1;
+        const double mx = ora_absmax(field, m, 2);
+        for (int64_t i = 0; i < m; ++i) {
+            const double re = field[4 * i] / mx, im = field[4 * i + 1] / mx;
+            const double ph = (atan2(im, re) + M_PI) / pi2;
+            const double d = acos(ora_mag(re, im));
+            encoded[2 * i] = (ph + M_PI) + d;
+            encoded[2 * i + 1] = (ph + M_PI) - d;
+        }
+        break;
+    }
+    default:
         return -1;
     }
     return 0;

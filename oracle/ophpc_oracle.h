@@ -10,7 +10,8 @@
  *   ophGen::RS_Diffraction   ophgen/src/ophGen.cpp:361-445
  *   ophGen::Fresnel_Diffraction ophgen/src/ophGen.cpp:447-514
  *   ophGen::transVW          ophgen/src/ophGen.cpp:1976-1985
- *   ophGen::Phase/Amplitude  ophgen/src/ophGen.cpp:1843-1864
+ *   ophGen::Phase/Amplitude/RealPart/ImaginaryPart ophgen/src/ophGen.cpp:1821-1864
+ *   ophGen::TwoPhase/Burckhardt/SimpleNI ophgen/src/ophGen.cpp:1866-1974
  *   ophGen::normalize        ophgen/src/ophGen.cpp:654-687 (+ function.h:79-99)
  * Parity of this restatement is pinned against the reference itself
  * (oracle/_ref, built from the reference sources) by tests/test_oracle.py
@@ -55,7 +56,10 @@ int oracle_field_at(const oracle_config* cfg, const double* vertices, int64_t n_
                     int32_t diff_flag, int32_t channel, const int64_t* pixel_index,
                     int64_t n_pix, double* out);
 
-/* ENCODE_PHASE = 0, ENCODE_AMPLITUDE = 1. field: [n][re, im]. */
+/* One channel of n pixels, as ophGen::encoding calls its encoder per
+ * channel: ENCODE_PHASE 0, AMPLITUDE 1, REAL 2, IMAGINARY 3, SIMPLENI 4,
+ * BURCKHARDT 5, TWOPHASE 6. field: [n][re, im]. Burckhardt and TwoPhase
+ * leave the entries they do not write as they were (encoded is in/out). */
 int oracle_encode(const double* field, int64_t n, int32_t encode_flag, double* encoded);
 
 /* Global min/max over all channels, then (uchar)(((v-min)/gap)*255 + 0.5). */

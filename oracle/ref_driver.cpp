@@ -145,6 +145,40 @@ int ophref_run_save_ohc(const char* xml_path, const void* vertices, unsigned lon
     return h.pc->saveAsOhc(ohc_path) ? 0 : -3;
 }
 
+// Encodes a given field with the reference's ophGen::encoding +
+// ophGen::normalize (ophgen/src/ophGen.cpp:816-849,654-687). The config
+// (xml_path) sets the shape; field_in: [n_channels][pnY*pnX][re,im]. When
+// pre_flag >= 0 that encoding (and normalize) runs first on the same object,
+// so the encoders that write only some entries (Burckhardt, TwoPhase) leave
+// its values in the others. Outputs as in ophref_run. Returns 0 on success.
+int ophref_encode_field(const char* xml_path, const double* field_in, int pre_flag, unsigned flag,
+                        double* encoded_out, unsigned char* normalized_out)
+{
+    Holder h;
+    h.pc = new ophPointCloud();
+    if (!h.pc->readConfig(xml_path)) return -1;
+    OphConfig& ctx = h.pc->getContext();
+    const long long pnXY = (long long)ctx.pixel_number[_X] * ctx.pixel_number[_Y];
+    const unsigned nch = ctx.waveNum;
+    Complex<Real>** H = h.pc->getComplexField();
+    for (unsigned c = 0; c < nch; ++c)
+        for (long long i = 0; i < pnXY; ++i)
+            H[c][i] = Complex<Real>(field_in[(c * pnXY + i) * 2], field_in[(c * pnXY + i) * 2 + 1]);
+    if (pre_flag >= 0) {
+        h.pc->encoding((unsigned)pre_flag);
+        h.pc->normalize();
+    }
+    h.pc->encoding(flag);
+    h.pc->normalize();
+    Real** E = h.pc->getEncodedBuffer();
+    uchar** U = h.pc->getNormalizedBuffer();
+    for (unsigned c = 0; c < nch; ++c) {
+        if (encoded_out) std::memcpy(encoded_out + c * pnXY, E[c], sizeof(Real) * pnXY);
+        if (normalized_out) std::memcpy(normalized_out + c * pnXY, U[c], (size_t)pnXY);
+    }
+    return 0;
+}
+
 // Loads a .ohc with Openholo::loadAsOhc (Openholo/src/Openholo.cpp:280-319)
 // and copies out the shape (shape[0..2] = pnX, pnY, channels), pitch[2],
 // wavelengths[3] and, when field is non-NULL and cap_doubles suffices,

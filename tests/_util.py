@@ -37,14 +37,17 @@ def run_generate(ctx, geom_kwargs: dict, vertices: np.ndarray, diff_flag: int, m
     return f[..., 0] + 1j * f[..., 1]
 
 
-def run_encode(ctx, field: np.ndarray, encode_flag: int):
-    """Device encode + normalise of a complex128 [nch, ...] field."""
+def run_encode(ctx, field: np.ndarray, encode_flag: int, prior=None):
+    """Device encode + normalise of a complex128 [nch, ...] field; `prior`
+    (default zeros) is what the encoded buffer holds before the call."""
     import torch
     nch = field.shape[0]
     npx = field[0].size
     f = np.ascontiguousarray(field, dtype=np.complex128)
     df = torch.from_numpy(f.view(np.float64).reshape(nch, npx, 2)).cuda()
-    enc = torch.empty((nch, npx), dtype=torch.float64, device="cuda")
+    enc = torch.zeros((nch, npx), dtype=torch.float64, device="cuda")
+    if prior is not None:
+        enc.copy_(torch.from_numpy(np.ascontiguousarray(prior, dtype=np.float64).reshape(nch, npx)))
     nrm = torch.empty((nch, npx), dtype=torch.uint8, device="cuda")
     ctx.encode(df.data_ptr(), nch, npx, encode_flag, enc.data_ptr(), nrm.data_ptr(),
                torch.cuda.current_stream().cuda_stream)

@@ -159,6 +159,40 @@ def make_ohc(xml):
     return out
 
 
+ENCODER_FLAGS = (2, 3, 4, 5, 6)   # Real, Imaginary, SimpleNI, Burckhardt, TwoPhase
+
+
+def make_encoders(xml):
+    """The reference's encoding + normalize of given fields: the fresnel_3ch
+    golden field (3 channels, 80x48) and a seeded 41x23 one-channel field
+    whose pixel count divides by neither 2 nor 3; on the latter also
+    Burckhardt after Phase and TwoPhase after Amplitude on the same object
+    (the entries they skip keep the earlier encoding)."""
+    out = {}
+    z = np.load(os.path.join(HERE, "fresnel_3ch.npz"))
+    with open(xml, "w") as f:
+        f.write(str(z["xml"]))
+    res = {}
+    for flag in ENCODER_FLAGS:
+        res[f"enc_{flag}"], res[f"codes_{flag}"] = oracle.ref_encode_field(xml, z["field"], flag)
+    np.savez_compressed(os.path.join(HERE, "encoders_3ch.npz"), **res)
+    out["encoders_3ch"] = len(res)
+    rng = np.random.default_rng(5)
+    g = oracle.Geometry(pnx=41, pny=23, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    with open(xml, "w") as f:
+        f.write(g.xml())
+    fld = rng.normal(size=(1, 23, 41)) + 1j * rng.normal(size=(1, 23, 41))
+    res = {"field": fld, "xml": g.xml()}
+    for flag in ENCODER_FLAGS:
+        res[f"enc_{flag}"], res[f"codes_{flag}"] = oracle.ref_encode_field(xml, fld, flag)
+    for flag, pre in ((5, 0), (6, 1)):
+        res[f"enc_{flag}_after_{pre}"], res[f"codes_{flag}_after_{pre}"] = oracle.ref_encode_field(xml, fld, flag,
+                                                                                                   pre)
+    np.savez_compressed(os.path.join(HERE, "encoders_odd_1ch.npz"), **res)
+    out["encoders_odd_1ch"] = len(res)
+    return out
+
+
 def main():
     if not oracle.ref_available():
         oracle.build(with_reference=True)
@@ -236,15 +270,17 @@ def main():
             out[name] = os.path.getsize(bmp)
 
         out.update(make_ohc(xml))
+        out.update(make_encoders(xml))
     for k, v in out.items():
         print(k, v)
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["ohc"]:   # only the OHC fixtures
+    only = {"ohc": make_ohc, "encoders": make_encoders}
+    if len(sys.argv) == 2 and sys.argv[1] in only:   # one group of fixtures
         if not oracle.ref_available():
             oracle.build(with_reference=True)
         with tempfile.TemporaryDirectory() as d:
-            print(make_ohc(os.path.join(d, "cfg.xml")))
+            print(only[sys.argv[1]](os.path.join(d, "cfg.xml")))
     else:
         main()

@@ -106,3 +106,27 @@ def test_normalize_edge_cases(oracle_mod):
     codes, mn, mx = oracle_mod.normalize(-np.arange(1.0, 5.0).reshape(1, 4))
     assert mx == 2.2250738585072014e-308 and mn == -4.0
     assert codes.tolist() == [[191, 128, 64, 0]]
+
+
+ENCODER_FLAGS = (2, 3, 4, 5, 6)
+
+
+def test_oracle_encoders_match_reference(oracle_mod):
+    """Real, Imaginary, SimpleNI, Burckhardt and TwoPhase + normalize,
+    bit-exact against the reference's own output on the same fields."""
+    f3 = np.load(os.path.join(GOLD, "fresnel_3ch.npz"))["field"]
+    g3 = np.load(os.path.join(GOLD, "encoders_3ch.npz"))
+    g1 = np.load(os.path.join(GOLD, "encoders_odd_1ch.npz"))
+    for field, gold in ((f3, g3), (g1["field"], g1)):
+        for flag in ENCODER_FLAGS:
+            enc = oracle_mod.encode(field, flag)
+            assert np.array_equal(enc, gold[f"enc_{flag}"], equal_nan=True), flag
+            codes, _, _ = oracle_mod.normalize(enc)
+            assert np.array_equal(codes, gold[f"codes_{flag}"]), flag
+    # Burckhardt after Phase, TwoPhase after Amplitude: skipped entries keep
+    # the earlier encoding (943 pixels: neither 2 nor 3 divides the count)
+    for flag, pre in ((5, 0), (6, 1)):
+        enc = oracle_mod.encode(g1["field"], flag, prior=oracle_mod.encode(g1["field"], pre))
+        assert np.array_equal(enc, g1[f"enc_{flag}_after_{pre}"])
+        codes, _, _ = oracle_mod.normalize(enc)
+        assert np.array_equal(codes, g1[f"codes_{flag}_after_{pre}"])
