@@ -438,7 +438,9 @@ def gpu_arm(args, w):
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
             "relL2": rel,
             "roofline": {"bound": "sfu", "kernel": "rs_kernel", "achieved": achieved_rs, "peak": peak_rs,
-                         "unit": "interactions/s", "frac": achieved_rs / peak_rs, "traffic": None,
+                         "unit": "interactions/s", "frac": achieved_rs / peak_rs,
+                         "traffic": RS_TRAFFIC_BYTES.get(w.name), "traffic_unit": "bytes per launch (DRAM)",
+                         "algorithmic_bytes": w.n_points * nch * 64 + npx * nch * 16,
                          "peak_basis": f"{sms} SMs x 16 MUFU/clk / 2 MUFU (sin, cos) per interaction x "
                                        f"{sm_mhz:.0f} MHz median SM clock under load"},
             "fresnel": {"value": inter * world / t_fr, "unit": UNIT, "ms_per_generate": t_fr * 1e3,
@@ -459,6 +461,12 @@ def gpu_arm(args, w):
         dist.destroy_process_group()
     ctx.close()
     return line
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one rs_kernel launch of the
+# workload's RS generate, from a 1-pass ncu capture of
+# `bench.py --profile-case rs_fhd` (profiles/rs_kernel_sphere_fhd_dram.md).
+RS_TRAFFIC_BYTES = {"sphere_fhd": 27.46e6 + 151.67e6}
 
 
 def profile_case(name: str) -> None:

@@ -172,18 +172,21 @@ cudaError_t pool_alloc(ophpc_context* ctx, T** p, size_t bytes, cudaStream_t s) 
 }
 
 // Device-side generate shared by the device and host entry points.
+// accumulate: add into d_field instead of overwriting it (plain kernels only).
 ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                              uint64_t n_points, uint32_t diff_flag, uint32_t mode, double* d_field,
-                             cudaStream_t s) {
+                             cudaStream_t s, int color_offset = 0, bool accumulate = false) {
     JobGeom jg = make_geom(cfg, (int64_t)n_points);
+    jg.accumulate = accumulate ? 1 : 0;
     const int64_t plane = (int64_t)cfg->pixel_number[0] * cfg->pixel_number[1];
     const int64_t field_elems = plane * cfg->n_channels;
     const bool tensor = diff_flag == OPHPC_DIFF_FRESNEL && (mode & (OPHPC_MODE_TENSOR_FP16 | OPHPC_MODE_TENSOR_BF16X3));
     if (n_points == 0) {
+        if (accumulate) return OPHPC_SUCCESS;
         cudaError_t e = cudaMemsetAsync(d_field, 0, sizeof(double2) * field_elems, s);
         return e == cudaSuccess ? OPHPC_SUCCESS : cuda_fail(ctx, e, "cudaMemsetAsync(field)");
     }
-    if (tensor) {
+    if (tensor && !accumulate) {
         return tc_generate_fresnel(ctx->pool, cfg, d_vertices, n_points, mode, d_field, s, &ctx->last_error);
     }
     const int bps = diff_flag == OPHPC_DIFF_RS ? ctx->rs_bps : ctx->fr_bps;
@@ -199,7 +202,7 @@ ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const 
         return cuda_fail(ctx, e, "scratch allocation (partials)");
     }
     launch_prep(d_vertices, (int64_t)n_points, cfg->scale, cfg->distance, cfg->field_length,
-                cfg->viewing_window, (int)diff_flag, jg, d_recs, s);
+                cfg->viewing_window, (int)diff_flag, jg, d_recs, s, color_offset);
     if (diff_flag == OPHPC_DIFF_RS)
         launch_rs(d_recs, jg, (double2*)d_field, d_partials, s);
     else
@@ -226,6 +229,29 @@ ophpc_status check_job(ophpc_context* ctx, const ophpc_config* cfg, uint64_t n_p
 }
 
 }  // namespace
+
+namespace ophpc {
+
+// For the reference-signature launchers (pc_refabi.cu): one channel, the
+// amplitude from color[color_offset], added into d_field; plain kernels.
+ophpc_status generate_accumulate(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
+                                 uint64_t n_points, uint32_t diff_flag, int color_offset, double* d_field,
+                                 cudaStream_t s) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    ophpc_status st = check_job(ctx, cfg, n_points, diff_flag, 0);
+    if (st != OPHPC_SUCCESS) return st;
+    if (color_offset < 0 || color_offset + (int)cfg->n_channels > OPHPC_MAX_CHANNELS)
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "colour index must be 0..2");
+    DeviceGuard guard(ctx->device);
+    if (!d_field || !is_device_ptr(d_field)) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_dst must be device memory");
+    if (n_points > 0 && (!d_vertices || !is_device_ptr(d_vertices)))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "vertices must be device memory");
+    return generate_device(ctx, cfg, d_vertices, n_points, diff_flag, 0, d_field, s, color_offset, true);
+}
+
+}  // namespace ophpc
 
 extern "C" {
 

@@ -124,9 +124,10 @@ void count_launches(unsigned n);
 uint64_t launches_so_far();
 
 // Launchers (defined in the .cu files).
+// color_offset: channel c takes its amplitude from color[c + color_offset].
 void launch_prep(const void* d_vertices, int64_t n_points, const double* scale, double distance,
                  double field_length, int viewing_window, int diff_flag, const JobGeom& jg,
-                 PointRec* d_recs, cudaStream_t stream);
+                 PointRec* d_recs, cudaStream_t stream, int color_offset = 0);
 void launch_rs(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,
                cudaStream_t stream);
 void launch_fresnel(const PointRec* d_recs, const JobGeom& jg, double2* d_field, double2* d_partials,

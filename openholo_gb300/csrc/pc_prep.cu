@@ -21,6 +21,7 @@ struct PrepArgs {
     double field_length;
     int viewing_window;
     int diff_flag;
+    int color_offset;
 };
 
 __device__ __forceinline__ double trans_vw(double p, double f) {
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(256) prep_points_kernel(const double* __restri
     y = __dmul_rn(y, a.scale[1]);
     zs = __dmul_rn(zs, a.scale[2]);
     const double z = __dadd_rn(zs, a.distance);
-    const double amp = v[3 + ch];
+    const double amp = v[3 + ch + a.color_offset];
     PointRec r;
     r.x = x;
     r.y = y;
@@ -102,9 +103,10 @@ __global__ void __launch_bounds__(256) prep_points_kernel(const double* __restri
 
 void launch_prep(const void* d_vertices, int64_t n_points, const double* scale, double distance,
                  double field_length, int viewing_window, int diff_flag, const JobGeom& jg,
-                 PointRec* d_recs, cudaStream_t stream) {
+                 PointRec* d_recs, cudaStream_t stream, int color_offset) {
     if (n_points <= 0) return;
     PrepArgs a;
+    a.color_offset = color_offset;
     for (int i = 0; i < 3; ++i) a.scale[i] = scale[i];
     a.distance = distance;
     a.field_length = field_length;

@@ -112,3 +112,36 @@ def test_facade_config_and_model_state(tmp_path):
         assert h.getComplexField().shape == (2, 24, 40)
         assert h.generateHologram(7) == 0.0    # bad flag -> 0.0, as the reference
         assert not h.readConfig(str(tmp_path / "missing.xml"))
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_public_headers_compile(tmp_path, lang):
+    """Every include/*.h compiles on its own as C11 and as C++17."""
+    import shutil
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    std = "-std=c11" if lang == "c" else "-std=c++17"
+    for h in sorted(glob.glob(os.path.join(ROOT, "include", "*.h"))):
+        if lang == "c" and "class ophPointCloud" in open(h).read():
+            continue
+        src = tmp_path / ("t.c" if lang == "c" else "t.cpp")
+        src.write_text(f'#include "{os.path.basename(h)}"\nint main(void) {{ return 0; }}\n')
+        r = subprocess.run([cc, std, "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                            os.path.join(ROOT, "include"), str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, (h, r.stderr)
+
+
+def test_reference_launcher_reports_status_without_crashing():
+    """cudaPointCloud_RS with the reference's signature: no config -> a
+    status on the calling thread (no device here: NO_DEVICE; with one:
+    INVALID_ARGUMENT), nothing launched."""
+    L = oph.lib()
+    ip, up = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint)
+    L.cudaPointCloud_RS.argtypes = [ip, ip, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, up, up]
+    L.cudaPointCloud_RS.restype = None
+    L.ophpc_refabi_last_status.restype = ctypes.c_int
+    one, zero = ctypes.c_int(1), ctypes.c_uint(0)
+    L.cudaPointCloud_RS(ctypes.byref(one), ctypes.byref(one), None, None, None, ctypes.byref(zero),
+                        ctypes.byref(zero))
+    assert L.ophpc_refabi_last_status() in (1, 10)
