@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-points", type=int, default=0, help="points in the CPU sample (0 = auto)")
-    ap.add_argument("--serving-jobs", type=int, default=64, help="jobs in the serving stream (512 = full)")
+    ap.add_argument("--serving-jobs", type=int, default=128, help="jobs in the serving stream (512 = full)")
     ap.add_argument("--profile-case", default=None,
                     help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
                          "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points)")
@@ -208,13 +208,15 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
     Every job is first run alone (isolated latency = its service time); the
     mean isolated service time sets the arrival rate of each offered load.
     Latency = completion - arrival (server clock). Jobs return their 8-bit
-    phase holograms (the field stays on the device)."""
+    phase holograms (the field stays on the device). The default policy
+    (short jobs first, then earliest deadline) runs every load;
+    shortest-remaining-work runs the 80% load beside it."""
     import threading
 
     import torch
 
     from openholo_gb300 import make_config, workloads
-    from openholo_gb300.serving import Server
+    from openholo_gb300.serving import POLICY_DEADLINE, POLICY_SHORTEST_REMAINING, Server
 
     jobs = workloads.serving_stream(n_jobs, rate_per_s=1.0, seed=seed, max_points=max_points)
     prepared = []
@@ -224,7 +226,36 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
         hc = torch.empty((w.n_channels, w.pny, w.pnx), dtype=torch.uint8).pin_memory()
         prepared.append((make_config(**w.geometry_kwargs()), hv, hc, w.n_points, jb.diff_flag, w.interactions))
     out = {"jobs": n_jobs, "max_points": max_points, "loads": {}}
-    with Server(0, max_in_flight=16, step_ms=2.0) as srv:
+    rng = np.random.default_rng(seed + 1)
+    gaps = rng.exponential(1.0, n_jobs)
+    iso = None
+
+    def run_load(srv, load, mean_s):
+        arrivals = np.cumsum(gaps) * mean_s / load
+        tickets = [None] * n_jobs
+
+        def feeder():
+            t0 = time.perf_counter()
+            for i, (cfg, hv, hc, n, d, _) in enumerate(prepared):
+                dt = arrivals[i] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                tickets[i] = srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0)
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        res = [srv.wait_stats(t) for t in tickets]
+        lat = np.array([r.t_done - r.t_submit for r in res])
+        span = max(r.t_done for r in res) - min(r.t_submit for r in res)
+        slow = lat / iso
+        return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "p99_over_isolated_p99": float(np.percentile(lat, 99) / np.percentile(iso, 99)),
+                "slowdown_p50": float(np.percentile(slow, 50)), "slowdown_p99": float(np.percentile(slow, 99)),
+                "throughput_interactions_per_s": float(sum(p[5] for p in prepared) / span),
+                "jobs_per_s": n_jobs / span}
+
+    with Server(0, max_in_flight=16, step_ms=2.0, policy=POLICY_DEADLINE) as srv:
         iso = []
         for cfg, hv, hc, n, d, _ in prepared:
             r = srv.wait_stats(srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0))
@@ -233,33 +264,12 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
         mean_s = float(iso.mean())
         out["isolated_ms"] = {"p50": float(np.percentile(iso, 50) * 1e3), "p99": float(np.percentile(iso, 99) * 1e3),
                               "mean": mean_s * 1e3}
-        rng = np.random.default_rng(seed + 1)
-        gaps = rng.exponential(1.0, n_jobs)
+        out["policy"] = ("short jobs (< 20 ms estimated) first, the rest by earliest deadline "
+                         "(submission + 2 x estimated isolated time)")
         for load in loads:
-            arrivals = np.cumsum(gaps) * mean_s / load
-            tickets = [None] * n_jobs
-
-            def feeder():
-                t0 = time.perf_counter()
-                for i, (cfg, hv, hc, n, d, _) in enumerate(prepared):
-                    dt = arrivals[i] - (time.perf_counter() - t0)
-                    if dt > 0:
-                        time.sleep(dt)
-                    tickets[i] = srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0)
-
-            th = threading.Thread(target=feeder)
-            th.start()
-            th.join()
-            res = [srv.wait_stats(t) for t in tickets]
-            lat = np.array([r.t_done - r.t_submit for r in res])
-            span = max(r.t_done for r in res) - min(r.t_submit for r in res)
-            slow = lat / iso
-            out["loads"][f"{load:.2f}"] = {
-                "p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "p99_over_isolated_p99": float(np.percentile(lat, 99) / np.percentile(iso, 99)),
-                "slowdown_p50": float(np.percentile(slow, 50)), "slowdown_p99": float(np.percentile(slow, 99)),
-                "throughput_interactions_per_s": float(sum(p[5] for p in prepared) / span),
-                "jobs_per_s": n_jobs / span}
+            out["loads"][f"{load:.2f}"] = run_load(srv, load, mean_s)
+    with Server(0, max_in_flight=16, step_ms=2.0, policy=POLICY_SHORTEST_REMAINING) as srv:
+        out["shortest_remaining_0.80"] = run_load(srv, 0.8, mean_s)
     return out
 
 

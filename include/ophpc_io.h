@@ -44,7 +44,11 @@ ophpc_status ophpc_read_config(const char* xml_path, ophpc_config* cfg, ophpc_im
 
 /* Loads a PLY point cloud (ASCII, binary_little_endian or
  * binary_big_endian) into 56-byte vertex records. With out == NULL only the
- * count is returned. Returns the vertex count, or -1 on error. Colours are
+ * header is read and its vertex count returned (the data are checked by the
+ * loading call). With capacity >= the count the records are decoded
+ * straight into out (which may be page-locked memory); otherwise the first
+ * `capacity` records are copied. Returns the vertex count, or -1 on error
+ * (unreadable file, malformed header, truncated data). Colours are
  * (double)(c / 255.f) from red/green/blue (or diffuse_*); a file without a
  * `color` element with a `channel` property gets 0.5 in every channel, as
  * the reference does. */

@@ -5,14 +5,25 @@
  * job to completion, ophgen/src/ophPointCloud.cpp:151-191). A server owns a
  * worker thread, a device memory budget and `max_in_flight` slots. Jobs of
  * any resolution, point count, wavelength set and method are submitted at
- * any time; the worker admits them in arrival order as soon as a slot is
- * free and their device memory fits both the budget and the free HBM
- * reported by cudaMemGetInfo, then runs every admitted job as a sequence of
- * steps of ~step_ms of GPU time on its own stream, so that admitted jobs
- * overlap on the device. Each step goes to a stream whose priority follows
- * the job's remaining work (least remaining first). A job's result does not
- * depend on the other jobs: its chunking is fixed by the job and its FP64
- * field is accumulated in the same order whatever else runs.
+ * any time; the worker admits them as soon as a slot is free and their
+ * device memory fits both the budget and the free HBM reported by
+ * cudaMemGetInfo, then runs every admitted job as a sequence of steps of
+ * ~step_ms of GPU time on its own stream, so that admitted jobs overlap on
+ * the device. The policy orders admission and the streams' priorities:
+ *   OPHPC_SERVE_DEADLINE (default): jobs whose estimated isolated service
+ *     time (interactions at the kernels' rate + copies + a fixed per-job
+ *     cost) is under 20 ms first, least remaining work first among them;
+ *     then the others by earliest deadline, a job's deadline being its
+ *     submission time + 2 x its estimated isolated time. Short jobs overtake
+ *     long ones, but a long job's priority rises as its deadline nears
+ *     instead of starving behind other long ones;
+ *   OPHPC_SERVE_SHORTEST_REMAINING: admission in arrival order, priority by
+ *     remaining work (best median latency, worst tail).
+ * Admission never skips the first job in policy order that does not fit, so
+ * a large job cannot be starved of memory by smaller ones behind it.
+ * A job's result does not depend on the other jobs: its chunking is fixed
+ * by the job and its FP64 field is accumulated in the same order whatever
+ * else runs.
  *
  * Host buffers (vertices in, field / codes out) must stay valid until the
  * job is waited for; page-locked buffers let the copies overlap with other
@@ -29,9 +40,12 @@ extern "C" {
 
 typedef struct ophpc_server ophpc_server;
 
+#define OPHPC_SERVE_DEADLINE 0u
+#define OPHPC_SERVE_SHORTEST_REMAINING 1u
+
 typedef struct ophpc_server_options {
     uint32_t max_in_flight;    /* admitted jobs at once (0 = 16) */
-    uint32_t pad;
+    uint32_t policy;           /* OPHPC_SERVE_DEADLINE (0) or OPHPC_SERVE_SHORTEST_REMAINING */
     uint64_t memory_budget;    /* bytes of device memory for jobs (0 = half the free memory) */
     uint64_t reserve_bytes;    /* free device memory always left untouched (0 = 512 MiB) */
     double step_ms;            /* target GPU time of one scheduling step (<= 0: 2 ms) */

@@ -151,9 +151,15 @@ int ophPointCloud::loadPointCloud(const char* pc_file) {
         last_error_ = "cannot load point cloud";
         return -1;
     }
+    Vertex* v = new Vertex[n > 0 ? n : 1];
+    if (ophpc_load_ply(pc_file, reinterpret_cast<ophpc_vertex*>(v), (uint64_t)n) != n) {
+        delete[] v;
+        OPH_LOG("<FAILED> Loading ply file.\n");
+        last_error_ = "cannot load point cloud";
+        return -1;
+    }
     delete[] vertices_;
-    vertices_ = new Vertex[n > 0 ? n : 1];
-    ophpc_load_ply(pc_file, reinterpret_cast<ophpc_vertex*>(vertices_), (uint64_t)n);
+    vertices_ = v;
     n_points_ = (ulonglong)n;
     return (int)n;
 }

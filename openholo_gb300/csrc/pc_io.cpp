@@ -27,6 +27,7 @@
 #include <map>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace {
@@ -193,43 +194,42 @@ bool host_little_endian() {
     return b == 1;
 }
 
-// Reads one binary scalar of type t as double (byte-swapped if needed).
-bool read_scalar(std::istream& is, PT t, bool swap, double* out) {
-    unsigned char buf[8];
-    const int n = psize(t);
-    if (n == 0 || !is.read((char*)buf, n)) return false;
-    if (swap) std::reverse(buf, buf + n);
-    switch (t) {
-        case PT::I8: { int8_t v; std::memcpy(&v, buf, 1); *out = v; break; }
-        case PT::U8: { uint8_t v; std::memcpy(&v, buf, 1); *out = v; break; }
-        case PT::I16: { int16_t v; std::memcpy(&v, buf, 2); *out = v; break; }
-        case PT::U16: { uint16_t v; std::memcpy(&v, buf, 2); *out = v; break; }
-        case PT::I32: { int32_t v; std::memcpy(&v, buf, 4); *out = v; break; }
-        case PT::U32: { uint32_t v; std::memcpy(&v, buf, 4); *out = v; break; }
-        case PT::F32: { float v; std::memcpy(&v, buf, 4); *out = v; break; }
-        case PT::F64: { double v; std::memcpy(&v, buf, 8); *out = v; break; }
-        default: return false;
-    }
-    return true;
-}
-
 inline double colour(int c) { return (double)((float)c / 255.f); }
 
-int64_t load_ply(const char* path_in, std::vector<ophpc_vertex>& out) {
-    if (!path_in) return -1;
-    std::string path = path_in;
-    if (path.find(".ply") == std::string::npos && path.find(".PLY") == std::string::npos) path += ".ply";
-    std::ifstream f(path, std::ios::in | std::ios::binary);
-    if (!f.is_open()) return -1;
+// Decodes one binary scalar of type t at p (byte-swapped if needed).
+inline double decode_scalar(const unsigned char* p, PT t, bool swap) {
+    unsigned char b[8];
+    const int n = psize(t);
+    std::memcpy(b, p, (size_t)n);
+    if (swap) std::reverse(b, b + n);
+    switch (t) {
+        case PT::I8: { int8_t v; std::memcpy(&v, b, 1); return v; }
+        case PT::U8: return b[0];
+        case PT::I16: { int16_t v; std::memcpy(&v, b, 2); return v; }
+        case PT::U16: { uint16_t v; std::memcpy(&v, b, 2); return v; }
+        case PT::I32: { int32_t v; std::memcpy(&v, b, 4); return v; }
+        case PT::U32: { uint32_t v; std::memcpy(&v, b, 4); return v; }
+        case PT::F32: { float v; std::memcpy(&v, b, 4); return v; }
+        case PT::F64: { double v; std::memcpy(&v, b, 8); return v; }
+        default: return 0.0;
+    }
+}
+
+struct PlyHeader {
+    bool binary = false, big = false;
+    std::vector<Elem> elems;
+    int iv = -1, ic = -1, ifc = -1;
+};
+
+// Header up to and including `end_header`; f is left at the first data byte.
+bool parse_ply_header(std::ifstream& f, PlyHeader& h) {
     std::string line, tok;
-    if (!std::getline(f, line)) return -1;
+    if (!std::getline(f, line)) return false;
     {
         std::istringstream ls(line);
         ls >> tok;
-        if (tok != "ply" && tok != "PLY") return -1;
+        if (tok != "ply" && tok != "PLY") return false;
     }
-    bool binary = false, big = false;
-    std::vector<Elem> elems;
     bool header_done = false;
     while (std::getline(f, line)) {
         std::istringstream ls(line);
@@ -238,14 +238,14 @@ int64_t load_ply(const char* path_in, std::vector<ophpc_vertex>& out) {
         if (tok == "format") {
             std::string fmt;
             ls >> fmt;
-            if (fmt == "binary_little_endian") binary = true;
-            else if (fmt == "binary_big_endian") binary = big = true;
+            if (fmt == "binary_little_endian") h.binary = true;
+            else if (fmt == "binary_big_endian") h.binary = h.big = true;
         } else if (tok == "element") {
             Elem e;
             ls >> e.name >> e.size;
-            elems.push_back(e);
+            h.elems.push_back(e);
         } else if (tok == "property") {
-            if (elems.empty()) return -1;
+            if (h.elems.empty()) return false;
             Prop p;
             std::string t;
             ls >> t;
@@ -257,25 +257,46 @@ int64_t load_ply(const char* path_in, std::vector<ophpc_vertex>& out) {
             }
             p.type = ptype(t);
             ls >> p.name;
-            elems.back().props.push_back(p);
+            h.elems.back().props.push_back(p);
         } else if (tok == "end_header") {
             header_done = true;
             break;
         }
     }
-    if (!header_done) return -1;
-    int iv = -1, ic = -1, ifc = -1;
-    for (size_t k = 0; k < elems.size(); ++k) {
-        if (iv < 0 && elems[k].name == "vertex") iv = (int)k;
-        if (ic < 0 && elems[k].name == "color") ic = (int)k;
-        if (ifc < 0 && elems[k].name == "face") ifc = (int)k;
+    if (!header_done) return false;
+    for (size_t k = 0; k < h.elems.size(); ++k) {
+        if (h.iv < 0 && h.elems[k].name == "vertex") h.iv = (int)k;
+        if (h.ic < 0 && h.elems[k].name == "color") h.ic = (int)k;
+        if (h.ifc < 0 && h.elems[k].name == "face") h.ifc = (int)k;
     }
-    if (iv < 0) return -1;
-    const Elem& V = elems[iv];
+    if (h.iv < 0) return false;
+    const Elem& V = h.elems[h.iv];
+    if (V.find("x") < 0 || V.find("y") < 0 || V.find("z") < 0) return false;
+    if (V.size > (uint64_t)INT32_MAX) return false;
+    return true;
+}
+
+// Whole-file PLY reader. The header is parsed line by line; the data are
+// read in one block and decoded in place: an element without list
+// properties has a fixed record size, so its records are decoded at
+// precomputed offsets; elements with lists (faces) are walked record by
+// record. ASCII records are one line each, tokens split on whitespace.
+// out must hold the header's vertex count.
+int64_t load_ply(const char* path_in, ophpc_vertex* out, bool count_only) {
+    if (!path_in) return -1;
+    std::string path = path_in;
+    if (path.find(".ply") == std::string::npos && path.find(".PLY") == std::string::npos) path += ".ply";
+    std::ifstream f(path, std::ios::in | std::ios::binary);
+    if (!f.is_open()) return -1;
+    PlyHeader h;
+    if (!parse_ply_header(f, h)) return -1;
+    const Elem& V = h.elems[h.iv];
+    const uint64_t n = V.size;
+    if (count_only) return (int64_t)n;
+
     const int px = V.find("x"), py = V.find("y"), pz = V.find("z");
-    if (px < 0 || py < 0 || pz < 0) return -1;
-    const bool found_channel = ic >= 0 && elems[ic].find("channel") >= 0;
-    const bool found_face = ifc >= 0 && elems[ifc].find("vertex_indices") >= 0;
+    const bool found_channel = h.ic >= 0 && h.elems[h.ic].find("channel") >= 0;
+    const bool found_face = h.ifc >= 0 && h.elems[h.ifc].find("vertex_indices") >= 0;
     int pr = V.find("red"), pg = V.find("green"), pb = V.find("blue");
     if (pb < 0) {
         pr = V.find("diffuse_red");
@@ -284,75 +305,156 @@ int64_t load_ply(const char* path_in, std::vector<ophpc_vertex>& out) {
     }
     const int pphase = V.find("phase");
     int fr = -1, fg = -1, fb = -1;
-    if (ifc >= 0) {
-        fr = elems[ifc].find("red");
-        fg = elems[ifc].find("green");
-        fb = elems[ifc].find("blue");
+    if (h.ifc >= 0) {
+        fr = h.elems[h.ifc].find("red");
+        fg = h.elems[h.ifc].find("green");
+        fb = h.elems[h.ifc].find("blue");
     }
-    const uint64_t n = V.size;
-    if (n > (uint64_t)INT32_MAX) return -1;
-    out.assign(n, ophpc_vertex{});
-    const bool swap = binary && (big == host_little_endian());
+    std::memset(out, 0, sizeof(ophpc_vertex) * (size_t)n);
 
-    for (size_t k = 0; k < elems.size(); ++k) {
-        const Elem& E = elems[k];
-        for (uint64_t e = 0; e < E.size; ++e) {
-            std::vector<double> vals(E.props.size(), 0.0);
-            if (binary) {
-                for (size_t j = 0; j < E.props.size(); ++j) {
+    // the data block
+    const std::streampos data_at = f.tellg();
+    f.seekg(0, std::ios::end);
+    const std::streampos file_end = f.tellg();
+    f.seekg(data_at);
+    const size_t nbytes = (size_t)(file_end - data_at);
+    std::string data(nbytes + 1, '\0');
+    if (nbytes && !f.read(&data[0], (std::streamsize)nbytes)) return -1;
+    const unsigned char* q = (const unsigned char*)data.data();
+    const unsigned char* const qend = q + nbytes;
+    const bool swap = h.binary && (h.big == host_little_endian());
+
+    auto put_vertex = [&](uint64_t e, const double* vals, bool binary) {
+        ophpc_vertex& vx = out[e];
+        if (binary) {   // binary coordinates land in a float in the reference
+            vx.pos[0] = V.props[px].type == PT::F64 ? vals[px] : (double)(float)vals[px];
+            vx.pos[1] = V.props[py].type == PT::F64 ? vals[py] : (double)(float)vals[py];
+            vx.pos[2] = V.props[pz].type == PT::F64 ? vals[pz] : (double)(float)vals[pz];
+        } else {
+            vx.pos[0] = vals[px];
+            vx.pos[1] = vals[py];
+            vx.pos[2] = vals[pz];
+        }
+        if (!found_face) {
+            vx.color[0] = colour(pr >= 0 ? (int)vals[pr] : 0);
+            vx.color[1] = colour(pg >= 0 ? (int)vals[pg] : 0);
+            vx.color[2] = colour(pb >= 0 ? (int)vals[pb] : 0);
+        }
+        if (pphase >= 0) vx.phase = (double)(float)vals[pphase];
+    };
+    auto put_face = [&](uint64_t e, const double* vals) {
+        if (e >= n || fb < 0) return;
+        ophpc_vertex& vx = out[e];
+        vx.color[0] = colour(fr >= 0 ? (int)vals[fr] : 0);
+        vx.color[1] = colour(fg >= 0 ? (int)vals[fg] : 0);
+        vx.color[2] = colour((int)vals[fb]);
+    };
+
+    std::vector<double> vals;
+    for (size_t k = 0; k < h.elems.size(); ++k) {
+        const Elem& E = h.elems[k];
+        const size_t np = E.props.size();
+        vals.assign(np, 0.0);
+        if (h.binary) {
+            bool fixed = true;
+            size_t stride = 0;
+            std::vector<size_t> off(np);
+            for (size_t j = 0; j < np; ++j) {
+                if (E.props[j].is_list || psize(E.props[j].type) == 0) fixed = false;
+                off[j] = stride;
+                stride += (size_t)psize(E.props[j].type);
+            }
+            if (fixed) {
+                if (E.size > (uint64_t)(qend - q) / (stride ? stride : 1)) return -1;
+                if ((int)k == h.iv) {
+                    // only the properties a vertex record uses, decoded in
+                    // parallel over record ranges
+                    const int want[7] = {px, py, pz, pr, pg, pb, pphase};
+                    const unsigned char* base = q;
+                    auto decode_range = [&](uint64_t e0, uint64_t e1) {
+                        double vv[64];
+                        std::vector<double> big(np > 64 ? np : 0);
+                        double* vr = np > 64 ? big.data() : vv;
+                        for (size_t j = 0; j < np; ++j) vr[j] = 0.0;
+                        for (uint64_t e = e0; e < e1; ++e) {
+                            const unsigned char* r = base + e * stride;
+                            for (int w : want)
+                                if (w >= 0) vr[w] = decode_scalar(r + off[w], E.props[w].type, swap);
+                            put_vertex(e, vr, true);
+                        }
+                    };
+                    const uint64_t per = 1u << 16;
+                    const unsigned nt = (unsigned)std::min<uint64_t>(
+                        std::max(1u, std::min(16u, std::thread::hardware_concurrency())), (E.size + per - 1) / per);
+                    if (nt <= 1) {
+                        decode_range(0, E.size);
+                    } else {
+                        std::vector<std::thread> th;
+                        const uint64_t chunk = (E.size + nt - 1) / nt;
+                        for (unsigned t = 0; t < nt; ++t) {
+                            const uint64_t e0 = t * chunk, e1 = std::min<uint64_t>(E.size, e0 + chunk);
+                            if (e0 < e1) th.emplace_back(decode_range, e0, e1);
+                        }
+                        for (auto& t : th) t.join();
+                    }
+                } else if ((int)k == h.ifc) {
+                    for (uint64_t e = 0; e < E.size; ++e) {
+                        const unsigned char* r = q + e * stride;
+                        for (size_t j = 0; j < np; ++j) vals[j] = decode_scalar(r + off[j], E.props[j].type, swap);
+                        put_face(e, vals.data());
+                    }
+                }
+                q += stride * E.size;
+                continue;
+            }
+            for (uint64_t e = 0; e < E.size; ++e) {
+                std::fill(vals.begin(), vals.end(), 0.0);
+                for (size_t j = 0; j < np; ++j) {
                     const Prop& p = E.props[j];
                     if (p.is_list) {
-                        double cnt;
-                        if (!read_scalar(f, p.list_type, swap, &cnt)) return -1;
-                        for (long c = 0; c < (long)cnt; ++c) {
-                            double dummy;
-                            if (!read_scalar(f, p.type, swap, &dummy)) return -1;
-                        }
+                        const int cs = psize(p.list_type), es = psize(p.type);
+                        if (cs == 0 || es == 0 || qend - q < cs) return -1;
+                        const double cnt = decode_scalar(q, p.list_type, swap);
+                        q += cs;
+                        if (!(cnt >= 0) || cnt * es > (double)(qend - q)) return -1;
+                        q += (size_t)cnt * (size_t)es;
                         continue;
                     }
-                    if (!read_scalar(f, p.type, swap, &vals[j])) return -1;
+                    const int sz = psize(p.type);
+                    if (sz == 0 || qend - q < sz) return -1;
+                    vals[j] = decode_scalar(q, p.type, swap);
+                    q += sz;
                 }
-            } else {
-                if (!std::getline(f, line)) return -1;
-                std::istringstream ls(line);
-                for (size_t j = 0; j < E.props.size(); ++j) {
-                    std::string v;
-                    if (!(ls >> v)) break;
+                if ((int)k == h.iv) put_vertex(e, vals.data(), true);
+                else if ((int)k == h.ifc) put_face(e, vals.data());
+            }
+        } else {
+            for (uint64_t e = 0; e < E.size; ++e) {
+                if (q >= qend) return -1;   // a missing line
+                const unsigned char* eol = (const unsigned char*)std::memchr(q, '\n', (size_t)(qend - q));
+                if (!eol) eol = qend;
+                std::fill(vals.begin(), vals.end(), 0.0);
+                const char* c = (const char*)q;
+                const char* le = (const char*)eol;
+                for (size_t j = 0; j < np; ++j) {
+                    while (c < le && std::isspace((unsigned char)*c)) ++c;
+                    if (c >= le) break;
+                    const char* t0 = c;
+                    while (c < le && !std::isspace((unsigned char)*c)) ++c;
+                    const std::string tok(t0, c);
                     const Prop& p = E.props[j];
-                    if (p.type == PT::F32 || p.type == PT::F64) vals[j] = std::strtod(v.c_str(), nullptr);
-                    else vals[j] = (double)std::strtol(v.c_str(), nullptr, 10);
+                    if (p.type == PT::F32 || p.type == PT::F64) vals[j] = std::strtod(tok.c_str(), nullptr);
+                    else vals[j] = (double)std::strtol(tok.c_str(), nullptr, 10);
                     if (p.is_list) break;   // lists in ASCII carry no vertex data we read
                 }
-            }
-            if ((int)k == iv) {
-                ophpc_vertex& vx = out[e];
-                if (binary) {
-                    // binary coordinates land in a float in the reference
-                    vx.pos[0] = V.props[px].type == PT::F64 ? vals[px] : (double)(float)vals[px];
-                    vx.pos[1] = V.props[py].type == PT::F64 ? vals[py] : (double)(float)vals[py];
-                    vx.pos[2] = V.props[pz].type == PT::F64 ? vals[pz] : (double)(float)vals[pz];
-                } else {
-                    vx.pos[0] = vals[px];
-                    vx.pos[1] = vals[py];
-                    vx.pos[2] = vals[pz];
-                }
-                if (!found_face) {
-                    vx.color[0] = colour(pr >= 0 ? (int)vals[pr] : 0);
-                    vx.color[1] = colour(pg >= 0 ? (int)vals[pg] : 0);
-                    vx.color[2] = colour(pb >= 0 ? (int)vals[pb] : 0);
-                }
-                if (pphase >= 0) vx.phase = (double)(float)vals[pphase];
-            } else if ((int)k == ifc && e < n && fb >= 0) {
-                ophpc_vertex& vx = out[e];
-                vx.color[0] = colour(fr >= 0 ? (int)vals[fr] : 0);
-                vx.color[1] = colour(fg >= 0 ? (int)vals[fg] : 0);
-                vx.color[2] = colour((int)vals[fb]);
+                if ((int)k == h.iv) put_vertex(e, vals.data(), false);
+                else if ((int)k == h.ifc) put_face(e, vals.data());
+                q = eol < qend ? eol + 1 : qend;
             }
         }
     }
-    if (!found_channel) {
-        for (auto& vx : out) vx.color[0] = vx.color[1] = vx.color[2] = 0.5;
-    }
+    if (!found_channel)
+        for (uint64_t e = 0; e < n; ++e) out[e].color[0] = out[e].color[1] = out[e].color[2] = 0.5;
     return (int64_t)n;
 }
 
@@ -580,10 +682,13 @@ ophpc_status ophpc_read_config(const char* xml_path, ophpc_config* cfg, ophpc_im
 }
 
 int64_t ophpc_load_ply(const char* path, ophpc_vertex* out, uint64_t capacity) {
-    std::vector<ophpc_vertex> v;
-    const int64_t n = load_ply(path, v);
+    if (!out) return load_ply(path, nullptr, true);
+    const int64_t n = load_ply(path, nullptr, true);
     if (n < 0) return -1;
-    if (out) std::memcpy(out, v.data(), sizeof(ophpc_vertex) * (size_t)std::min<uint64_t>(capacity, (uint64_t)n));
+    if (capacity >= (uint64_t)n) return load_ply(path, out, false);   // straight into the caller's buffer
+    std::vector<ophpc_vertex> v((size_t)n);
+    if (load_ply(path, v.data(), false) < 0) return -1;
+    std::memcpy(out, v.data(), sizeof(ophpc_vertex) * (size_t)capacity);
     return n;
 }
 

@@ -9,8 +9,11 @@
 // stream. Jobs therefore overlap on the device; a job that arrives while
 // others run is admitted as soon as a slot and memory free up and its
 // kernels interleave with theirs at CTA granularity. Steps are issued on
-// streams whose priority follows the job's remaining work (shortest
-// remaining first), so short jobs are not stuck behind long ones.
+// streams whose priority follows the policy's order: by default short jobs
+// first (least remaining work first among them), then the others by
+// earliest deadline (submission + 2 x estimated isolated time); or purely
+// shortest remaining work. Short jobs are not stuck behind long ones and
+// long ones are not starved by a stream of short ones.
 //
 // A job's result does not depend on what else runs: its chunking is fixed
 // by the job alone and every chunk adds into the FP64 field in order.
@@ -38,6 +41,10 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kPrioLevels = 6;   // CUDA exposes six stream priorities on this GPU family
+constexpr double kDeadlineFactor = 2.0;
+constexpr double kShortJobS = 20e-3;     // estimated isolated time below which a job goes first
+constexpr double kJobFixedS = 3e-3;      // per-job launch, sync and bookkeeping time
+constexpr double kCopyBytesPerS = 20e9;  // host <-> device copies, page-locked
 
 struct ServeJob {
     uint64_t ticket = 0;
@@ -58,11 +65,24 @@ struct ServeJob {
     unsigned long long* d_mm = nullptr;
     double t_submit = 0, t_admit = 0, t_done = 0;
     double remaining = 0;       // interactions left
+    double est_s = 0;           // estimated isolated service time
+    double deadline = 0;        // t_submit + kDeadlineFactor * est_s
     ophpc_status status = OPHPC_SUCCESS;
     bool finished = false;
 };
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+// Policy order, OPHPC_SERVE_DEADLINE: short jobs (estimated isolated time
+// under kShortJobS) first, least remaining work first among them; then the
+// others by earliest deadline. OPHPC_SERVE_SHORTEST_REMAINING: least
+// remaining work first.
+bool before(uint32_t policy, const ServeJob* a, const ServeJob* b) {
+    if (policy == OPHPC_SERVE_SHORTEST_REMAINING) return a->remaining < b->remaining;
+    const bool sa = a->est_s < kShortJobS, sb = b->est_s < kShortJobS;
+    if (sa != sb) return sa;
+    return sa ? a->remaining < b->remaining : a->deadline < b->deadline;
+}
 
 }  // namespace
 }  // namespace ophpc
@@ -238,11 +258,17 @@ void worker_main(ophpc_server* s) {
     cudaSetDevice(s->device);
     std::unique_lock<std::mutex> lk(s->mu);
     while (true) {
-        // admission, FIFO
+        // admission in policy order; the first job that does not fit blocks
+        // the ones behind it
+        const uint32_t pol = s->opt.policy;
         while (!s->queue.empty()) {
-            ServeJob* j = s->queue.front();
+            auto it = s->queue.begin();   // shortest-remaining: arrival order
+            if (pol == OPHPC_SERVE_DEADLINE)
+                it = std::min_element(s->queue.begin(), s->queue.end(),
+                                      [pol](const ServeJob* a, const ServeJob* b) { return before(pol, a, b); });
+            ServeJob* j = *it;
             if (!admit(s, j)) break;
-            s->queue.pop_front();
+            s->queue.erase(it);
             s->active.push_back(j);
         }
         if (s->stop && s->queue.empty() && s->active.empty()) break;
@@ -274,16 +300,17 @@ void worker_main(ophpc_server* s) {
             }
             ++i;
         }
-        // issue: rank active jobs by remaining work (shortest first)
+        // issue: rank active jobs in policy order (earliest deadline or
+        // least remaining work first)
         std::vector<ServeJob*> idle;
         for (ServeJob* j : s->active)
             if (!j->in_flight && j->stage < 3) idle.push_back(j);
         if (!idle.empty()) {
             std::vector<ServeJob*> ranked(s->active.begin(), s->active.end());
             std::sort(ranked.begin(), ranked.end(),
-                      [](const ServeJob* a, const ServeJob* b) { return a->remaining < b->remaining; });
+                      [pol](const ServeJob* a, const ServeJob* b) { return before(pol, a, b); });
             for (ServeJob* j : idle) {
-                // rank among admitted jobs by remaining work -> priority bucket
+                // rank among admitted jobs -> priority bucket
                 const size_t r = (size_t)(std::find(ranked.begin(), ranked.end(), j) - ranked.begin());
                 const int prio = (int)(r * kPrioLevels / ranked.size());
                 enqueue_step(s, j, std::min(prio, kPrioLevels - 1));
@@ -320,6 +347,7 @@ ophpc_status ophpc_server_create(int32_t device, const ophpc_server_options* opt
     s->device = device;
     if (options) s->opt = *options;
     if (s->opt.max_in_flight == 0) s->opt.max_in_flight = 16;
+    if (s->opt.policy > OPHPC_SERVE_SHORTEST_REMAINING) return OPHPC_ERROR_INVALID_ARGUMENT;
     if (s->opt.step_ms <= 0) s->opt.step_ms = 2.0;
     if (s->opt.reserve_bytes == 0) s->opt.reserve_bytes = (size_t)512 << 20;
     if (s->opt.memory_budget == 0) {
@@ -370,6 +398,9 @@ ophpc_status ophpc_server_submit(ophpc_server* s, const ophpc_job* job, uint64_t
     cp = std::max<int64_t>(kChunk, cp / kChunk * kChunk);
     j->chunk_points = cp;
     j->remaining = (double)job->n_points * px;
+    const double copy_bytes = (double)sizeof(ophpc_vertex) * job->n_points +
+                              (job->h_codes ? px : 0.0) + (job->h_field ? 16.0 * px : 0.0);
+    j->est_s = kJobFixedS + j->remaining / rate + copy_bytes / kCopyBytesPerS;
     if (cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming) != cudaSuccess) return OPHPC_ERROR_CUDA;
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->stop) {
@@ -378,6 +409,7 @@ ophpc_status ophpc_server_submit(ophpc_server* s, const ophpc_job* job, uint64_t
     }
     j->ticket = s->next_ticket++;
     j->t_submit = now_s(s);
+    j->deadline = j->t_submit + kDeadlineFactor * j->est_s;
     *ticket = j->ticket;
     s->queue.push_back(j.get());
     s->jobs.emplace(j->ticket, std::move(j));

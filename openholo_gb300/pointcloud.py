@@ -109,16 +109,24 @@ def read_config(path: str) -> Tuple[int, OphpcConfig, ImageConfig]:
     return st, cfg, img
 
 
-def load_ply(path: str) -> np.ndarray:
-    """(n, 7) float64 vertices (pos[3], color[3], phase); raises on error."""
+def load_ply(path: str, pinned: bool = False):
+    """(n, 7) float64 vertices (pos[3], color[3], phase); raises on error.
+    pinned=True returns a page-locked torch tensor, decoded straight into
+    it, ready for an asynchronous host-to-device copy."""
     L = _L()
-    n = L.ophpc_load_ply(path.encode(), None, 0)
+    n = L.ophpc_load_ply(path.encode(), None, 0)   # header only
     if n < 0:
         raise OphpcError(4, f"cannot load {path}")
-    out = np.zeros((n, 7), dtype=np.float64)
-    if n:
-        L.ophpc_load_ply(path.encode(), out.ctypes.data, n)
-    return out
+    if pinned:
+        import torch
+        t = torch.empty((n, 7), dtype=torch.float64).pin_memory()
+        ptr = t.data_ptr()
+    else:
+        t = np.zeros((n, 7), dtype=np.float64)
+        ptr = t.ctypes.data
+    if n and L.ophpc_load_ply(path.encode(), ptr, n) != n:
+        raise OphpcError(4, f"cannot load {path}")
+    return t
 
 
 def save_bmp(path: str, pixels: np.ndarray, bits_per_pixel: int = 8, flip: int = 0, rotate: bool = False) -> None:

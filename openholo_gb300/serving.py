@@ -9,9 +9,12 @@ import numpy as np
 
 from ._abi import OphpcConfig, OphpcError, lib, make_config
 
+POLICY_DEADLINE = 0
+POLICY_SHORTEST_REMAINING = 1
+
 
 class ServerOptions(ctypes.Structure):
-    _fields_ = [("max_in_flight", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+    _fields_ = [("max_in_flight", ctypes.c_uint32), ("policy", ctypes.c_uint32),
                 ("memory_budget", ctypes.c_uint64), ("reserve_bytes", ctypes.c_uint64),
                 ("step_ms", ctypes.c_double)]
 
@@ -64,10 +67,10 @@ class Server:
     """Continuous-batching hologram server on one GPU."""
 
     def __init__(self, device: int = 0, max_in_flight: int = 16, memory_budget: int = 0, step_ms: float = 2.0,
-                 reserve_bytes: int = 0):
+                 reserve_bytes: int = 0, policy: int = POLICY_DEADLINE):
         self._L = _L()
-        o = ServerOptions(max_in_flight=max_in_flight, memory_budget=memory_budget, reserve_bytes=reserve_bytes,
-                          step_ms=step_ms)
+        o = ServerOptions(max_in_flight=max_in_flight, policy=policy, memory_budget=memory_budget,
+                          reserve_bytes=reserve_bytes, step_ms=step_ms)
         self._h = ctypes.c_void_p()
         st = self._L.ophpc_server_create(device, ctypes.byref(o), ctypes.byref(self._h))
         if st != 0:

@@ -159,6 +159,38 @@ def make_ohc(xml):
     return out
 
 
+def write_ply_binary_faces(path, xyz, rgb_f):
+    """binary_little_endian with a color channel element, colourless
+    vertices (float x y z) and one face per vertex (a uchar-counted int list
+    of 3 indices, then uchar red green blue): vertex e takes face e's colour.
+    (With colours on both elements the reference reads the face records
+    with the vertex's property indices and loses its place in the file.)"""
+    n = xyz.shape[0]
+    hdr = ("ply\nformat binary_little_endian 1.0\nelement color 1\nproperty int channel\n"
+           f"element vertex {n}\nproperty float x\nproperty float y\nproperty float z\n"
+           f"element face {n}\nproperty list uchar int vertex_indices\n"
+           "property uchar red\nproperty uchar green\nproperty uchar blue\nend_header\n")
+    with open(path, "wb") as f:
+        f.write(hdr.encode())
+        f.write(struct.pack("<i", 3))
+        for i in range(n):
+            f.write(struct.pack("<fff", xyz[i, 0], xyz[i, 1], xyz[i, 2]))
+        for i in range(n):
+            f.write(struct.pack("<Biii", 3, i, (i + 1) % n, (i + 2) % n))
+            f.write(struct.pack("<BBB", *(int(c) for c in rgb_f[i])))
+
+
+def make_ply_faces():
+    """PLY with a face element: what the reference's PLYparser returns."""
+    rng = np.random.default_rng(13)
+    n = 48
+    xyz = np.round(rng.uniform(-0.5, 0.5, (n, 3)), 6)
+    path = os.path.join(HERE, "ply_binary_faces.ply")
+    write_ply_binary_faces(path, xyz, rng.integers(0, 256, (n, 3)))
+    np.savez_compressed(os.path.join(HERE, "ply_faces.npz"), ply_binary_faces=oracle.ref_load_ply(path))
+    return {"ply_faces": n}
+
+
 ENCODER_FLAGS = (2, 3, 4, 5, 6)   # Real, Imaginary, SimpleNI, Burckhardt, TwoPhase
 
 
@@ -271,12 +303,13 @@ def main():
 
         out.update(make_ohc(xml))
         out.update(make_encoders(xml))
+        out.update(make_ply_faces())
     for k, v in out.items():
         print(k, v)
 
 
 if __name__ == "__main__":
-    only = {"ohc": make_ohc, "encoders": make_encoders}
+    only = {"ohc": make_ohc, "encoders": make_encoders, "ply_faces": lambda xml: make_ply_faces()}
     if len(sys.argv) == 2 and sys.argv[1] in only:   # one group of fixtures
         if not oracle.ref_available():
             oracle.build(with_reference=True)

@@ -19,6 +19,79 @@ def test_ply_matches_reference_parser(name):
     assert np.array_equal(got, want)
 
 
+def test_ply_faces_match_reference_parser():
+    """Face colours (a list property before them) land on the vertices."""
+    want = np.load(os.path.join(GOLD, "ply_faces.npz"))["ply_binary_faces"]
+    assert np.array_equal(P.load_ply(os.path.join(GOLD, "ply_binary_faces.ply")), want)
+
+
+def _binary_ply(path, xyz, rgb, extra_double=False, truncate=0):
+    """binary_little_endian vertices: float x y z, [double nx unused],
+    uchar red green blue, float phase; optionally cut short."""
+    n = xyz.shape[0]
+    props = "property float x\nproperty float y\nproperty float z\n"
+    if extra_double:
+        props += "property double nx\n"
+    props += "property uchar red\nproperty uchar green\nproperty uchar blue\nproperty float phase\n"
+    hdr = (f"ply\nformat binary_little_endian 1.0\nelement color 1\nproperty int channel\n"
+           f"element vertex {n}\n{props}end_header\n").encode()
+    fields = [("x", "<f4"), ("y", "<f4"), ("z", "<f4")] + ([("nx", "<f8")] if extra_double else []) + \
+             [("r", "u1"), ("g", "u1"), ("b", "u1"), ("p", "<f4")]
+    rec = np.zeros(n, dtype=fields)
+    rec["x"], rec["y"], rec["z"] = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    rec["r"], rec["g"], rec["b"] = rgb[:, 0], rgb[:, 1], rgb[:, 2]
+    rec["p"] = np.linspace(0, 6, n, dtype=np.float32)
+    body = struct.pack("<i", 3) + rec.tobytes()
+    with open(path, "wb") as f:
+        f.write(hdr + body[:len(body) - truncate])
+    return rec
+
+
+@pytest.mark.parametrize("extra_double", [False, True])
+def test_ply_binary_bulk_decode(tmp_path, extra_double):
+    """200,000 records (decoded in parallel ranges), with and without a
+    property the vertex does not use between the coordinates and colours."""
+    rng = np.random.default_rng(21)
+    n = 200_000
+    xyz = rng.uniform(-1, 1, (n, 3)).astype(np.float32)
+    rgb = rng.integers(0, 256, (n, 3)).astype(np.uint8)
+    rec = _binary_ply(tmp_path / "b.ply", xyz, rgb, extra_double)
+    got = P.load_ply(str(tmp_path / "b.ply"))
+    assert got.shape == (n, 7)
+    assert np.array_equal(got[:, :3], xyz.astype(np.float64))
+    assert np.array_equal(got[:, 3:6], (rgb.astype(np.float32) / np.float32(255.0)).astype(np.float64))
+    assert np.array_equal(got[:, 6], rec["p"].astype(np.float64))
+
+
+def test_ply_truncated_data_fails(tmp_path):
+    rng = np.random.default_rng(22)
+    xyz = rng.uniform(-1, 1, (100, 3)).astype(np.float32)
+    rgb = rng.integers(0, 256, (100, 3)).astype(np.uint8)
+    _binary_ply(tmp_path / "t.ply", xyz, rgb, truncate=5)
+    with pytest.raises(Exception):
+        P.load_ply(str(tmp_path / "t.ply"))
+    with P.PointCloud() as h:
+        assert h.loadPointCloud(str(tmp_path / "t.ply")) == -1
+    # ASCII with a missing last line
+    txt = "ply\nformat ascii 1.0\nelement vertex 3\nproperty float x\nproperty float y\nproperty float z\n" \
+          "end_header\n1 2 3\n4 5 6\n"
+    (tmp_path / "a.ply").write_text(txt)
+    with pytest.raises(Exception):
+        P.load_ply(str(tmp_path / "a.ply"))
+
+
+def test_ply_count_reads_header_only(tmp_path):
+    """ophpc_load_ply(path, NULL, 0) answers from the header alone."""
+    import ctypes
+    from openholo_gb300 import lib
+    rng = np.random.default_rng(23)
+    _binary_ply(tmp_path / "c.ply", rng.uniform(-1, 1, (50, 3)).astype(np.float32),
+                rng.integers(0, 256, (50, 3)).astype(np.uint8), truncate=20)
+    L = lib()
+    L.ophpc_load_ply.restype = ctypes.c_int64
+    assert L.ophpc_load_ply(str(tmp_path / "c.ply").encode(), None, ctypes.c_uint64(0)) == 50
+
+
 def test_ply_appends_extension_and_fails_cleanly(tmp_path):
     got = P.load_ply(os.path.join(GOLD, "ply_ascii_channel"))   # ".ply" appended
     assert got.shape[0] == 64

@@ -86,3 +86,20 @@ def test_memory_admission_serialises_jobs(gpu_ctx):
         big = dict(pnx=4096, pny=4096, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
         with pytest.raises(OphpcError):
             srv.submit(big, np.zeros((10, 7)), 0)
+
+
+def test_policies_give_identical_results(gpu_ctx):
+    """Earliest-deadline and shortest-remaining scheduling reorder steps, not
+    arithmetic: every job's field is the same under both."""
+    from openholo_gb300 import OphpcError
+    from openholo_gb300.serving import POLICY_DEADLINE, POLICY_SHORTEST_REMAINING, Server
+    jobs = _jobs(seed=7)
+    fields = {}
+    for pol in (POLICY_DEADLINE, POLICY_SHORTEST_REMAINING):
+        with Server(0, max_in_flight=4, step_ms=0.5, policy=pol) as srv:
+            tickets = [srv.submit(g, v, d) for g, v, d in jobs]
+            fields[pol] = [srv.wait(t).field for t in tickets]
+    for a, b in zip(fields[POLICY_DEADLINE], fields[POLICY_SHORTEST_REMAINING]):
+        assert np.array_equal(a, b)
+    with pytest.raises(OphpcError):
+        Server(0, policy=7)
