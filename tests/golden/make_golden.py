@@ -191,6 +191,60 @@ def make_ply_faces():
     return {"ply_faces": n}
 
 
+REFERENCE = oracle.REFERENCE_TREE
+DICE_DIR = os.path.join(REFERENCE, "Example", "dataset", "Dice", "PointCloud")
+DICE_RGB = os.path.join(REFERENCE, "Openholo_python", "test", "PointCloud_Dice_RGB.ply")
+
+
+def _sampled(field, enc, codes, n_sample, seed):
+    """Field, encodings and codes at seeded pixels of every channel, plus the
+    normalisation range (min, max of the encoded buffer over all channels)."""
+    nch, pny, pnx = field.shape
+    rng = np.random.default_rng(seed)
+    idx = np.sort(rng.choice(pny * pnx, n_sample, replace=False))
+    out = {"pixel_index": idx, "field_at": field.reshape(nch, -1)[:, idx]}
+    for k, name in enumerate(("phase", "amp")):
+        out[f"codes_{name}_at"] = codes[k].reshape(nch, -1)[:, idx]
+        out[f"enc_{name}_range"] = np.array([enc[k].min(), enc[k].max()])
+    return out
+
+
+def make_dice(xml):
+    """The reference's own example fixtures through its CPU path:
+    Example/dataset/Dice/PointCloud (Dice_PointCloud.xml + dice_100000.ply,
+    7,493 points, 1920x1080, RS and Fresnel) and
+    Openholo_python/test/PointCloud_Dice_RGB.ply (1,461 points) with the Dice
+    geometry in three colours. Stored: the vertices the reference's PLY
+    parser returns, the config, and the field / codes at 16,384 seeded
+    pixels with the normalisation range (the full 1920x1080 field is 33 MB
+    per channel)."""
+    out = {}
+    dice_xml = open(os.path.join(DICE_DIR, "Dice_PointCloud.xml")).read()
+    ply = os.path.join(DICE_DIR, "dice_100000.ply")
+    verts = oracle.ref_load_ply(ply)
+    with open(xml, "w") as f:
+        f.write(dice_xml)
+    res = {"vertices": verts, "xml": dice_xml}
+    for diff, tag in ((0, "rs"), (1, "fresnel")):
+        field, enc, codes, secs = oracle.ref_run(xml, ply_path=ply, diff_flag=diff, encode_flag=2)
+        for k, v in _sampled(field, enc, codes, 16384, 31 + diff).items():
+            res[f"{tag}_{k}"] = v
+        out[f"dice_{tag}"] = round(secs, 1)
+    np.savez_compressed(os.path.join(HERE, "dice.npz"), **res)
+    rgb_xml = dice_xml.replace("<SLM_WaveNum>1</SLM_WaveNum>", "<SLM_WaveNum>3</SLM_WaveNum>").replace(
+        "<SLM_WaveLength_1>532e-9</SLM_WaveLength_1>",
+        "<SLM_WaveLength_1>638e-9</SLM_WaveLength_1> <SLM_WaveLength_2>532e-9</SLM_WaveLength_2> "
+        "<SLM_WaveLength_3>473e-9</SLM_WaveLength_3>")
+    with open(xml, "w") as f:
+        f.write(rgb_xml)
+    field, enc, codes, secs = oracle.ref_run(xml, ply_path=DICE_RGB, diff_flag=0, encode_flag=2)
+    res = {"vertices": oracle.ref_load_ply(DICE_RGB), "xml": rgb_xml}
+    res.update(_sampled(field, enc, codes, 16384, 33))
+    np.savez_compressed(os.path.join(HERE, "dice_rgb.npz"), **res)
+    out["dice_rgb_rs"] = round(secs, 1)
+    return out
+
+
 ENCODER_FLAGS = (2, 3, 4, 5, 6)   # Real, Imaginary, SimpleNI, Burckhardt, TwoPhase
 
 
@@ -304,12 +358,14 @@ def main():
         out.update(make_ohc(xml))
         out.update(make_encoders(xml))
         out.update(make_ply_faces())
+        out.update(make_dice(xml))
     for k, v in out.items():
         print(k, v)
 
 
 if __name__ == "__main__":
-    only = {"ohc": make_ohc, "encoders": make_encoders, "ply_faces": lambda xml: make_ply_faces()}
+    only = {"ohc": make_ohc, "encoders": make_encoders, "ply_faces": lambda xml: make_ply_faces(),
+            "dice": make_dice}
     if len(sys.argv) == 2 and sys.argv[1] in only:   # one group of fixtures
         if not oracle.ref_available():
             oracle.build(with_reference=True)
