@@ -16,8 +16,11 @@
 // where r_p^2 - r_c^2 = 2 dx_c u + u^2 + 2 dy_c v + v^2 is formed from small
 // tile-local offsets (u, v) and splits into a per-column plus a per-row part.
 // In the FAST class (tile inside the window, |w| small) the series
-// w/2 - w^2/8 replaces sqrt and division, so a pixel costs ~11 FP32 ops and
-// two MUFU (sin, cos). Tiles the window cuts, or with large |w|, go to the
+// w/2 - w^2/8 replaces sqrt and division, and the phase is carried in
+// radians: 2 pi frac(r_c/lambda) plus tile-local offsets that the class
+// keeps within +-16 turns, so the MUFU sin/cos (whose own argument scaling
+// stays accurate to ~1e-5 rad there) needs no per-pixel reduction. A pixel
+// costs 7 FP32 issue slots and two MUFU (sin, cos). Tiles the window cuts, or with large |w|, go to the
 // EXACT class: integer rectangle test, the reference's cone test (FP32 with
 // a margin, FP64 replica of ophGen.cpp:415-428 when inside the margin) and
 // the exact r_p. Sums run in FP32 per chunk and are folded into FP64
@@ -29,9 +32,9 @@ namespace ophpc {
 namespace {
 
 struct __align__(16) RsSRec {
-    float P, Q, h, g;        // FAST: 2dxc/rc2, 2dyc/rc2, 1/rc2, rc/(2 lambda). EXACT: 2dxc, 2dyc, rc2, rc
-    float fc, ac, dxc, dyc;  // frac(rc/lambda) in [-.5,.5]; FAST: coef/rc2, -rc/(8 lambda), -
-                             // EXACT: coef, dxc, dyc
+    float P, Q, h, g;        // FAST: 2dxc/rc2, 2dyc/rc2, 1/rc2, pi rc/lambda. EXACT: 2dxc, 2dyc, rc2, rc
+    float fc, ac, dxc, dyc;  // FAST: 2 pi frac(rc/lambda), coef/rc2, -pi rc/(4 lambda), -
+                             // EXACT: frac(rc/lambda) in [-.5,.5], coef, dxc, dyc
     float zz, mabs;          // EXACT: z^2, absolute margin of the FP32 cone test
     int32_t idx;             // EXACT: point index (FP64 fallback)
     int32_t xl, xh, yl, yh;  // EXACT: window rectangle relative to the tile origin
@@ -44,6 +47,10 @@ constexpr float kTwoPi = 6.283185307179586f;
 // and |w| below kMaxW (the dropped amplitude term is w^2).
 constexpr float kSeriesTol = 2e-8f;
 constexpr float kMaxW = 1e-3f;
+// FAST also requires the tile-local phase offset (tc/2)|w| + (tc/8)w^2 below
+// this many turns: the FP32 phase in radians then stays under ~103 rad.
+constexpr float kMaxTurns = 16.f;
+constexpr float kPi = 3.14159265358979f;
 
 __device__ __forceinline__ int warp_prefix(unsigned ballot) {
     return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
@@ -137,7 +144,8 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                     const float nmax = fmaf(2.f * fabsf(dxf), uext_f, uext_f * uext_f) +
                                        fmaf(2.f * fabsf(dyf), vext_f, vext_f * vext_f);
                     const float wmax = nmax * hf;
-                    const bool series_ok = wmax < kMaxW && tcf * wmax * wmax * wmax * (1.f / 16.f) < kSeriesTol;
+                    const bool series_ok = wmax < kMaxW && tcf * wmax * wmax * wmax * (1.f / 16.f) < kSeriesTol &&
+                                           tcf * wmax * fmaf(0.125f, wmax, 0.5f) < kMaxTurns;
                     RsSRec& t = tmp[q];
                     t.fc = fc;
                     if (rect_full && cone_full && series_ok) {
@@ -145,8 +153,10 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                         t.P = 2.f * dxf * hf;
                         t.Q = 2.f * dyf * hf;
                         t.h = hf;
-                        t.g = 0.5f * tcf;           // phase = fc + (tc/2) w - (tc/8) w^2
-                        t.dxc = -0.125f * tcf;
+                        // phase (rad) = 2 pi (fc + (tc/2) w - (tc/8) w^2)
+                        t.fc = kTwoPi * fc;
+                        t.g = kPi * tcf;
+                        t.dxc = -0.25f * kPi * tcf;
                         t.ac = (float)p.coef * hf;
                     } else {
                         cls[q] = 2;
@@ -208,8 +218,8 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
         for (int k = 0; k < kPixH * kPixW; ++k) sr[k] = si[k] = 0.f;
 #pragma unroll 1
         for (int j = 0; j < n_fast; ++j) {
-            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);    // P, Q, h, tc/2
-            const float4 b = *reinterpret_cast<const float4*>(&s_rec[j].fc);   // fc, ac, -tc/8, -
+            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);    // P, Q, h, pi tc
+            const float4 b = *reinterpret_cast<const float4*>(&s_rec[j].fc);   // 2 pi fc, ac, -pi tc/4, -
             float A[kPixW], B[kPixH];
 #pragma unroll
             for (int c = 0; c < kPixW; ++c) A[c] = fmaf(a.x, u[c], a.z * uu[c]);
@@ -220,10 +230,9 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
 #pragma unroll
                 for (int c = 0; c < kPixW; ++c) {
                     const float w = A[c] + B[r];
-                    float t = fmaf(w, fmaf(w, b.z, a.w), b.x);
-                    t = reduce_turns(t);
+                    const float ph = fmaf(w, fmaf(w, b.z, a.w), b.x);   // radians, |ph| < ~103
                     float s, co;
-                    __sincosf(t * kTwoPi, &s, &co);
+                    __sincosf(ph, &s, &co);
                     const float amp = fmaf(-b.y, w, b.y);
                     const int k = r * kPixW + c;
                     sr[k] = fmaf(amp, s, sr[k]);
