@@ -420,6 +420,7 @@ def gpu_arm(args, w):
     if rank == 0:
         cpu = None
         rel = None
+        rel_fp64 = {}
         if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
             # cpu_baseline leg: the CPU point-cloud path on a bounded sample of
             # the same workload, and the GPU result on that sample checked
@@ -434,6 +435,20 @@ def gpu_arm(args, w):
             g = fsub.cpu().numpy()
             got = g[..., 0] + 1j * g[..., 1]
             rel = float(np.linalg.norm(got - ref_field) / np.linalg.norm(ref_field))
+            # every Fresnel variant against the FP64 CPU field on a smaller sample
+            n_fr = max(50, n_cpu // 3)
+            _, _, _, ref_fr = cpu_sample_run(w, n_fr, 1)
+            subf = w.subset(n_fr)
+            dsubf = torch.from_numpy(subf.vertices).cuda()
+            for name, mode in (("fresnel_plain", 0), ("fresnel_tc_fp16", oph.MODE_TENSOR_FP16),
+                               ("fresnel_tc_bf16x3", oph.MODE_TENSOR_BF16X3)):
+                ctx.generate(cfg, dsubf.data_ptr(), subf.n_points, oph.DIFF_FRESNEL, mode, fsub.data_ptr(), sp)
+                torch.cuda.synchronize()
+                g = fsub.cpu().numpy()
+                got = g[..., 0] + 1j * g[..., 1]
+                rel_fp64[name] = float(np.linalg.norm(got - ref_fr) / np.linalg.norm(ref_fr))
+            rel_fp64["rs"] = rel
+            rel_fp64["samples"] = f"RS {n_cpu} points, Fresnel {n_fr} points, full {w.pnx}x{w.pny}x{w.n_channels}"
             cpu = {"value": rate, "unit": UNIT, "cores": host_cores(), "kind": kind,
                    "sample": f"{n_cpu} of {w.n_points} points at full {w.pnx}x{w.pny}, {w.n_channels} channels, RS "
                              f"({secs:.1f} s, OpenMP, {cpu_model()})",
@@ -447,6 +462,7 @@ def gpu_arm(args, w):
                        "step": "generateHologram(RS, 3 channels) + phase encode + normalise",
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
             "relL2": rel,
+            "relL2_vs_fp64": rel_fp64 or None,
             "roofline": {"bound": "sfu", "kernel": "rs_kernel", "achieved": achieved_rs, "peak": peak_rs,
                          "unit": "interactions/s", "frac": achieved_rs / peak_rs,
                          "traffic": RS_TRAFFIC_BYTES.get(w.name), "traffic_unit": "bytes per launch (DRAM)",

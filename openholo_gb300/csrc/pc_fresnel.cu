@@ -11,8 +11,12 @@
 // tau_c is evaluated in FP64 per (point, tile) and reduced mod 1 (the one FP64
 // step); each thread then forms one complex factor per column and per row of
 // its 4x4 pixel block (8 sin/cos pairs) and accumulates their products: a
-// complex rank-1 update per point, four FMAs per pixel. The rectangle is
-// applied as 0/1 masks on the factors. Sums run in FP32 per chunk of 256
+// complex rank-1 update per point, four FMAs per pixel. Points whose window
+// holds the whole tile and whose column / row phases span under 16 turns
+// (FAST, the common case) carry the phases in radians straight into the
+// MUFU sin/cos, with no reduction and no masks; for the others (CUT) the
+// phases are reduced mod 1 and the rectangle is applied as 0/1 masks on the
+// factors. Sums run in FP32 per chunk of 256
 // points and fold into FP64 shared-memory sums; every pixel is stored once.
 #include "pc_common.cuh"
 
@@ -33,6 +37,10 @@ struct __align__(16) FrSRec {
 static_assert(sizeof(FrSRec) == 64, "FrSRec size");
 
 constexpr float kTwoPi = 6.283185307179586f;
+// FAST class: column and row phases stay within this many turns over the
+// tile, so the FP32 phase in radians stays under ~101 rad and MUFU sin/cos
+// take it without a reduction.
+constexpr float kMaxTurns = 16.f;
 
 __device__ __forceinline__ int warp_prefix(unsigned ballot) {
     return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
@@ -45,7 +53,7 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
     FrSRec* s_rec = reinterpret_cast<FrSRec*>(s_raw);
     // FP64 running sums, [pixel][thread]: consecutive threads hit consecutive 16-byte words
     double2* s_acc = reinterpret_cast<double2*>(s_raw + sizeof(FrSRec) * kChunk);
-    __shared__ int s_cnt[2][kThreads / 32];
+    __shared__ int s_cnt[2][2][kThreads / 32];   // [fast|cut][q][warp]
 
     const int ch = blockIdx.z / jg.ksplit;
     const int part = blockIdx.z % jg.ksplit;
@@ -56,6 +64,9 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
 
     const int tx = threadIdx.x % kThreadsX, ty = threadIdx.x / kThreadsX;
     const int warp = threadIdx.x >> 5;
+    // largest |u|, |v| of a tile pixel from the tile centre (one column /
+    // row of slack)
+    const float uext_f = (float)((kTileW / 2 + 1) * g.ppX), vext_f = (float)((kTileH / 2 + 1) * g.ppY);
     float u[kPixW], uu[kPixW], v[kPixH], vv[kPixH];
 #pragma unroll
     for (int c = 0; c < kPixW; ++c) {
@@ -90,28 +101,40 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
     const PointRec* chrec = recs + (int64_t)ch * n;
 
     for (int64_t cb = p_beg; cb < p_end; cb += kChunk) {
-        bool keep[2];
+        int cls[2];   // 0 skip, 1 FAST (window holds the tile, small phase spans), 2 CUT
         FrSRec tmp[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-            keep[q] = false;
+            cls[q] = 0;
             const int64_t idx = cb + threadIdx.x + q * kThreads;
             if (idx < p_end) {
                 const PointRec p = chrec[idx];
                 const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
                 const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
                 if (ix0 < ix1 && iy0 < iy1) {
-                    keep[q] = true;
                     const double dxc = Xc - p.x, dyc = Yc - p.y;
                     const double s = p.aux;   // 1 / (2 z lambda)
                     const double tc = (dxc * dxc + dyc * dyc + 2.0 * p.z * p.z) * s;
                     FrSRec& t = tmp[q];
                     const float P = (float)(2.0 * dxc * s), Q = (float)(2.0 * dyc * s), sf = (float)s;
                     const float fc = (float)(tc - rint(tc));
-                    t.P = make_float2(P, P);
-                    t.Q = make_float2(Q, Q);
-                    t.s = make_float2(sf, sf);
-                    t.fc = make_float2(fc, fc);
+                    const bool full = p.x_lo <= X0 && p.x_hi >= vx1 && p.y_lo <= Y0 && p.y_hi >= vy1;
+                    // column phase fc + P u + s u^2 and row phase Q v + s v^2 (turns) over the tile
+                    const float colspan = 0.5f + fabsf(P) * uext_f + sf * uext_f * uext_f;
+                    const float rowspan = fabsf(Q) * vext_f + sf * vext_f * vext_f;
+                    if (full && colspan < kMaxTurns && rowspan < kMaxTurns) {
+                        cls[q] = 1;   // phases in radians, no masks, no reduction
+                        t.P = make_float2(kTwoPi * P, kTwoPi * P);
+                        t.Q = make_float2(kTwoPi * Q, kTwoPi * Q);
+                        t.s = make_float2(kTwoPi * sf, kTwoPi * sf);
+                        t.fc = make_float2(kTwoPi * fc, kTwoPi * fc);
+                    } else {
+                        cls[q] = 2;
+                        t.P = make_float2(P, P);
+                        t.Q = make_float2(Q, Q);
+                        t.s = make_float2(sf, sf);
+                        t.fc = make_float2(fc, fc);
+                    }
                     t.ac = (float)p.coef;
                     t.xl = p.x_lo - X0;
                     t.xh = p.x_hi - X0;
@@ -120,25 +143,36 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
                 }
             }
         }
-        unsigned bk[2];
+        // deterministic compaction: FAST from the front, CUT from the back
+        unsigned bf[2], bc[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-            bk[q] = __ballot_sync(0xffffffffu, keep[q]);
-            if ((threadIdx.x & 31) == 0) s_cnt[q][warp] = __popc(bk[q]);
+            bf[q] = __ballot_sync(0xffffffffu, cls[q] == 1);
+            bc[q] = __ballot_sync(0xffffffffu, cls[q] == 2);
+            if ((threadIdx.x & 31) == 0) {
+                s_cnt[0][q][warp] = __popc(bf[q]);
+                s_cnt[1][q][warp] = __popc(bc[q]);
+            }
         }
         __syncthreads();
-        int n_keep = 0, off[2];
+        int n_fast = 0, n_cut = 0, off_f[2], off_c[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
 #pragma unroll
             for (int w = 0; w < kThreads / 32; ++w) {
-                if (w == warp) off[q] = n_keep;
-                n_keep += s_cnt[q][w];
+                if (w == warp) {
+                    off_f[q] = n_fast;
+                    off_c[q] = n_cut;
+                }
+                n_fast += s_cnt[0][q][w];
+                n_cut += s_cnt[1][q][w];
             }
         }
 #pragma unroll
-        for (int q = 0; q < 2; ++q)
-            if (keep[q]) s_rec[off[q] + warp_prefix(bk[q])] = tmp[q];
+        for (int q = 0; q < 2; ++q) {
+            if (cls[q] == 1) s_rec[off_f[q] + warp_prefix(bf[q])] = tmp[q];
+            else if (cls[q] == 2) s_rec[kChunk - 1 - (off_c[q] + warp_prefix(bc[q]))] = tmp[q];
+        }
         __syncthreads();
 
         // accumulators: one packed (re, im) pair per pixel
@@ -146,8 +180,54 @@ fresnel_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __r
 #pragma unroll
         for (int k = 0; k < kPixH * kPixW; ++k) acc[k] = 0ull;
         const f2::v2 two_pi = f2::splat(kTwoPi);
+        // ---- FAST: radians, no window masks, no reduction -----------------
 #pragma unroll 1
-        for (int j = 0; j < n_keep; ++j) {
+        for (int j = 0; j < n_fast; ++j) {
+            const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&s_rec[j]);
+            const ulonglong2 r0 = R[0], r1 = R[1];
+            const f2::v2 P = r0.x, Q = r0.y, sp = r1.x, fc = r1.y;
+            const float ac = s_rec[j].ac;
+            f2::v2 ca[kPixW], cb[kPixW];
+#pragma unroll
+            for (int p = 0; p < kPixW / 2; ++p) {
+                const f2::v2 t = f2::fma(P, up[p], f2::fma(sp, uup[p], fc));
+                float x[2];
+                f2::unpack(t, x[0], x[1]);
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    float sn, cs;
+                    __sincosf(x[k], &sn, &cs);
+                    ca[2 * p + k] = f2::splat(ac * cs);
+                    cb[2 * p + k] = f2::splat(ac * sn);
+                }
+            }
+            f2::v2 r1p[kPixH], r2p[kPixH];
+#pragma unroll
+            for (int p = 0; p < kPixH / 2; ++p) {
+                const f2::v2 t = f2::fma(Q, vp[p], f2::mul(sp, vvp[p]));
+                float x[2];
+                f2::unpack(t, x[0], x[1]);
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    float sn, cs;
+                    __sincosf(x[k], &sn, &cs);
+                    r1p[2 * p + k] = f2::pack(cs, sn);
+                    r2p[2 * p + k] = f2::pack(-sn, cs);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < kPixH; ++r) {
+#pragma unroll
+                for (int c = 0; c < kPixW; ++c) {
+                    const int k = r * kPixW + c;
+                    acc[k] = f2::fma(ca[c], r1p[r], f2::fma(cb[c], r2p[r], acc[k]));
+                }
+            }
+        }
+        // ---- CUT: the window cuts the tile or a phase span is large --------
+#pragma unroll 1
+        for (int jj = 0; jj < n_cut; ++jj) {
+            const int j = kChunk - 1 - jj;
             const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&s_rec[j]);
             const ulonglong2 r0 = R[0], r1 = R[1];
             const f2::v2 P = r0.x, Q = r0.y, sp = r1.x, fc = r1.y;
