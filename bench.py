@@ -449,6 +449,27 @@ def gpu_arm(args, w):
                 rel_fp64[name] = float(np.linalg.norm(got - ref_fr) / np.linalg.norm(ref_fr))
             rel_fp64["rs"] = rel
             rel_fp64["samples"] = f"RS {n_cpu} points, Fresnel {n_fr} points, full {w.pnx}x{w.pny}x{w.n_channels}"
+            # all points at seeded pixels: the error at the workload's full
+            # size (it grows with the point count: part of it is common to
+            # every point's phase)
+            import oracle
+            gw = oracle.Geometry(pnx=w.pnx, pny=w.pny, ppx=w.pp, ppy=w.pp, wavelengths=list(w.wavelengths),
+                                 scale=w.scale, distance=w.distance)
+            pix = np.sort(np.random.default_rng(17).choice(npx, 256, replace=False))
+            full, wants = {}, {}
+            for name, diff, mode in (("rs", 0, 0), ("fresnel_plain", 1, 0),
+                                     ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3),
+                                     ("fresnel_tc_fp16", 1, oph.MODE_TENSOR_FP16)):
+                ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, fsub.data_ptr(), sp)
+                torch.cuda.synchronize()
+                g = fsub.reshape(nch, npx, 2)[:, torch.from_numpy(pix).cuda()].cpu().numpy()
+                got = g[..., 0] + 1j * g[..., 1]
+                if diff not in wants:
+                    wants[diff] = np.stack([oracle.field_at(gw, w.vertices, diff, c, pix) for c in range(nch)])
+                want = wants[diff]
+                full[name] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+            full["samples"] = f"all {w.n_points} points at 256 seeded pixels per channel"
+            rel_fp64["full_size"] = full
             cpu = {"value": rate, "unit": UNIT, "cores": host_cores(), "kind": kind,
                    "sample": f"{n_cpu} of {w.n_points} points at full {w.pnx}x{w.pny}, {w.n_channels} channels, RS "
                              f"({secs:.1f} s, OpenMP, {cpu_model()})",
