@@ -175,7 +175,9 @@ def reference_arm(args, w):
     rank, world, _ = env_rank()
     if rank != 0:
         return
-    n = args.cpu_points or 60
+    # 300 points: enough for the OpenMP point loop to keep 16+ threads busy
+    # (60 points left it starved and under-reported the CPU by 2.5x)
+    n = args.cpu_points or 300
     for _ in range(max(0, args.warmup)):
         cpu_sample_run(w, n, 0)
     times = []
