@@ -20,7 +20,9 @@
 // radians: 2 pi frac(r_c/lambda) plus tile-local offsets that the class
 // keeps within +-16 turns, so the MUFU sin/cos (whose own argument scaling
 // stays accurate to ~1e-5 rad there) needs no per-pixel reduction. A pixel
-// costs 7 FP32 issue slots and two MUFU (sin, cos). Tiles the window cuts, or with large |w|, go to the
+// costs 7 FP32 issue slots and two MUFU (sin, cos); two pixels of each 4x4
+// block instead take the phase in turns, reduce it, and evaluate sin/cos as
+// polynomials on the FMA pipe, which relieves the MUFU (the kernel's bound). Tiles the window cuts, or with large |w|, go to the
 // EXACT class: integer rectangle test, the reference's cone test (FP32 with
 // a margin, FP64 replica of ophGen.cpp:415-428 when inside the margin) and
 // the exact r_p. Sums run in FP32 per chunk and are folded into FP64
@@ -51,6 +53,36 @@ constexpr float kMaxW = 1e-3f;
 // this many turns: the FP32 phase in radians then stays under ~103 rad.
 constexpr float kMaxTurns = 16.f;
 constexpr float kPi = 3.14159265358979f;
+
+// Pixels of a thread's 4x4 block (bit r*4 + c) whose sin/cos run as
+// polynomials on the FMA pipe instead of the MUFU, to balance the two pipes:
+// two corner pixels of 16. Measured at sphere_fhd on GB300: 0 pixels
+// 2.28e12 interactions/s, 1 2.37e12, 2 2.36-2.43e12 (by placement), 3
+// 2.26e12, 4 2.15e12; the block issue rate, not the MUFU, binds beyond two.
+constexpr unsigned kPolyMask = 0x8001u;
+
+// sin(2 pi t) and cos(2 pi t) for t in [-0.5, 0.5]: sin = t S(t^2) (degree 5
+// in t^2), cos = C(t^2) (degree 6), least-squares fits on Chebyshev nodes of
+// [0, 0.5] made for this kernel; evaluated with FMA in FP32 the error is
+// below 4e-7 (sin) and 6e-7 (cos) absolute, as good as the MUFU's.
+__device__ __forceinline__ void sincos_turns_poly(float t, float* s, float* c) {
+    const float u = t * t;
+    float ps = -1.230215740e+01f;
+    ps = fmaf(ps, u, 4.122758102e+01f);
+    ps = fmaf(ps, u, -7.658597565e+01f);
+    ps = fmaf(ps, u, 8.159687805e+01f);
+    ps = fmaf(ps, u, -4.134145737e+01f);
+    ps = fmaf(ps, u, 6.283183575e+00f);
+    float pc = 6.547553062e+00f;
+    pc = fmaf(pc, u, -2.598241234e+01f);
+    pc = fmaf(pc, u, 6.017204666e+01f);
+    pc = fmaf(pc, u, -8.545075989e+01f);
+    pc = fmaf(pc, u, 6.493915558e+01f);
+    pc = fmaf(pc, u, -1.973920631e+01f);
+    pc = fmaf(pc, u, 1.0f);
+    *s = ps * t;
+    *c = pc;
+}
 
 __device__ __forceinline__ int warp_prefix(unsigned ballot) {
     return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
@@ -153,10 +185,14 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                         t.P = 2.f * dxf * hf;
                         t.Q = 2.f * dyf * hf;
                         t.h = hf;
-                        // phase (rad) = 2 pi (fc + (tc/2) w - (tc/8) w^2)
+                        // phase (rad) = 2 pi (fc + (tc/2) w - (tc/8) w^2);
+                        // the same in turns for the polynomial pixels
                         t.fc = kTwoPi * fc;
                         t.g = kPi * tcf;
                         t.dxc = -0.25f * kPi * tcf;
+                        t.dyc = fc;
+                        t.zz = 0.5f * tcf;
+                        t.mabs = -0.125f * tcf;
                         t.ac = (float)p.coef * hf;
                     } else {
                         cls[q] = 2;
@@ -219,7 +255,8 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
 #pragma unroll 1
         for (int j = 0; j < n_fast; ++j) {
             const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);    // P, Q, h, pi tc
-            const float4 b = *reinterpret_cast<const float4*>(&s_rec[j].fc);   // 2 pi fc, ac, -pi tc/4, -
+            const float4 b = *reinterpret_cast<const float4*>(&s_rec[j].fc);   // 2 pi fc, ac, -pi tc/4, fc
+            const float2 tq = *reinterpret_cast<const float2*>(&s_rec[j].zz);   // tc/2, -tc/8 (turns)
             float A[kPixW], B[kPixH];
 #pragma unroll
             for (int c = 0; c < kPixW; ++c) A[c] = fmaf(a.x, u[c], a.z * uu[c]);
@@ -230,11 +267,16 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
 #pragma unroll
                 for (int c = 0; c < kPixW; ++c) {
                     const float w = A[c] + B[r];
-                    const float ph = fmaf(w, fmaf(w, b.z, a.w), b.x);   // radians, |ph| < ~103
-                    float s, co;
-                    __sincosf(ph, &s, &co);
-                    const float amp = fmaf(-b.y, w, b.y);
                     const int k = r * kPixW + c;
+                    float s, co;
+                    if ((kPolyMask >> k) & 1u) {
+                        const float tt = reduce_turns(fmaf(w, fmaf(w, tq.y, tq.x), b.w));
+                        sincos_turns_poly(tt, &s, &co);
+                    } else {
+                        const float ph = fmaf(w, fmaf(w, b.z, a.w), b.x);   // radians, |ph| < ~103
+                        __sincosf(ph, &s, &co);
+                    }
+                    const float amp = fmaf(-b.y, w, b.y);
                     sr[k] = fmaf(amp, s, sr[k]);
                     si[k] = fmaf(amp, co, si[k]);
                 }
