@@ -68,6 +68,24 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(x: float, dist, device: str) -> float:
+    """The largest x over the ranks (the slowest rank's step time): an
+    all-reduce of one value, on `device` ("cuda" under NCCL, "cpu" under
+    gloo). With no process group, x itself."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(units_per_rank: float, world: int, t_slowest: float) -> float:
+    """Whole-job throughput: every rank processes its own units (weak
+    scaling), the job ends with the slowest rank."""
+    return units_per_rank * world / t_slowest
+
+
 def host_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -338,20 +356,16 @@ def gpu_arm(args, w):
     barrier()
     wall = time.perf_counter() - wall0
     launches = lib.ophpc_kernel_launches() - l0
-    t_step = sum(step_times) / len(step_times)
-    if dist is not None:
-        tt = torch.tensor([t_step], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = max_over_ranks(sum(step_times) / len(step_times), dist, "cuda")
     inter = w.interactions
-    value = inter * world / t_step
+    value = job_value(inter, world, t_step)
 
     # --- dominant kernel alone (generate = prep + rs kernel) for the roofline
     gen_rs = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_RS, 0, field.data_ptr(), sp), 3)
     t_rs = sum(gen_rs) / len(gen_rs)
     gen_fr = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_FRESNEL, 0, field.data_ptr(), sp),
                    max(3, args.steps // 2))
-    t_fr = sum(gen_fr) / len(gen_fr)
+    t_fr = max_over_ranks(sum(gen_fr) / len(gen_fr), dist, "cuda")
 
     # --- tensor-core Fresnel (tcgen05): FP16 and split-BF16, relL2 against the
     # plain FP32 Fresnel field (itself within ~1e-6 of FP64)
@@ -405,7 +419,8 @@ def gpu_arm(args, w):
     torch.cuda.synchronize()
     e2e_times = timed(e2e_step, max(3, args.steps // 2))
     t_e2e = sum(e2e_times) / len(e2e_times)
-    e2e_value = inter * world / t_e2e
+    t_e2e = max_over_ranks(t_e2e, dist, "cuda")
+    e2e_value = job_value(inter, world, t_e2e)
     h2d = hv.numel() * 8
     d2h = hfield.numel() * 8 + hcodes.numel()
 
@@ -492,7 +507,7 @@ def gpu_arm(args, w):
                          "algorithmic_bytes": w.n_points * nch * 64 + npx * nch * 16,
                          "peak_basis": f"{sms} SMs x 16 MUFU/clk / 2 MUFU (sin, cos) per interaction x "
                                        f"{sm_mhz:.0f} MHz median SM clock under load"},
-            "fresnel": {"value": inter * world / t_fr, "unit": UNIT, "ms_per_generate": t_fr * 1e3,
+            "fresnel": {"value": job_value(inter, world, t_fr), "unit": UNIT, "ms_per_generate": t_fr * 1e3,
                         "kernel": "fresnel_kernel (FP32 cores, separable)"},
             "tensor_fresnel": tensor,
             "serving": serving,
