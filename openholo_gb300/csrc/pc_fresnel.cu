@@ -20,21 +20,24 @@
 // points and fold into FP64 shared-memory sums; every pixel is stored once.
 #include "pc_common.cuh"
 
+#include <cstddef>
+
 namespace ophpc {
 
 namespace {
 
 // Values duplicated into pairs for the packed FP32 arithmetic.
+// The CUT loop reads xl..yh as one int4, so they sit at a 16-byte offset.
 struct __align__(16) FrSRec {
     float2 P, Q;             // 2 dxc s, 2 dyc s
     float2 s, fc;            // s, frac(tau_c)
-    float ac;                // amp / (lambda z)
     int32_t xl, xh;          // window columns relative to the tile origin
-    int32_t yl;              // window rows relative to the tile origin
-    int32_t yh;
+    int32_t yl, yh;          // window rows relative to the tile origin
+    float ac;                // amp / (lambda z)
     int32_t pad[3];
 };
 static_assert(sizeof(FrSRec) == 64, "FrSRec size");
+static_assert(offsetof(FrSRec, xl) % 16 == 0, "xl..yh are read as one int4");
 
 constexpr float kTwoPi = 6.283185307179586f;
 // FAST class: column and row phases stay within this many turns over the

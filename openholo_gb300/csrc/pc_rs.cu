@@ -61,28 +61,6 @@ constexpr float kPi = 3.14159265358979f;
 // 2.26e12, 4 2.15e12; the block issue rate, not the MUFU, binds beyond two.
 constexpr unsigned kPolyMask = 0x8001u;
 
-// sin(2 pi t) and cos(2 pi t) for t in [-0.5, 0.5]: sin = t S(t^2) (degree 5
-// in t^2), cos = C(t^2) (degree 6), least-squares fits on Chebyshev nodes of
-// [0, 0.5] made for this kernel; evaluated with FMA in FP32 the error is
-// below 4e-7 (sin) and 6e-7 (cos) absolute, as good as the MUFU's.
-__device__ __forceinline__ void sincos_turns_poly(float t, float* s, float* c) {
-    const float u = t * t;
-    float ps = -1.230215740e+01f;
-    ps = fmaf(ps, u, 4.122758102e+01f);
-    ps = fmaf(ps, u, -7.658597565e+01f);
-    ps = fmaf(ps, u, 8.159687805e+01f);
-    ps = fmaf(ps, u, -4.134145737e+01f);
-    ps = fmaf(ps, u, 6.283183575e+00f);
-    float pc = 6.547553062e+00f;
-    pc = fmaf(pc, u, -2.598241234e+01f);
-    pc = fmaf(pc, u, 6.017204666e+01f);
-    pc = fmaf(pc, u, -8.545075989e+01f);
-    pc = fmaf(pc, u, 6.493915558e+01f);
-    pc = fmaf(pc, u, -1.973920631e+01f);
-    pc = fmaf(pc, u, 1.0f);
-    *s = ps * t;
-    *c = pc;
-}
 
 __device__ __forceinline__ int warp_prefix(unsigned ballot) {
     return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
