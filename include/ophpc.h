@@ -115,6 +115,12 @@ const char* ophpc_last_error(const ophpc_context* ctx);
 ophpc_status ophpc_create(int32_t device, ophpc_context** out);
 ophpc_status ophpc_destroy(ophpc_context* ctx);
 
+/* Device buffers passed to this library: complex fields (d_field,
+ * [re, im] pairs) must be 16-byte aligned and vertex and encoded buffers
+ * 8-byte aligned, as cudaMalloc and PyTorch allocations are; a buffer that
+ * is not is rejected with OPHPC_ERROR_INVALID_ARGUMENT before any work is
+ * queued. */
+
 /* Device path of generateHologram: d_vertices holds n_points ophpc_vertex
  * records in device memory; d_field receives the complex field of every
  * channel as interleaved doubles [n_channels][pnY][pnX][re, im] (the

@@ -16,6 +16,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -153,6 +154,10 @@ void choose_split(JobGeom& jg, int slots) {
     jg.points_per_split = std::max<int64_t>(kChunk, ((per + kChunk - 1) / kChunk) * kChunk);
 }
 
+// The kernels read and write the complex field as double2 (16-byte) words and
+// the vertices / encoded values as doubles.
+bool aligned(const void* p, uintptr_t bytes) { return ((uintptr_t)p & (bytes - 1)) == 0; }
+
 bool is_device_ptr(const void* p) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
@@ -248,6 +253,8 @@ ophpc_status generate_accumulate(ophpc_context* ctx, const ophpc_config* cfg, co
     if (!d_field || !is_device_ptr(d_field)) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_dst must be device memory");
     if (n_points > 0 && (!d_vertices || !is_device_ptr(d_vertices)))
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "vertices must be device memory");
+    if (!aligned(d_field, 16) || !aligned(d_vertices, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_dst must be 16-byte and vertices 8-byte aligned");
     return generate_device(ctx, cfg, d_vertices, n_points, diff_flag, 0, d_field, s, color_offset, true);
 }
 
@@ -356,6 +363,8 @@ ophpc_status ophpc_generate(ophpc_context* ctx, const ophpc_config* cfg, const o
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be device memory");
     if (n_points > 0 && (!d_vertices || !is_device_ptr(d_vertices)))
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_vertices must be device memory");
+    if (!aligned(d_field, 16) || !aligned(d_vertices, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_vertices 8-byte aligned");
     return generate_device(ctx, cfg, d_vertices, n_points, diff_flag, mode, d_field, (cudaStream_t)stream);
 }
 
@@ -422,6 +431,8 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded must be device memory");
     if (d_normalized && !is_device_ptr(d_normalized))
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_normalized must be device memory");
+    if (!aligned(d_field, 16) || !aligned(d_encoded, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_encoded 8-byte aligned");
     cudaStream_t s = (cudaStream_t)stream;
     unsigned long long* d_mm = nullptr;
     cudaError_t e = pool_alloc(ctx, &d_mm, 8 * sizeof(unsigned long long), s);
@@ -459,6 +470,7 @@ ophpc_status ophpc_normalize(ophpc_context* ctx, const double* d_encoded, uint32
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded must be device memory");
     if (!d_normalized || !is_device_ptr(d_normalized))
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_normalized must be device memory");
+    if (!aligned(d_encoded, 8)) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded must be 8-byte aligned");
     cudaStream_t s = (cudaStream_t)stream;
     unsigned long long* d_mm = nullptr;
     cudaError_t e = pool_alloc(ctx, &d_mm, 2 * sizeof(unsigned long long), s);

@@ -18,6 +18,8 @@
 #include "ophpc.h"
 #include "pc_common.cuh"
 
+#include <cstdint>
+
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -130,6 +132,8 @@ extern "C" ophpc_status ophpc_generate_static_scratch(const ophpc_config* cfg, c
     if (n_points > (uint64_t)OPHPC_STATIC_SCRATCH_RECORDS / cfg->n_channels) return OPHPC_ERROR_INVALID_ARGUMENT;
     if (!d_field || !on_device(d_field)) return OPHPC_ERROR_INVALID_ARGUMENT;
     if (n_points > 0 && (!d_vertices || !on_device(d_vertices))) return OPHPC_ERROR_INVALID_ARGUMENT;
+    // the kernels move the field as 16-byte double2 words and read vertices as doubles
+    if (((uintptr_t)d_field & 15) != 0 || ((uintptr_t)d_vertices & 7) != 0) return OPHPC_ERROR_INVALID_ARGUMENT;
     void* scratch = nullptr;
     if (scratch_on_current_device(&scratch) != cudaSuccess) return OPHPC_ERROR_CUDA;
     cudaStream_t s = (cudaStream_t)stream;

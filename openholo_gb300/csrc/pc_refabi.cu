@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -123,7 +124,8 @@ void sum_Kernel(const int&, const int&, double* dst, double* src, int size) {
         t_last = OPHPC_SUCCESS;
         return;
     }
-    if (!dst || !src) return report("sum_Kernel", OPHPC_ERROR_INVALID_ARGUMENT, nullptr);
+    if (!dst || !src || ((uintptr_t)dst & 15) != 0 || ((uintptr_t)src & 15) != 0)
+        return report("sum_Kernel", OPHPC_ERROR_INVALID_ARGUMENT, nullptr);   // cuDoubleComplex is 16-byte aligned
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

@@ -151,3 +151,28 @@ def test_deterministic(gpu_ctx):
         a = run_generate(gpu_ctx, gk, v, diff)
         b = run_generate(gpu_ctx, gk, v, diff)
         assert np.array_equal(a, b)
+
+
+def test_misaligned_buffers_are_rejected(gpu_ctx):
+    """A field that is not 16-byte aligned (or vertices / encoded values not
+    8-byte aligned) is refused before anything is launched."""
+    import torch
+
+    import openholo_gb300 as oph
+    cfg = oph.make_config(64, 48, 8e-6, 8e-6, [532e-9])
+    v = torch.zeros((8 * 7 + 1,), dtype=torch.float64, device="cuda")
+    v[3 + 1] = 1.0
+    f = torch.zeros((64 * 48 * 2 + 2,), dtype=torch.float64, device="cuda")
+    s = torch.cuda.current_stream().cuda_stream
+    with pytest.raises(oph.OphpcError):
+        gpu_ctx.generate(cfg, v.data_ptr(), 8, 0, 0, f.data_ptr() + 8, s)       # field 8 bytes off
+    with pytest.raises(oph.OphpcError):
+        gpu_ctx.generate(cfg, v.data_ptr() + 4, 8, 0, 0, f.data_ptr(), s)       # vertices 4 bytes off
+    e = torch.zeros((64 * 48 + 1,), dtype=torch.float64, device="cuda")
+    with pytest.raises(oph.OphpcError):
+        gpu_ctx.encode(f.data_ptr() + 8, 1, 64 * 48, 0, e.data_ptr(), None, s)
+    with pytest.raises(oph.OphpcError):
+        gpu_ctx.encode(f.data_ptr(), 1, 64 * 48, 0, e.data_ptr() + 4, None, s)
+    gpu_ctx.generate(cfg, v.data_ptr(), 8, 0, 0, f.data_ptr(), s)              # aligned: fine
+    torch.cuda.synchronize()
+    assert torch.isfinite(f).all()
