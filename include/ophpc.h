@@ -59,7 +59,12 @@ typedef enum ophpc_status {
 #define OPHPC_MODE_FASTMATH 4u
 /* GB300 additions (no reference counterpart): Fresnel as a separable complex
  * contraction on the tcgen05 tensor cores, FP16 operands or split-BF16
- * (hi/lo, three products), FP32 accumulation. Ignored for RS. */
+ * (hi/lo, three products), FP32 accumulation. With PC_DIFF_RS,
+ * OPHPC_MODE_TENSOR_BF16X3 runs RS on the tensor cores too: per 128x128
+ * pixel tile a row-factor x column-factor expansion plus a first-order
+ * cross pair, split-BF16 (cross pair FP16), with the pairs the expansion
+ * does not hold for added by the FP32-core RS kernel; OPHPC_MODE_TENSOR_FP16
+ * is ignored for RS. */
 #define OPHPC_MODE_TENSOR_FP16 0x100u
 #define OPHPC_MODE_TENSOR_BF16X3 0x200u
 

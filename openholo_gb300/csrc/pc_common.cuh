@@ -57,7 +57,14 @@ struct JobGeom {
     // overwriting it (a job computed as several point-range launches).
     int64_t p0, p1;
     int32_t accumulate;
-    int32_t pad;
+    // RS only, set for the CUDA-core complement of the tensor-core RS
+    // kernel: skip the (point, tile) pairs that kernel evaluated
+    // (rs_tc_eligible on the enclosing 128x128 tile). tc_left[ch][ty][tx]
+    // counts, per 128x128 tile, the pairs left to the CUDA cores; tiles with
+    // none are skipped whole.
+    int32_t tc_skip;
+    const int32_t* tc_left;
+    int32_t tc_tiles_x, tc_tiles_y;
 };
 
 // Pixel-centre coordinates, exactly as the reference forms them

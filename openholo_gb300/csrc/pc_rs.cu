@@ -28,6 +28,7 @@
 // the exact r_p. Sums run in FP32 per chunk and are folded into FP64
 // shared-memory sums after every chunk; every pixel is stored once.
 #include "pc_common.cuh"
+#include "pc_tcrs.cuh"
 
 namespace ophpc {
 
@@ -79,6 +80,12 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
     const int part = blockIdx.z % jg.ksplit;
     const ChannelGeom& g = jg.ch[ch];
     const int X0 = blockIdx.x * kTileW, Y0 = blockIdx.y * kTileH;
+    // complement of the tensor-core RS kernel: the enclosing 128x128 tile,
+    // skipped whole when that kernel left none of its pairs
+    const int tcX0 = X0 / kRsTcTile * kRsTcTile, tcY0 = Y0 / kRsTcTile * kRsTcTile;
+    if (jg.tc_skip &&
+        jg.tc_left[((int64_t)ch * jg.tc_tiles_y + tcY0 / kRsTcTile) * jg.tc_tiles_x + tcX0 / kRsTcTile] == 0)
+        return;
     const int vx1 = min(X0 + kTileW, g.pnX), vy1 = min(Y0 + kTileH, g.pnY);
     const int xc = X0 + kTileW / 2, yc = Y0 + kTileH / 2;
     const double Xc = pixel_x(g, xc), Yc = pixel_y(g, yc);
@@ -125,7 +132,8 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                 const PointRec p = chrec[idx];
                 const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
                 const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
-                if (ix0 < ix1 && iy0 < iy1) {
+                float wxm_t, wym_t;
+                if (ix0 < ix1 && iy0 < iy1 && !(jg.tc_skip && rs_tc_eligible(p, g, tcX0, tcY0, &wxm_t, &wym_t))) {
                     // FP64: only frac(r_c / lambda). sqrt from an FP32 seed
                     // refined by two Newton steps (relative error < 1e-20).
                     const double dxc = Xc - p.x, dyc = Yc - p.y;

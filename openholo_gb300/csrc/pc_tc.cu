@@ -33,6 +33,7 @@
 #include "pc_tc.cuh"
 
 #include "pc_common.cuh"
+#include "pc_tcgen05.cuh"
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -46,6 +47,8 @@
 namespace ophpc {
 namespace {
 
+using namespace tc5;
+
 constexpr int kBM = 128;            // SLM rows per tile = TMEM lanes
 constexpr int kBN = 128;            // SLM columns per tile
 constexpr int kBK = 64;             // points per k-block: one 128-byte swizzle row of 16-bit values
@@ -55,7 +58,7 @@ constexpr int kStageBytes = 4 * kTileBytes;         // Ar, Ai, Br, Bi
 constexpr int kAccCols = 2 * kBN;                   // one accumulator buffer: D_re [0,128), D_im [128,256)
 constexpr int kTmemCols = 2 * kAccCols;             // two buffers (all 512 TMEM columns)
 constexpr int kEpiWarps = 8;                        // 2 per TMEM lane group, each half of the columns
-constexpr int kEpiCols = kBN / (kEpiWarps / 4);     // 32 columns of D_re and of D_im per epilogue thread
+constexpr int kEpiCols = kBN / (kEpiWarps / 4);     // 64 columns of D_re and of D_im per epilogue thread
 constexpr int kGemmThreads = 64 + 32 * kEpiWarps;   // warp 0 TMA, warp 1 MMA + TMEM, warps 2-9 epilogue
 static_assert(kEpiCols % 16 == 0, "16-column TMEM loads");
 static_assert(2 * kBM * (kBN + 1) * 4 <= kStages * kStageBytes, "epilogue staging fits in the stage ring");
@@ -68,112 +71,10 @@ constexpr int kTablePoints = 128;                   // points per table-kernel b
 constexpr uint64_t kWaitLimitNs = 10ull * 1000 * 1000 * 1000;   // 10 s per wait
 constexpr size_t kGemmSmem = (size_t)kStages * kStageBytes + 1024 + 256;
 
-// ------------------------------------------------------------------ PTX
 
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait. Returns false when the deadline passed or another role
-// raised the CTA's abort flag.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort, uint64_t deadline) {
-    while (!mbar_try_wait(bar, parity)) {
-        if (*abort) return false;
-        if (global_ns() > deadline) {
-            *abort = 1;
-            return false;
-        }
-    }
-    return true;
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-            "r"(smem_u32(dst)),
-        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tmem_alloc(uint32_t* result_smem, uint32_t ncols) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(result_smem)),
-                 "r"(ncols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void umma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-            d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
-        : "memory");
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-// 32 lanes x 16 consecutive 32-bit columns, added into acc[0..15].
-__device__ __forceinline__ void tmem_ld16_add(uint32_t taddr, float* acc) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) acc[i] += __uint_as_float(r[i]);
-}
-
-// Shared-memory matrix descriptor (tcgen05): K-major operand, 128-byte
-// swizzle, rows of 128 bytes, 8-row core groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t smem_addr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((smem_addr & 0x3FFFF) >> 4);   // start address, 16-byte units
-    d |= (uint64_t)1 << 16;                        // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;              // stride byte offset: 8 rows x 128 B
-    d |= (uint64_t)1 << 46;                        // descriptor version for sm_100 family
-    d |= (uint64_t)2 << 61;                        // layout: 128-byte swizzle
-    return d;
-}
-
-// Instruction descriptor, kind::f16: FP32 accumulate, A and B of one type
-// (0 = FP16, 1 = BF16), both K-major, M = 128, N = kBN.
+// Instruction descriptor of this kernel's MMAs: M = 128, N = kBN.
 __host__ __device__ constexpr uint32_t make_idesc(uint32_t ab_format, bool negate_a) {
-    return (1u << 4)                       // D format: F32
-           | (ab_format << 7)              // A format
-           | (ab_format << 10)             // B format
-           | ((negate_a ? 1u : 0u) << 13)  // negate A
-           | ((uint32_t)(kBN >> 3) << 17)  // N / 8
-           | ((uint32_t)(kBM >> 4) << 24); // M / 16
+    return idesc_f16(ab_format, negate_a, kBM, kBN);
 }
 
 // ------------------------------------------------------------------ tables

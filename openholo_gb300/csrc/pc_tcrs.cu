@@ -1,0 +1,522 @@
+// Tensor-core Rayleigh-Sommerfeld (tcgen05, sm_103a).
+//
+// The reference's RS sum (ophgen/src/ophGen.cpp:361-445)
+//   H(p) = sum_j coef_j / r_pj^2 * (sin(k r_pj), -cos(k r_pj)),  coef = a z / lambda,
+// is not separable over the whole SLM, but it is over one 128x128 pixel
+// tile. With the tile centre (Xc, Yc), dx = Xc - x_j, dy = Yc - y_j,
+// r_c^2 = dx^2 + dy^2 + z^2 and pixel offsets u = X - Xc, v = Y - Yc:
+//   r_p^2 = r_c^2 (1 + w_x + w_y),  w_x = (2 dx u + u^2) / r_c^2,  w_y = (2 dy v + v^2) / r_c^2
+//   r_p / lambda = tau + tau S(w_x) + tau S(w_y) - tau w_x w_y / 4 + O(tau w^3 cross, tau w^4)
+//   S(w) = w/2 - w^2/8 + w^3/16,  tau = r_c / lambda
+//   1 / r_p^2 = (1 / r_c^2)(1 - w_x + w_x^2)(1 - w_y + w_y^2) (1 + O(w_x w_y))
+// so that, with theta = -(pi/2) tau w_x w_y and e^{i theta} ~ 1 + i theta,
+//   coef / r_p^2 e^{i 2 pi r_p / lambda} ~ R_j(v) C_j(u) + [i k_j w_y R_j(v)] [w_x C_j(u) / wxm_j]
+//   R_j(v) = (coef / r_c^2) (1 - w_y + w_y^2) e^{i 2 pi (frac(tau) + tau S(w_y))}
+//   C_j(u) = (1 - w_x + w_x^2) e^{i 2 pi tau S(w_x)},    k_j = -(pi/2) tau wxm_j
+// a complex rank-2 update per point. The tile's field is then the complex
+// contraction D = sum_j A_j B_j^T over the points, run on the tensor cores:
+//
+//   warps 0-7   producers: per (point, tile) record in FP64 (frac(tau) is the
+//               only FP64 step; k r reaches ~6e6 rad), then per stage of 16
+//               points warps 0-3 write the row factors A (128 rows) and
+//               warps 4-7 the column factors B (128 columns) into shared
+//               memory in the UMMA K-major 32-byte-swizzle layout:
+//               split-BF16 (hi + lo) for R and C, FP16 for the cross pair;
+//   warp 8      allocates 512 TMEM columns; one thread issues per stage
+//               eight tcgen05.mma kind::f16, M=128, N=256, K=16: the N=256
+//               B operand [Br; Bi] (or [-Bi; Br]) yields D_re and D_im of
+//               one product at once; passes (hi,hi), (hi,lo), (lo,hi) in
+//               BF16 and the cross pair in FP16;
+//   warps 0-7   also drain the TMEM accumulators: every 64 stages (1024
+//               points; the tensor core's FP32 accumulation loses ~1e-8 of
+//               the sum per point) into FP32 registers, double-buffered, and
+//               every 16 drains into the FP64 field.
+//
+// Pairs for which the expansion does not hold (window cuts the tile, the cone
+// test is not passed by the whole tile, |w| or the cross phase too large:
+// rs_tc_eligible) get zero factors here and are added afterwards by the
+// CUDA-core rs_kernel, which skips exactly the pairs this kernel took.
+//
+// Every mbarrier wait is bounded (%globaltimer); on a timeout the CTA raises
+// an error word, waits (bounded) for its issued MMAs, frees TMEM and returns.
+#include "pc_tcrs.cuh"
+
+#include "pc_tcgen05.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+namespace ophpc {
+namespace {
+
+using namespace tc5;
+
+constexpr int kProducerWarps = 8;
+constexpr int kProducers = 32 * kProducerWarps;          // 256
+constexpr int kThreadsTc = kProducers;                   // warp 0 also issues the MMAs
+constexpr int kStagePts = 16;                            // points per stage: one K=16 MMA step
+constexpr int kStagesTc = 3;
+constexpr int kPlane = kRsTcTile * kStagePts * 2;        // 4096 B: 128 rows x 32 B
+// planes of one stage (kB?n: the negated imaginary plane, so that [Bn; Br]
+// and [Br; Bi] are both contiguous N=256 operands)
+enum : int { kAhr = 0, kAhi, kAlr, kAli, kA2r, kA2i, kBhn, kBhr, kBhi, kBln, kBlr, kBli, kB2n, kB2r, kB2i, kPlanes };
+constexpr int kStageBytesTc = kPlanes * kPlane;          // 61,440
+constexpr int kChunkTc = kProducers;                     // points per record round
+constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 16
+constexpr int kPeriod = 64;                              // stages per TMEM accumulation run
+constexpr int kFlushPeriods = 16;                        // drains kept in FP32 before an FP64 flush
+constexpr int kAccColsTc = 2 * kRsTcTile;                // one buffer: D_re [0,128), D_im [128,256)
+constexpr int kTmemColsTc = 2 * kAccColsTc;              // two buffers: all 512 columns
+constexpr int kEpiColsTc = kRsTcTile / 2;                // 64 columns of D_re and of D_im per thread
+constexpr uint64_t kWaitNs = 10ull * 1000 * 1000 * 1000; // 10 s per wait
+constexpr float kCrossScale = 64.f;                      // moves the cross pair into FP16's normal range
+constexpr float kTwoPiF = 6.283185307179586f;
+
+struct __align__(16) TcRsRec {
+    float P, Q, h, tau;    // 2 dx / rc^2, 2 dy / rc^2, 1 / rc^2, rc / lambda
+    float fc, ac, k2, bx;  // frac(rc / lambda), coef / (rc^2 amax) (0: pair not taken), k * 64, 1 / (64 wxm)
+};
+static_assert(sizeof(TcRsRec) == 32, "TcRsRec size");
+
+constexpr size_t kSmemTc = 1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsRec) * kChunkTc + 256;
+static_assert(kSmemTc <= 232448, "shared memory per CTA");
+
+struct TcRsArgs {
+    JobGeom jg;
+    const PointRec* recs;   // [n_channels][n_points]
+    double2* field;         // [n_channels][pnY][pnX], overwritten
+    const float* amax;      // [n_channels]: max coef / z^2
+    int32_t* left;          // [n_channels][tiles_y][tiles_x]: pairs left to the CUDA cores
+    int* error;
+    int32_t tiles_x, tiles_y;
+};
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory"); }
+__device__ __forceinline__ void st_v4(uint32_t addr, const uint32_t* w) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3])
+                 : "memory");
+}
+__device__ __forceinline__ uint32_t bf2(float lo, float hi) {
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ float2 unbf2(uint32_t w) {
+    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
+}
+__device__ __forceinline__ uint32_t h2(float lo, float hi) {
+    const __half2 v = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+__device__ __forceinline__ float reduce_turns_f(float t) {
+    const float m = 12582912.0f;   // 1.5 * 2^23: round to nearest integer
+    return __fsub_rn(t, __fsub_rn(__fadd_rn(t, m), m));
+}
+
+// Adds TMEM accumulator buffer p&1 (this warp's 32 lanes, 64 columns of
+// D_re and of D_im) into acc_re / acc_im and hands the buffer back to the
+// MMA issuer. Warp-collective; false when the CTA is aborting.
+__device__ __forceinline__ bool drain_period(int p, uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
+                                             uint32_t tmem, int grp, int half, int lane, float (&acc_re)[kEpiColsTc],
+                                             float (&acc_im)[kEpiColsTc]) {
+    const int b = p & 1;
+    bool ok = mbar_wait(&acc_full[b], (uint32_t)(p >> 1) & 1u, abort, global_ns() + kWaitNs);
+    tc_fence_after();
+    ok = __all_sync(0xffffffffu, ok && !*abort);
+    if (!ok) return false;
+    const uint32_t col = tmem + ((uint32_t)(grp * 32) << 16) + (uint32_t)(b * kAccColsTc + half * kEpiColsTc);
+#pragma unroll
+    for (int c = 0; c < kEpiColsTc; c += 16) {
+        tmem_ld16_add(col + (uint32_t)c, &acc_re[c]);
+        tmem_ld16_add(col + (uint32_t)(kRsTcTile + c), &acc_im[c]);
+    }
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&acc_empty[b]);
+    return true;
+}
+
+// field (+)= amax * (-i) D over this thread's row and 64 columns, then
+// clears the FP32 sums.
+__device__ __forceinline__ void flush_field(const TcRsArgs& a, int ch, int X0, int Y0, int grp, int half, int lane,
+                                            float amax, bool add, float (&acc_re)[kEpiColsTc],
+                                            float (&acc_im)[kEpiColsTc]) {
+    const ChannelGeom& g = a.jg.ch[ch];
+    const int row = Y0 + grp * 32 + lane;
+    if (row < g.pnY) {
+        double2* dst = a.field + ((int64_t)ch * g.pnY + row) * g.pnX;
+#pragma unroll
+        for (int i = 0; i < kEpiColsTc; ++i) {
+            const int col = X0 + half * kEpiColsTc + i;
+            if (col < g.pnX) {
+                const double re = (double)acc_im[i] * (double)amax, im = -(double)acc_re[i] * (double)amax;
+                if (add) {
+                    const double2 o = dst[col];
+                    dst[col] = make_double2(o.x + re, o.y + im);
+                } else {
+                    dst[col] = make_double2(re, im);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < kEpiColsTc; ++i) acc_re[i] = acc_im[i] = 0.f;
+}
+
+// Issues the eight MMAs of stage k (warp 0, lane 0 only): waits until the
+// producers filled the stage and, when k opens an accumulation run, until
+// the run two back was drained from the same TMEM buffer. False on abort.
+__device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* full, uint64_t* empty,
+                                            uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
+                                            uint32_t tmem) {
+    constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);
+    constexpr uint32_t id_h = idesc_f16(0u, false, kRsTcTile, 2 * kRsTcTile);
+    const int p = k / kPeriod, b = p & 1;
+    const bool opens = (k % kPeriod) == 0;
+    if (opens && p >= 2 && !mbar_wait(&acc_empty[b], (uint32_t)((p / 2) - 1) & 1u, abort, global_ns() + kWaitNs))
+        return false;
+    const int s = k % kStagesTc;
+    if (!mbar_wait(&full[s], (uint32_t)(k / kStagesTc) & 1u, abort, global_ns() + kWaitNs)) return false;
+    tc_fence_after();
+    const uint32_t d = tmem + (uint32_t)(b * kAccColsTc);
+    const uint32_t st = smem_u32(base + s * kStageBytesTc);
+#define PL(x) sw32_desc(st + (uint32_t)((x) * kPlane))
+    umma(d, PL(kAhr), PL(kBhr), id_bf, opens ? 0u : 1u);   // Ar [Br; Bi]
+    umma(d, PL(kAhi), PL(kBhn), id_bf, 1u);                // Ai [-Bi; Br]
+    umma(d, PL(kAhr), PL(kBlr), id_bf, 1u);
+    umma(d, PL(kAhi), PL(kBln), id_bf, 1u);
+    umma(d, PL(kAlr), PL(kBhr), id_bf, 1u);
+    umma(d, PL(kAli), PL(kBhn), id_bf, 1u);
+    umma(d, PL(kA2r), PL(kB2r), id_h, 1u);
+    umma(d, PL(kA2i), PL(kB2n), id_h, 1u);
+#undef PL
+    umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
+    if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(&acc_full[b]);
+    return true;
+}
+
+// One CTA per 128x128 tile of one channel; 8 warps, all producers and
+// drains, warp 0 also allocates TMEM and (lane 0) issues each stage's MMAs
+// one stage after producing it. Eight warps keep two per SM sub-partition,
+// so a thread can hold the 128 FP32 sums of its drain share in registers.
+__global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    TcRsRec* s_rec = reinterpret_cast<TcRsRec*>(base + kStagesTc * kStageBytesTc);
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
+    uint64_t* empty = full + kStagesTc;
+    uint64_t* acc_full = empty + kStagesTc;   // [2]: MMA -> drain, buffer ready
+    uint64_t* acc_empty = acc_full + 2;       // [2]: drain -> MMA, buffer free
+    uint64_t* drain_bar = acc_empty + 2;      // abort path: issued MMAs complete
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain_bar + 1);
+    volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int ch = blockIdx.z;
+    const ChannelGeom& g = a.jg.ch[ch];
+    const int X0 = blockIdx.x * kRsTcTile, Y0 = blockIdx.y * kRsTcTile;
+    const int64_t n = a.jg.n_points;
+    const int total = (int)((n + kStagePts - 1) / kStagePts);
+    const int nchunks = (int)((n + kChunkTc - 1) / kChunkTc);
+    const int periods = (total + kPeriod - 1) / kPeriod;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStagesTc; ++s) {
+            mbar_init(&full[s], kProducerWarps);
+            mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], kProducerWarps);
+        }
+        mbar_init(drain_bar, 1);
+        *abort = 0;
+        *s_left = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, kTmemColsTc);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int t = threadIdx.x;                 // 0..255
+    const bool side_a = warp < 4;              // rows (A) or columns (B)
+    const int rc = (warp & 3) * 32 + lane;     // row m or column n of the tile
+    const float off = side_a ? (float)((double)(kRsTcHalf - rc) * g.ppY) : (float)((double)(rc - kRsTcHalf) * g.ppX);
+    const float off2 = off * off;
+    const uint32_t swz = (uint32_t)((rc >> 2) & 1);   // 32-byte swizzle: rows 4-7 of 8 swap halves
+    const uint32_t row_off0 = (uint32_t)rc * 32u + (swz << 4), row_off1 = (uint32_t)rc * 32u + ((1u ^ swz) << 4);
+    const int grp = warp & 3, half = warp >> 2;       // drain: TMEM lanes 32*grp.., columns half*64..
+    const int vx1 = min(X0 + kRsTcTile, g.pnX), vy1 = min(Y0 + kRsTcTile, g.pnY);
+    const double Xc = pixel_x(g, X0 + kRsTcHalf), Yc = pixel_y(g, Y0 + kRsTcHalf);
+    const float amax = a.amax[ch];
+    const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
+    const PointRec* chrec = a.recs + (int64_t)ch * n;
+    float acc_re[kEpiColsTc], acc_im[kEpiColsTc];
+#pragma unroll
+    for (int i = 0; i < kEpiColsTc; ++i) acc_re[i] = acc_im[i] = 0.f;
+    bool dead = false;
+    bool wrote = a.jg.accumulate != 0;
+    int left = 0, drained = 0, pending = 0, issued = 0;
+
+    for (int c = 0; c < nchunks; ++c) {
+        producers_sync();   // the previous chunk's records are no longer read
+        {
+            TcRsRec r;
+            r.P = r.Q = r.h = r.tau = r.fc = r.ac = r.k2 = r.bx = 0.f;
+            const int64_t idx = (int64_t)c * kChunkTc + t;
+            if (!dead && idx < n) {
+                const PointRec p = chrec[idx];
+                const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
+                const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
+                float wxm, wym;
+                if (ix0 < ix1 && iy0 < iy1) {
+                    if (rs_tc_eligible(p, g, X0, Y0, &wxm, &wym)) {
+                        // FP64: frac(r_c / lambda) only. sqrt from an FP32
+                        // seed refined by two Newton steps.
+                        const double dxc = Xc - p.x, dyc = Yc - p.y;
+                        const double rc2 = fma(dxc, dxc, fma(dyc, dyc, p.aux));
+                        const double y0 = (double)rsqrtf((float)rc2);
+                        const double hy = 0.5 * y0;
+                        double rcd = rc2 * y0;
+                        rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
+                        rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
+                        const double tc = rcd * g.inv_lambda;
+                        const float hf = 1.0f / (float)rc2;
+                        r.P = 2.f * (float)dxc * hf;
+                        r.Q = 2.f * (float)dyc * hf;
+                        r.h = hf;
+                        r.tau = (float)tc;
+                        r.fc = (float)(tc - rint(tc));
+                        r.ac = (float)p.coef * hf * inv_amax;
+                        r.k2 = -1.5707963267948966f * r.tau * wxm * kCrossScale;
+                        r.bx = 1.f / (wxm * kCrossScale);
+                    } else {
+                        ++left;
+                    }
+                }
+            }
+            s_rec[t] = r;
+        }
+        producers_sync();
+        const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
+        for (int it = it0; it < it1; ++it) {
+            // drain the previous run once two stages of this one are queued
+            if (!dead && (it % kPeriod) == 2 && it >= kPeriod) {
+                dead = !drain_period(drained, acc_full, acc_empty, abort, tmem, grp, half, lane, acc_re, acc_im);
+                ++drained;
+                if (!dead && ++pending == kFlushPeriods) {
+                    flush_field(a, ch, X0, Y0, grp, half, lane, amax, wrote, acc_re, acc_im);
+                    wrote = true;
+                    pending = 0;
+                }
+            }
+            const int s = it % kStagesTc;
+            if (!dead) {
+                const bool ok =
+                    mbar_wait(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, global_ns() + kWaitNs);
+                dead = !__all_sync(0xffffffffu, ok);
+            }
+            if (dead) continue;
+            const uint32_t st = smem_u32(base + s * kStageBytesTc);
+            const int j0 = (it - it0) * kStagePts;
+#pragma unroll 1
+            for (int h8 = 0; h8 < 2; ++h8) {
+                uint32_t w_hr[4], w_hi[4], w_lr[4], w_li[4], w_xr[4], w_xi[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float vr[2], vi[2], xr[2], xi[2];
+#pragma unroll
+                    for (int e = 0; e < 2; ++e) {
+                        const TcRsRec& r = s_rec[j0 + h8 * 8 + q * 2 + e];
+                        const float4 r0 = *reinterpret_cast<const float4*>(&r.P);
+                        const float4 r1 = *reinterpret_cast<const float4*>(&r.fc);
+                        const float w = fmaf(side_a ? r0.y : r0.x, off, r0.z * off2);
+                        const float s3 = fmaf(w, fmaf(w, 0.0625f, -0.125f), 0.5f);   // S(w) / w
+                        float ph = (r0.w * w) * s3;                                  // turns
+                        if (side_a) ph += r1.x;
+                        ph = reduce_turns_f(ph);
+                        float sn, cs;
+                        __sincosf(ph * kTwoPiF, &sn, &cs);
+                        float amp = fmaf(w, w, 1.f - w);
+                        if (side_a) amp *= r1.y;
+                        vr[e] = amp * cs;
+                        vi[e] = amp * sn;
+                        if (side_a) {
+                            const float kw = r1.z * w;   // i k w_y R
+                            xr[e] = -kw * vi[e];
+                            xi[e] = kw * vr[e];
+                        } else {
+                            const float sc = w * r1.w;   // w_x C / (64 wxm)
+                            xr[e] = sc * vr[e];
+                            xi[e] = sc * vi[e];
+                        }
+                    }
+                    w_hr[q] = bf2(vr[0], vr[1]);
+                    w_hi[q] = bf2(vi[0], vi[1]);
+                    const float2 hr = unbf2(w_hr[q]), hi = unbf2(w_hi[q]);
+                    w_lr[q] = bf2(vr[0] - hr.x, vr[1] - hr.y);
+                    w_li[q] = bf2(vi[0] - hi.x, vi[1] - hi.y);
+                    w_xr[q] = h2(xr[0], xr[1]);
+                    w_xi[q] = h2(xi[0], xi[1]);
+                }
+                const uint32_t ro = st + (h8 ? row_off1 : row_off0);
+                if (side_a) {
+                    st_v4(ro + kAhr * kPlane, w_hr);
+                    st_v4(ro + kAhi * kPlane, w_hi);
+                    st_v4(ro + kAlr * kPlane, w_lr);
+                    st_v4(ro + kAli * kPlane, w_li);
+                    st_v4(ro + kA2r * kPlane, w_xr);
+                    st_v4(ro + kA2i * kPlane, w_xi);
+                } else {
+                    uint32_t nh[4], nl[4], nx[4];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        nh[q] = w_hi[q] ^ 0x80008000u;   // -Bi: flip both sign bits
+                        nl[q] = w_li[q] ^ 0x80008000u;
+                        nx[q] = w_xi[q] ^ 0x80008000u;
+                    }
+                    st_v4(ro + kBhn * kPlane, nh);
+                    st_v4(ro + kBhr * kPlane, w_hr);
+                    st_v4(ro + kBhi * kPlane, w_hi);
+                    st_v4(ro + kBln * kPlane, nl);
+                    st_v4(ro + kBlr * kPlane, w_lr);
+                    st_v4(ro + kBli * kPlane, w_li);
+                    st_v4(ro + kB2n * kPlane, nx);
+                    st_v4(ro + kB2r * kPlane, w_xr);
+                    st_v4(ro + kB2i * kPlane, w_xi);
+                }
+            }
+            fence_async_smem();   // generic-proxy writes -> visible to the tensor core
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&full[s]);
+            // warp 0 issues the previous stage's MMAs (one stage of slack for
+            // the other warps to fill it)
+            if (warp == 0 && it > 0) {
+                bool ok = true;
+                if (lane == 0) ok = issue_stage(it - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (ok) issued = it;
+                else dead = true;
+            }
+        }
+    }
+    if (warp == 0 && !dead && total > 0) {
+        bool ok = true;
+        if (lane == 0) ok = issue_stage(total - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (ok) issued = total;
+        else dead = true;
+    }
+    // the runs not drained yet, then the last flush
+    for (int p = drained; p < periods && !dead; ++p)
+        dead = !drain_period(p, acc_full, acc_empty, abort, tmem, grp, half, lane, acc_re, acc_im);
+    if (!dead) flush_field(a, ch, X0, Y0, grp, half, lane, amax, wrote, acc_re, acc_im);
+    const int wl = __reduce_add_sync(0xffffffffu, left);
+    if (lane == 0 && wl) atomicAdd(s_left, wl);
+    if (warp == 0 && lane == 0 && issued > 0 && *abort) {
+        // aborted: wait (bounded) for the MMAs already issued before TMEM is released
+        umma_commit(drain_bar);
+        const uint64_t dl = global_ns() + 1000ull * 1000 * 1000;
+        while (!mbar_try_wait(drain_bar, 0) && global_ns() < dl) {
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, kTmemColsTc);
+    if (threadIdx.x == 0) {
+        a.left[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x] = *s_left;
+        if (*abort) atomicExch(a.error, 1);
+    }
+}
+
+// Largest coef / z^2 of a channel: bounds every coef / r_c^2, so the
+// factors stay within [-1, 1] (FP16 range for the cross pair).
+__global__ void rs_amax_kernel(const PointRec* __restrict__ recs, int64_t n, float* out) {
+    float m = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf((float)(recs[i].coef / recs[i].aux)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));   // m >= 0
+}
+
+size_t align_up(size_t v, size_t al) { return (v + al - 1) / al * al; }
+
+}  // namespace
+
+ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
+                            const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, cudaStream_t s,
+                            std::string* err) {
+    auto fail = [&](ophpc_status st, const char* msg) {
+        if (err) *err = msg;
+        return st;
+    };
+    static std::once_flag attr_once;
+    std::call_once(attr_once,
+                   [] { cudaFuncSetAttribute(tc_rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTc); });
+    const int nch = jg.n_channels;
+    const int pnX = cfg->pixel_number[0], pnY = cfg->pixel_number[1];
+    const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
+    const size_t rec_bytes = align_up(sizeof(PointRec) * n_points * nch, 256);
+    const size_t left_bytes = align_up(sizeof(int32_t) * (size_t)nch * tiles_x * tiles_y, 256);
+    unsigned char* buf = nullptr;
+    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + 256, pool, s) != cudaSuccess)
+        return fail(OPHPC_ERROR_OUT_OF_MEMORY, "tensor-core RS scratch allocation failed");
+    PointRec* recs = (PointRec*)buf;
+    int32_t* left = (int32_t*)(buf + rec_bytes);
+    float* amax = (float*)(buf + rec_bytes + left_bytes);   // [3]
+    int* errw = (int*)(amax + 4);
+    cudaMemsetAsync(amax, 0, 32, s);   // amax[0..3] and the error word
+
+    launch_prep(d_vertices, (int64_t)n_points, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window,
+                (int)OPHPC_DIFF_RS, jg, recs, s);
+    for (int c = 0; c < nch; ++c) {
+        count_launches(1);
+        rs_amax_kernel<<<256, 256, 0, s>>>(recs + (int64_t)c * n_points, (int64_t)n_points, amax + c);
+    }
+    TcRsArgs ta;
+    std::memset(&ta, 0, sizeof(ta));
+    ta.jg = jg;
+    ta.jg.accumulate = 0;
+    ta.recs = recs;
+    ta.field = (double2*)d_field;
+    ta.amax = amax;
+    ta.left = left;
+    ta.error = errw;
+    ta.tiles_x = tiles_x;
+    ta.tiles_y = tiles_y;
+    count_launches(1);
+    tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTc, s>>>(ta);
+
+    // the CUDA-core complement: the pairs the tensor-core kernel left
+    JobGeom jc = jg;
+    jc.ksplit = 1;
+    jc.points_per_split = (int64_t)n_points;
+    jc.p0 = 0;
+    jc.p1 = 0;
+    jc.accumulate = 1;
+    jc.tc_skip = 1;
+    jc.tc_left = left;
+    jc.tc_tiles_x = tiles_x;
+    jc.tc_tiles_y = tiles_y;
+    launch_rs(recs, jc, (double2*)d_field, nullptr, s);
+
+    cudaError_t e = cudaGetLastError();
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return fail(OPHPC_ERROR_CUDA, cudaGetErrorString(e));
+    if (herr) return fail(OPHPC_ERROR_TIMEOUT, "tensor-core RS kernel wait timed out");
+    return OPHPC_SUCCESS;
+}
+
+}  // namespace ophpc
