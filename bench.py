@@ -57,7 +57,8 @@ def parse():
     ap.add_argument("--serving-jobs", type=int, default=128, help="jobs in the serving stream (512 = full)")
     ap.add_argument("--profile-case", default=None,
                     help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
-                         "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points)")
+                         "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points), "
+                         "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points)")
     ap.add_argument("--serving-max-points", type=int, default=100_000,
                     help="largest point count of a serving job (500000 = full)")
     return ap.parse_args()
@@ -548,6 +549,8 @@ def profile_case(name: str) -> None:
         w = workloads.box_4k(n_points=131_072)
         diff = 1
         mode = oph.MODE_TENSOR_FP16 if name == "tc_fp16_4k" else oph.MODE_TENSOR_BF16X3
+    elif name == "tcrs_fhd":   # tensor-core RS, sphere_fhd geometry, 20,000 of its points
+        w, diff, mode = workloads.sphere_fhd().subset(20_000), 0, oph.MODE_TENSOR_BF16X3
     else:
         raise SystemExit(f"unknown profile case {name}")
     ctx = oph.Context(0)

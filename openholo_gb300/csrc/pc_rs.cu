@@ -86,6 +86,8 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
     if (jg.tc_skip &&
         jg.tc_left[((int64_t)ch * jg.tc_tiles_y + tcY0 / kRsTcTile) * jg.tc_tiles_x + tcX0 / kRsTcTile] == 0)
         return;
+    RsTcTile tct;
+    if (jg.tc_skip) tct = rs_tc_tile(g, tcX0, tcY0);
     const int vx1 = min(X0 + kTileW, g.pnX), vy1 = min(Y0 + kTileH, g.pnY);
     const int xc = X0 + kTileW / 2, yc = Y0 + kTileH / 2;
     const double Xc = pixel_x(g, xc), Yc = pixel_y(g, yc);
@@ -133,7 +135,7 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                 const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
                 const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
                 float wxm_t, wym_t;
-                if (ix0 < ix1 && iy0 < iy1 && !(jg.tc_skip && rs_tc_eligible(p, g, tcX0, tcY0, &wxm_t, &wym_t))) {
+                if (ix0 < ix1 && iy0 < iy1 && !(jg.tc_skip && rs_tc_eligible(p, tct, &wxm_t, &wym_t))) {
                     // FP64: only frac(r_c / lambda). sqrt from an FP32 seed
                     // refined by two Newton steps (relative error < 1e-20).
                     const double dxc = Xc - p.x, dyc = Yc - p.y;

@@ -55,30 +55,30 @@ namespace {
 
 using namespace tc5;
 
-constexpr int kProducerWarps = 8;
-constexpr int kProducers = 32 * kProducerWarps;          // 256
-constexpr int kThreadsTc = kProducers;                   // warp 0 also issues the MMAs
+constexpr int kWarpsTc = 16;
+constexpr int kThreadsTc = 32 * kWarpsTc;                // 512: producers, drains; warp 0 issues the MMAs
 constexpr int kStagePts = 16;                            // points per stage: one K=16 MMA step
+constexpr int kHalfPts = kStagePts / 2;                  // points per thread per stage (one 16-byte chunk)
 constexpr int kStagesTc = 3;
 constexpr int kPlane = kRsTcTile * kStagePts * 2;        // 4096 B: 128 rows x 32 B
 // planes of one stage (kB?n: the negated imaginary plane, so that [Bn; Br]
 // and [Br; Bi] are both contiguous N=256 operands)
 enum : int { kAhr = 0, kAhi, kAlr, kAli, kA2r, kA2i, kBhn, kBhr, kBhi, kBln, kBlr, kBli, kB2n, kB2r, kB2i, kPlanes };
 constexpr int kStageBytesTc = kPlanes * kPlane;          // 61,440
-constexpr int kChunkTc = kProducers;                     // points per record round
-constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 16
-constexpr int kPeriod = 64;                              // stages per TMEM accumulation run
-constexpr int kFlushPeriods = 16;                        // drains kept in FP32 before an FP64 flush
-constexpr int kAccColsTc = 2 * kRsTcTile;                // one buffer: D_re [0,128), D_im [128,256)
-constexpr int kTmemColsTc = 2 * kAccColsTc;              // two buffers: all 512 columns
-constexpr int kEpiColsTc = kRsTcTile / 2;                // 64 columns of D_re and of D_im per thread
+constexpr int kChunkTc = kThreadsTc;                     // points per record round (one per thread)
+constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 32
+constexpr int kPeriod = 64;                              // stages per TMEM accumulation run (1024 points)
+constexpr int kFlushPeriods = 16;                        // runs summed in TMEM before an FP64 flush
+constexpr int kDCols = 2 * kRsTcTile;                    // accumulator D: re [0,128), im [128,256)
+constexpr int kTmemColsTc = 2 * kDCols;                  // D, then the running sum S
 constexpr uint64_t kWaitNs = 10ull * 1000 * 1000 * 1000; // 10 s per wait
 constexpr float kCrossScale = 64.f;                      // moves the cross pair into FP16's normal range
 constexpr float kTwoPiF = 6.283185307179586f;
 
+// Per (point, tile) record. The column side reads the first four values only.
 struct __align__(16) TcRsRec {
-    float P, Q, h, tau;    // 2 dx / rc^2, 2 dy / rc^2, 1 / rc^2, rc / lambda
-    float fc, ac, k2, bx;  // frac(rc / lambda), coef / (rc^2 amax) (0: pair not taken), k * 64, 1 / (64 wxm)
+    float h, tau, P, bx;   // 1 / rc^2, rc / lambda, 2 dx / rc^2, 1 / (64 wxm)
+    float Q, fc, ac, k2;   // 2 dy / rc^2, frac(rc / lambda), coef / (rc^2 amax) (0: pair not taken), 64 k
 };
 static_assert(sizeof(TcRsRec) == 32, "TcRsRec size");
 
@@ -96,9 +96,9 @@ struct TcRsArgs {
 };
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory"); }
-__device__ __forceinline__ void st_v4(uint32_t addr, const uint32_t* w) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(w[0]), "r"(w[1]), "r"(w[2]), "r"(w[3])
+__device__ __forceinline__ void all_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreadsTc) : "memory"); }
+__device__ __forceinline__ void st_v4(uint32_t addr, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
+    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(w0), "r"(w1), "r"(w2), "r"(w3)
                  : "memory");
 }
 __device__ __forceinline__ uint32_t bf2(float lo, float hi) {
@@ -117,72 +117,94 @@ __device__ __forceinline__ float reduce_turns_f(float t) {
     return __fsub_rn(t, __fsub_rn(__fadd_rn(t, m), m));
 }
 
-// Adds TMEM accumulator buffer p&1 (this warp's 32 lanes, 64 columns of
-// D_re and of D_im) into acc_re / acc_im and hands the buffer back to the
-// MMA issuer. Warp-collective; false when the CTA is aborting.
-__device__ __forceinline__ bool drain_period(int p, uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
-                                             uint32_t tmem, int grp, int half, int lane, float (&acc_re)[kEpiColsTc],
-                                             float (&acc_im)[kEpiColsTc]) {
-    const int b = p & 1;
-    bool ok = mbar_wait(&acc_full[b], (uint32_t)(p >> 1) & 1u, abort, global_ns() + kWaitNs);
-    tc_fence_after();
-    ok = __all_sync(0xffffffffu, ok && !*abort);
-    if (!ok) return false;
-    const uint32_t col = tmem + ((uint32_t)(grp * 32) << 16) + (uint32_t)(b * kAccColsTc + half * kEpiColsTc);
+// Factors of 8 points (recs[0..7]) for this thread's row (SIDE_A) or
+// column, written as one 16-byte chunk of every plane of the stage.
+template <bool SIDE_A>
+__device__ __forceinline__ void produce8(const TcRsRec* recs, float off, float off2, uint32_t ro) {
+    uint32_t w_hr[4], w_hi[4], w_lr[4], w_li[4], w_xr[4], w_xi[4];
 #pragma unroll
-    for (int c = 0; c < kEpiColsTc; c += 16) {
-        tmem_ld16_add(col + (uint32_t)c, &acc_re[c]);
-        tmem_ld16_add(col + (uint32_t)(kRsTcTile + c), &acc_im[c]);
-    }
-    tc_fence_before();
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&acc_empty[b]);
-    return true;
-}
-
-// field (+)= amax * (-i) D over this thread's row and 64 columns, then
-// clears the FP32 sums.
-__device__ __forceinline__ void flush_field(const TcRsArgs& a, int ch, int X0, int Y0, int grp, int half, int lane,
-                                            float amax, bool add, float (&acc_re)[kEpiColsTc],
-                                            float (&acc_im)[kEpiColsTc]) {
-    const ChannelGeom& g = a.jg.ch[ch];
-    const int row = Y0 + grp * 32 + lane;
-    if (row < g.pnY) {
-        double2* dst = a.field + ((int64_t)ch * g.pnY + row) * g.pnX;
+    for (int q = 0; q < 4; ++q) {
+        float vr[2], vi[2], xr[2], xi[2];
 #pragma unroll
-        for (int i = 0; i < kEpiColsTc; ++i) {
-            const int col = X0 + half * kEpiColsTc + i;
-            if (col < g.pnX) {
-                const double re = (double)acc_im[i] * (double)amax, im = -(double)acc_re[i] * (double)amax;
-                if (add) {
-                    const double2 o = dst[col];
-                    dst[col] = make_double2(o.x + re, o.y + im);
-                } else {
-                    dst[col] = make_double2(re, im);
-                }
+        for (int e = 0; e < 2; ++e) {
+            const TcRsRec& r = recs[q * 2 + e];
+            const float4 r0 = *reinterpret_cast<const float4*>(&r.h);   // h, tau, P, bx
+            float w, ph;
+            if (SIDE_A) {
+                const float4 r1 = *reinterpret_cast<const float4*>(&r.Q);   // Q, fc, ac, k2
+                w = fmaf(r1.x, off, r0.x * off2);
+                const float s3 = fmaf(w, fmaf(w, 0.0625f, -0.125f), 0.5f);   // S(w) / w
+                ph = fmaf(r0.y * w, s3, r1.y);                               // turns
+                ph = reduce_turns_f(ph);
+                float sn, cs;
+                __sincosf(ph * kTwoPiF, &sn, &cs);
+                const float amp = r1.z * fmaf(w, w, 1.f - w);
+                vr[e] = amp * cs;
+                vi[e] = amp * sn;
+                const float kw = r1.w * w;   // i k w_y R
+                xr[e] = -kw * vi[e];
+                xi[e] = kw * vr[e];
+            } else {
+                w = fmaf(r0.z, off, r0.x * off2);
+                const float s3 = fmaf(w, fmaf(w, 0.0625f, -0.125f), 0.5f);
+                ph = (r0.y * w) * s3;
+                ph = reduce_turns_f(ph);
+                float sn, cs;
+                __sincosf(ph * kTwoPiF, &sn, &cs);
+                const float amp = fmaf(w, w, 1.f - w);
+                vr[e] = amp * cs;
+                vi[e] = amp * sn;
+                const float sc = w * r0.w;   // w_x C / (64 wxm)
+                xr[e] = sc * vr[e];
+                xi[e] = sc * vi[e];
             }
         }
+        w_hr[q] = bf2(vr[0], vr[1]);
+        w_hi[q] = bf2(vi[0], vi[1]);
+        const float2 hr = unbf2(w_hr[q]), hi = unbf2(w_hi[q]);
+        w_lr[q] = bf2(vr[0] - hr.x, vr[1] - hr.y);
+        w_li[q] = bf2(vi[0] - hi.x, vi[1] - hi.y);
+        w_xr[q] = h2(xr[0], xr[1]);
+        w_xi[q] = h2(xi[0], xi[1]);
     }
-#pragma unroll
-    for (int i = 0; i < kEpiColsTc; ++i) acc_re[i] = acc_im[i] = 0.f;
+#define ST(plane, w) st_v4(ro + (plane) * kPlane, w[0], w[1], w[2], w[3])
+    if (SIDE_A) {
+        ST(kAhr, w_hr);
+        ST(kAhi, w_hi);
+        ST(kAlr, w_lr);
+        ST(kAli, w_li);
+        ST(kA2r, w_xr);
+        ST(kA2i, w_xi);
+    } else {
+        const uint32_t n = 0x80008000u;   // -Bi: flip both sign bits
+        st_v4(ro + kBhn * kPlane, w_hi[0] ^ n, w_hi[1] ^ n, w_hi[2] ^ n, w_hi[3] ^ n);
+        ST(kBhr, w_hr);
+        ST(kBhi, w_hi);
+        st_v4(ro + kBln * kPlane, w_li[0] ^ n, w_li[1] ^ n, w_li[2] ^ n, w_li[3] ^ n);
+        ST(kBlr, w_lr);
+        ST(kBli, w_li);
+        st_v4(ro + kB2n * kPlane, w_xi[0] ^ n, w_xi[1] ^ n, w_xi[2] ^ n, w_xi[3] ^ n);
+        ST(kB2r, w_xr);
+        ST(kB2i, w_xi);
+    }
+#undef ST
 }
 
 // Issues the eight MMAs of stage k (warp 0, lane 0 only): waits until the
-// producers filled the stage and, when k opens an accumulation run, until
-// the run two back was drained from the same TMEM buffer. False on abort.
+// stage is filled and, when k opens an accumulation run, until the previous
+// run was drained out of D. False on abort.
 __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* full, uint64_t* empty,
                                             uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
                                             uint32_t tmem) {
     constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);
     constexpr uint32_t id_h = idesc_f16(0u, false, kRsTcTile, 2 * kRsTcTile);
-    const int p = k / kPeriod, b = p & 1;
+    const int p = k / kPeriod;
     const bool opens = (k % kPeriod) == 0;
-    if (opens && p >= 2 && !mbar_wait(&acc_empty[b], (uint32_t)((p / 2) - 1) & 1u, abort, global_ns() + kWaitNs))
-        return false;
+    if (opens && p >= 1 && !mbar_wait(acc_empty, (uint32_t)(p - 1) & 1u, abort, global_ns() + kWaitNs)) return false;
     const int s = k % kStagesTc;
     if (!mbar_wait(&full[s], (uint32_t)(k / kStagesTc) & 1u, abort, global_ns() + kWaitNs)) return false;
     tc_fence_after();
-    const uint32_t d = tmem + (uint32_t)(b * kAccColsTc);
+    const uint32_t d = tmem;
     const uint32_t st = smem_u32(base + s * kStageBytesTc);
 #define PL(x) sw32_desc(st + (uint32_t)((x) * kPlane))
     umma(d, PL(kAhr), PL(kBhr), id_bf, opens ? 0u : 1u);   // Ar [Br; Bi]
@@ -195,23 +217,93 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
     umma(d, PL(kA2i), PL(kB2n), id_h, 1u);
 #undef PL
     umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
-    if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(&acc_full[b]);
+    if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(acc_full);
     return true;
 }
 
-// One CTA per 128x128 tile of one channel; 8 warps, all producers and
-// drains, warp 0 also allocates TMEM and (lane 0) issues each stage's MMAs
-// one stage after producing it. Eight warps keep two per SM sub-partition,
-// so a thread can hold the 128 FP32 sums of its drain share in registers.
+// Drains run p out of D (warp-collective, every warp): this warp's 32 TMEM
+// lanes x (32 columns of D_re + the 32 of D_im) are added into the running
+// sum S (or replace it when S was just flushed); on a flush run the sum goes
+// into the FP64 field instead. False when the CTA is aborting.
+__device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full, uint64_t* acc_empty,
+                                          volatile int* abort, uint32_t tmem, int warp, int lane,
+                                          const TcRsArgs& a, int ch, int X0, int Y0, float amax, bool& wrote) {
+    bool ok = mbar_wait(acc_full, (uint32_t)p & 1u, abort, global_ns() + kWaitNs);
+    tc_fence_after();
+    ok = __all_sync(0xffffffffu, ok && !*abort);
+    if (!ok) return false;
+    const bool fresh = (p % kFlushPeriods) == 0;                      // S holds nothing yet
+    const bool flush = (p % kFlushPeriods) == kFlushPeriods - 1 || p == periods - 1;
+    const int grp = warp & 3, quarter = warp >> 2;
+    const uint32_t lanes = (uint32_t)(grp * 32) << 16;
+    const ChannelGeom& g = a.jg.ch[ch];
+    const int row = Y0 + grp * 32 + lane;
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        const uint32_t cre = (uint32_t)(quarter * 32 + k * 16), cim = cre + kRsTcTile;
+        uint32_t dr[16], di[16], sr[16], si[16];
+        tmem_ld16(tmem + lanes + cre, dr);
+        tmem_ld16(tmem + lanes + cim, di);
+        if (!fresh) {
+            tmem_ld16(tmem + lanes + kDCols + cre, sr);
+            tmem_ld16(tmem + lanes + kDCols + cim, si);
+        }
+        tmem_wait_ld();
+        float vr[16], vi[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            vr[i] = __uint_as_float(dr[i]) + (fresh ? 0.f : __uint_as_float(sr[i]));
+            vi[i] = __uint_as_float(di[i]) + (fresh ? 0.f : __uint_as_float(si[i]));
+        }
+        if (flush) {
+            // field (+)= amax * (-i) (vr + i vi)
+            if (row < g.pnY) {
+                double2* dst = a.field + ((int64_t)ch * g.pnY + row) * g.pnX;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int col = X0 + (int)cre + i;
+                    if (col < g.pnX) {
+                        const double re = (double)vi[i] * (double)amax, im = -(double)vr[i] * (double)amax;
+                        if (wrote) {
+                            const double2 o = dst[col];
+                            dst[col] = make_double2(o.x + re, o.y + im);
+                        } else {
+                            dst[col] = make_double2(re, im);
+                        }
+                    }
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                sr[i] = __float_as_uint(vr[i]);
+                si[i] = __float_as_uint(vi[i]);
+            }
+            tmem_st16(tmem + lanes + kDCols + cre, sr);
+            tmem_st16(tmem + lanes + kDCols + cim, si);
+        }
+    }
+    if (flush) wrote = true;
+    tmem_wait_st();
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(acc_empty);
+    return true;
+}
+
+// One CTA per 128x128 tile of one channel, 16 warps. Every warp produces
+// factors (warps 0-7 the rows, 8-15 the columns; each 8 of a stage's 16
+// points) and drains the accumulator; warp 0 also allocates TMEM and (lane
+// 0) issues each stage's MMAs one stage after it was filled.
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcRsRec* s_rec = reinterpret_cast<TcRsRec*>(base + kStagesTc * kStageBytesTc);
     uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
     uint64_t* empty = full + kStagesTc;
-    uint64_t* acc_full = empty + kStagesTc;   // [2]: MMA -> drain, buffer ready
-    uint64_t* acc_empty = acc_full + 2;       // [2]: drain -> MMA, buffer free
-    uint64_t* drain_bar = acc_empty + 2;      // abort path: issued MMAs complete
+    uint64_t* acc_full = empty + kStagesTc;   // MMA -> drains: D holds a finished run
+    uint64_t* acc_empty = acc_full + 1;       // drains -> MMA: D was read
+    uint64_t* drain_bar = acc_empty + 1;      // abort path: issued MMAs complete
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain_bar + 1);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
@@ -227,13 +319,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStagesTc; ++s) {
-            mbar_init(&full[s], kProducerWarps);
+            mbar_init(&full[s], kWarpsTc);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&acc_full[b], 1);
-            mbar_init(&acc_empty[b], kProducerWarps);
-        }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, kWarpsTc);
         mbar_init(drain_bar, 1);
         *abort = 0;
         *s_left = 0;
@@ -245,42 +335,38 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    const int t = threadIdx.x;                 // 0..255
-    const bool side_a = warp < 4;              // rows (A) or columns (B)
-    const int rc = (warp & 3) * 32 + lane;     // row m or column n of the tile
+    const int t = threadIdx.x;
+    const bool side_a = t < 256;               // warps 0-7 rows (A), 8-15 columns (B)
+    const int hh = (t >> 7) & 1;               // which 8 of a stage's 16 points
+    const int rc = t & 127;                    // row m or column n of the tile
     const float off = side_a ? (float)((double)(kRsTcHalf - rc) * g.ppY) : (float)((double)(rc - kRsTcHalf) * g.ppX);
     const float off2 = off * off;
-    const uint32_t swz = (uint32_t)((rc >> 2) & 1);   // 32-byte swizzle: rows 4-7 of 8 swap halves
-    const uint32_t row_off0 = (uint32_t)rc * 32u + (swz << 4), row_off1 = (uint32_t)rc * 32u + ((1u ^ swz) << 4);
-    const int grp = warp & 3, half = warp >> 2;       // drain: TMEM lanes 32*grp.., columns half*64..
-    const int vx1 = min(X0 + kRsTcTile, g.pnX), vy1 = min(Y0 + kRsTcTile, g.pnY);
-    const double Xc = pixel_x(g, X0 + kRsTcHalf), Yc = pixel_y(g, Y0 + kRsTcHalf);
+    // 32-byte swizzle: rows 4-7 of every 8 swap their two 16-byte halves
+    const uint32_t row_off = (uint32_t)rc * 32u + (((uint32_t)hh ^ (uint32_t)((rc >> 2) & 1)) << 4);
+    const RsTcTile tile = rs_tc_tile(g, X0, Y0);
     const float amax = a.amax[ch];
     const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
     const PointRec* chrec = a.recs + (int64_t)ch * n;
-    float acc_re[kEpiColsTc], acc_im[kEpiColsTc];
-#pragma unroll
-    for (int i = 0; i < kEpiColsTc; ++i) acc_re[i] = acc_im[i] = 0.f;
     bool dead = false;
     bool wrote = a.jg.accumulate != 0;
-    int left = 0, drained = 0, pending = 0, issued = 0;
+    int left = 0, drained = 0, issued = 0;
 
     for (int c = 0; c < nchunks; ++c) {
-        producers_sync();   // the previous chunk's records are no longer read
+        all_sync();   // the previous chunk's records are no longer read
         {
             TcRsRec r;
-            r.P = r.Q = r.h = r.tau = r.fc = r.ac = r.k2 = r.bx = 0.f;
+            r.h = r.tau = r.P = r.bx = r.Q = r.fc = r.ac = r.k2 = 0.f;
             const int64_t idx = (int64_t)c * kChunkTc + t;
             if (!dead && idx < n) {
                 const PointRec p = chrec[idx];
-                const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
-                const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
+                const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
+                const int iy0 = max(Y0, p.y_lo), iy1 = min(tile.vy1, p.y_hi);
                 float wxm, wym;
                 if (ix0 < ix1 && iy0 < iy1) {
-                    if (rs_tc_eligible(p, g, X0, Y0, &wxm, &wym)) {
+                    if (rs_tc_eligible(p, tile, &wxm, &wym)) {
                         // FP64: frac(r_c / lambda) only. sqrt from an FP32
                         // seed refined by two Newton steps.
-                        const double dxc = Xc - p.x, dyc = Yc - p.y;
+                        const double dxc = tile.Xc - p.x, dyc = tile.Yc - p.y;
                         const double rc2 = fma(dxc, dxc, fma(dyc, dyc, p.aux));
                         const double y0 = (double)rsqrtf((float)rc2);
                         const double hy = 0.5 * y0;
@@ -289,14 +375,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                         rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
                         const double tc = rcd * g.inv_lambda;
                         const float hf = 1.0f / (float)rc2;
-                        r.P = 2.f * (float)dxc * hf;
-                        r.Q = 2.f * (float)dyc * hf;
                         r.h = hf;
                         r.tau = (float)tc;
+                        r.P = 2.f * (float)dxc * hf;
+                        r.bx = 1.f / (wxm * kCrossScale);
+                        r.Q = 2.f * (float)dyc * hf;
                         r.fc = (float)(tc - rint(tc));
                         r.ac = (float)p.coef * hf * inv_amax;
                         r.k2 = -1.5707963267948966f * r.tau * wxm * kCrossScale;
-                        r.bx = 1.f / (wxm * kCrossScale);
                     } else {
                         ++left;
                     }
@@ -304,18 +390,22 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
             }
             s_rec[t] = r;
         }
-        producers_sync();
+        all_sync();
         const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
         for (int it = it0; it < it1; ++it) {
-            // drain the previous run once two stages of this one are queued
-            if (!dead && (it % kPeriod) == 2 && it >= kPeriod) {
-                dead = !drain_period(drained, acc_full, acc_empty, abort, tmem, grp, half, lane, acc_re, acc_im);
+            // drain the finished run as the next one starts
+            if (!dead && (it % kPeriod) == 1 && it > kPeriod) {
+                dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0,
+                                  amax, wrote);
                 ++drained;
-                if (!dead && ++pending == kFlushPeriods) {
-                    flush_field(a, ch, X0, Y0, grp, half, lane, amax, wrote, acc_re, acc_im);
-                    wrote = true;
-                    pending = 0;
-                }
+            }
+            // warp 0 issues the previous stage's MMAs
+            if (warp == 0 && it > 0 && !dead) {
+                bool ok = true;
+                if (lane == 0) ok = issue_stage(it - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+                if (ok) issued = it;
+                else dead = true;
             }
             const int s = it % kStagesTc;
             if (!dead) {
@@ -324,89 +414,20 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                 dead = !__all_sync(0xffffffffu, ok);
             }
             if (dead) continue;
-            const uint32_t st = smem_u32(base + s * kStageBytesTc);
-            const int j0 = (it - it0) * kStagePts;
-#pragma unroll 1
-            for (int h8 = 0; h8 < 2; ++h8) {
-                uint32_t w_hr[4], w_hi[4], w_lr[4], w_li[4], w_xr[4], w_xi[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    float vr[2], vi[2], xr[2], xi[2];
-#pragma unroll
-                    for (int e = 0; e < 2; ++e) {
-                        const TcRsRec& r = s_rec[j0 + h8 * 8 + q * 2 + e];
-                        const float4 r0 = *reinterpret_cast<const float4*>(&r.P);
-                        const float4 r1 = *reinterpret_cast<const float4*>(&r.fc);
-                        const float w = fmaf(side_a ? r0.y : r0.x, off, r0.z * off2);
-                        const float s3 = fmaf(w, fmaf(w, 0.0625f, -0.125f), 0.5f);   // S(w) / w
-                        float ph = (r0.w * w) * s3;                                  // turns
-                        if (side_a) ph += r1.x;
-                        ph = reduce_turns_f(ph);
-                        float sn, cs;
-                        __sincosf(ph * kTwoPiF, &sn, &cs);
-                        float amp = fmaf(w, w, 1.f - w);
-                        if (side_a) amp *= r1.y;
-                        vr[e] = amp * cs;
-                        vi[e] = amp * sn;
-                        if (side_a) {
-                            const float kw = r1.z * w;   // i k w_y R
-                            xr[e] = -kw * vi[e];
-                            xi[e] = kw * vr[e];
-                        } else {
-                            const float sc = w * r1.w;   // w_x C / (64 wxm)
-                            xr[e] = sc * vr[e];
-                            xi[e] = sc * vi[e];
-                        }
-                    }
-                    w_hr[q] = bf2(vr[0], vr[1]);
-                    w_hi[q] = bf2(vi[0], vi[1]);
-                    const float2 hr = unbf2(w_hr[q]), hi = unbf2(w_hi[q]);
-                    w_lr[q] = bf2(vr[0] - hr.x, vr[1] - hr.y);
-                    w_li[q] = bf2(vi[0] - hi.x, vi[1] - hi.y);
-                    w_xr[q] = h2(xr[0], xr[1]);
-                    w_xi[q] = h2(xi[0], xi[1]);
-                }
-                const uint32_t ro = st + (h8 ? row_off1 : row_off0);
-                if (side_a) {
-                    st_v4(ro + kAhr * kPlane, w_hr);
-                    st_v4(ro + kAhi * kPlane, w_hi);
-                    st_v4(ro + kAlr * kPlane, w_lr);
-                    st_v4(ro + kAli * kPlane, w_li);
-                    st_v4(ro + kA2r * kPlane, w_xr);
-                    st_v4(ro + kA2i * kPlane, w_xi);
-                } else {
-                    uint32_t nh[4], nl[4], nx[4];
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        nh[q] = w_hi[q] ^ 0x80008000u;   // -Bi: flip both sign bits
-                        nl[q] = w_li[q] ^ 0x80008000u;
-                        nx[q] = w_xi[q] ^ 0x80008000u;
-                    }
-                    st_v4(ro + kBhn * kPlane, nh);
-                    st_v4(ro + kBhr * kPlane, w_hr);
-                    st_v4(ro + kBhi * kPlane, w_hi);
-                    st_v4(ro + kBln * kPlane, nl);
-                    st_v4(ro + kBlr * kPlane, w_lr);
-                    st_v4(ro + kBli * kPlane, w_li);
-                    st_v4(ro + kB2n * kPlane, nx);
-                    st_v4(ro + kB2r * kPlane, w_xr);
-                    st_v4(ro + kB2i * kPlane, w_xi);
-                }
-            }
+            const uint32_t ro = smem_u32(base + s * kStageBytesTc) + row_off;
+            const TcRsRec* recs8 = s_rec + (it - it0) * kStagePts + hh * kHalfPts;
+            if (side_a) produce8<true>(recs8, off, off2, ro);
+            else produce8<false>(recs8, off, off2, ro);
             fence_async_smem();   // generic-proxy writes -> visible to the tensor core
             __syncwarp();
             if (lane == 0) mbar_arrive(&full[s]);
-            // warp 0 issues the previous stage's MMAs (one stage of slack for
-            // the other warps to fill it)
-            if (warp == 0 && it > 0) {
-                bool ok = true;
-                if (lane == 0) ok = issue_stage(it - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
-                ok = __shfl_sync(0xffffffffu, ok, 0);
-                if (ok) issued = it;
-                else dead = true;
-            }
         }
     }
+    // When the last stage opens a run, the run before it must be drained
+    // (by every warp, warp 0 included) before warp 0 can issue that stage.
+    const int last_run = (total - 1) / kPeriod;
+    for (; drained < last_run && !dead; ++drained)
+        dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
     if (warp == 0 && !dead && total > 0) {
         bool ok = true;
         if (lane == 0) ok = issue_stage(total - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
@@ -414,10 +435,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
         if (ok) issued = total;
         else dead = true;
     }
-    // the runs not drained yet, then the last flush
+    // the runs not drained yet (the last one flushes into the field)
     for (int p = drained; p < periods && !dead; ++p)
-        dead = !drain_period(p, acc_full, acc_empty, abort, tmem, grp, half, lane, acc_re, acc_im);
-    if (!dead) flush_field(a, ch, X0, Y0, grp, half, lane, amax, wrote, acc_re, acc_im);
+        dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
     const int wl = __reduce_add_sync(0xffffffffu, left);
     if (lane == 0 && wl) atomicAdd(s_left, wl);
     if (warp == 0 && lane == 0 && issued > 0 && *abort) {

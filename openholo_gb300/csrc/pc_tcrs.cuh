@@ -24,8 +24,39 @@ constexpr float kRsTcMaxW = 1e-3f;
 constexpr float kRsTcMaxCross = 4e-3f;       // radians, first-order e^{i theta}: error theta^2/2
 constexpr float kRsTcMaxDropped = 2e-7f;     // turns
 
-// Decides whether the tensor-core RS kernel evaluates point p on the
-// 128x128 tile with origin (X0, Y0) of channel g. True only when
+// Constants of one 128x128 tile (origin X0, Y0) that the eligibility test
+// uses; both kernels form them with rs_tc_tile.
+struct RsTcTile {
+    int32_t X0, Y0, vx1, vy1;     // origin and end of the valid pixels
+    double Xc, Yc;                // centre pixel (X0 + 64, Y0 + 64)
+    float umin, umax, vmin, vmax; // offsets of the valid pixels from the centre (u with the column, v against the row)
+    float uext, vext;             // 64 pitches
+    float detx, dety, inv_lambda;
+};
+
+__device__ __forceinline__ RsTcTile rs_tc_tile(const ChannelGeom& g, int X0, int Y0) {
+    RsTcTile t;
+    t.X0 = X0;
+    t.Y0 = Y0;
+    t.vx1 = min(X0 + kRsTcTile, g.pnX);
+    t.vy1 = min(Y0 + kRsTcTile, g.pnY);
+    const int xc = X0 + kRsTcHalf, yc = Y0 + kRsTcHalf;
+    t.Xc = pixel_x(g, xc);
+    t.Yc = pixel_y(g, yc);
+    t.umin = __double2float_rn(__dmul_rn((double)(X0 - xc), g.ppX));
+    t.umax = __double2float_rn(__dmul_rn((double)(t.vx1 - 1 - xc), g.ppX));
+    t.vmax = __double2float_rn(__dmul_rn((double)(yc - Y0), g.ppY));
+    t.vmin = __double2float_rn(__dmul_rn((double)(yc - (t.vy1 - 1)), g.ppY));
+    t.uext = __double2float_rn(__dmul_rn((double)kRsTcHalf, g.ppX));
+    t.vext = __double2float_rn(__dmul_rn((double)kRsTcHalf, g.ppY));
+    t.detx = __double2float_rn(g.detx);
+    t.dety = __double2float_rn(g.dety);
+    t.inv_lambda = __double2float_rn(g.inv_lambda);
+    return t;
+}
+
+// Decides whether the tensor-core RS kernel evaluates point p on tile t.
+// True only when
 //  - the point's window rectangle holds every valid pixel of the tile,
 //  - every valid pixel of the tile passes the reference's cone test
 //    (ophgen/src/ophGen.cpp:415-428) with a relative margin of 1e-5,
@@ -33,44 +64,33 @@ constexpr float kRsTcMaxDropped = 2e-7f;     // turns
 //    terms the factors drop stay under kRsTcMaxDropped turns and the cross
 //    phase under kRsTcMaxCross radians.
 // wxm / wym receive the bounds of |w_x|, |w_y| over the tile.
-__device__ __forceinline__ bool rs_tc_eligible(const PointRec& p, const ChannelGeom& g, int X0, int Y0,
-                                               float* wxm_out, float* wym_out) {
-    const int vx1 = min(X0 + kRsTcTile, g.pnX), vy1 = min(Y0 + kRsTcTile, g.pnY);
-    if (!(p.x_lo <= X0 && p.x_hi >= vx1 && p.y_lo <= Y0 && p.y_hi >= vy1)) return false;
-    const int xc = X0 + kRsTcHalf, yc = Y0 + kRsTcHalf;
-    const float dxf = __double2float_rn(__dsub_rn(pixel_x(g, xc), p.x));
-    const float dyf = __double2float_rn(__dsub_rn(pixel_y(g, yc), p.y));
+__device__ __forceinline__ bool rs_tc_eligible(const PointRec& p, const RsTcTile& t, float* wxm_out,
+                                               float* wym_out) {
+    if (!(p.x_lo <= t.X0 && p.x_hi >= t.vx1 && p.y_lo <= t.Y0 && p.y_hi >= t.vy1)) return false;
+    const float dxf = __double2float_rn(__dsub_rn(t.Xc, p.x));
+    const float dyf = __double2float_rn(__dsub_rn(t.Yc, p.y));
     const float zzf = __double2float_rn(p.aux);
-    // offsets of the valid pixels from the centre: u grows with the column,
-    // v falls with the row
-    const float umin = __double2float_rn(__dmul_rn((double)(X0 - xc), g.ppX));
-    const float umax = __double2float_rn(__dmul_rn((double)(vx1 - 1 - xc), g.ppX));
-    const float vmax = __double2float_rn(__dmul_rn((double)(yc - Y0), g.ppY));
-    const float vmin = __double2float_rn(__dmul_rn((double)(yc - (vy1 - 1)), g.ppY));
-    const float uext = __double2float_rn(__dmul_rn((double)kRsTcHalf, g.ppX));
-    const float vext = __double2float_rn(__dmul_rn((double)kRsTcHalf, g.ppY));
     // cone test over the tile, conservative
-    const float xa = __fadd_rn(dxf, umin), xb = __fadd_rn(dxf, umax);
-    const float ya = __fadd_rn(dyf, vmin), yb = __fadd_rn(dyf, vmax);
-    const float slack = __fmul_rn(1e-6f, __fadd_rn(__fadd_rn(fabsf(dxf), fabsf(dyf)), __fadd_rn(uext, vext)));
+    const float xa = __fadd_rn(dxf, t.umin), xb = __fadd_rn(dxf, t.umax);
+    const float ya = __fadd_rn(dyf, t.vmin), yb = __fadd_rn(dyf, t.vmax);
+    const float slack = __fmul_rn(1e-6f, __fadd_rn(__fadd_rn(fabsf(dxf), fabsf(dyf)), __fadd_rn(t.uext, t.vext)));
     const float maxdx = __fadd_rn(fmaxf(fabsf(xa), fabsf(xb)), slack);
     const float maxdy = __fadd_rn(fmaxf(fabsf(ya), fabsf(yb)), slack);
     const float mindx = fmaxf(__fsub_rn((xa <= 0.f && xb >= 0.f) ? 0.f : fminf(fabsf(xa), fabsf(xb)), slack), 0.f);
     const float mindy = fmaxf(__fsub_rn((ya <= 0.f && yb >= 0.f) ? 0.f : fminf(fabsf(ya), fabsf(yb)), slack), 0.f);
-    const float detx = __double2float_rn(g.detx), dety = __double2float_rn(g.dety);
     const float keep = 1.f - 1e-5f;
-    const float rx = __fmul_rn(__fmul_rn(detx, __fsqrt_rn(__fadd_rn(__fmul_rn(mindy, mindy), zzf))), keep);
-    const float ry = __fmul_rn(__fmul_rn(dety, __fsqrt_rn(__fadd_rn(__fmul_rn(mindx, mindx), zzf))), keep);
+    const float rx = __fmul_rn(__fmul_rn(t.detx, __fsqrt_rn(__fadd_rn(__fmul_rn(mindy, mindy), zzf))), keep);
+    const float ry = __fmul_rn(__fmul_rn(t.dety, __fsqrt_rn(__fadd_rn(__fmul_rn(mindx, mindx), zzf))), keep);
     if (!(maxdx < rx && maxdy < ry)) return false;
     // expansion bounds
     const float rc2 = __fadd_rn(__fadd_rn(__fmul_rn(dxf, dxf), __fmul_rn(dyf, dyf)), zzf);
     const float hf = __fdiv_rn(1.0f, rc2);
     const float grow = 1.0f + 1e-4f;
-    const float nxm = __fadd_rn(__fmul_rn(__fmul_rn(2.f, fabsf(dxf)), uext), __fmul_rn(uext, uext));
-    const float nym = __fadd_rn(__fmul_rn(__fmul_rn(2.f, fabsf(dyf)), vext), __fmul_rn(vext, vext));
+    const float nxm = __fadd_rn(__fmul_rn(__fmul_rn(2.f, fabsf(dxf)), t.uext), __fmul_rn(t.uext, t.uext));
+    const float nym = __fadd_rn(__fmul_rn(__fmul_rn(2.f, fabsf(dyf)), t.vext), __fmul_rn(t.vext, t.vext));
     const float wxm = __fmul_rn(__fmul_rn(nxm, hf), grow);
     const float wym = __fmul_rn(__fmul_rn(nym, hf), grow);
-    const float tau = __fmul_rn(__fmul_rn(__fsqrt_rn(rc2), __double2float_rn(g.inv_lambda)), grow);
+    const float tau = __fmul_rn(__fmul_rn(__fsqrt_rn(rc2), t.inv_lambda), grow);
     const float s = __fadd_rn(wxm, wym);
     const float pxy = __fmul_rn(wxm, wym);
     const float cross = __fmul_rn(__fmul_rn(1.5707964f, tau), pxy);

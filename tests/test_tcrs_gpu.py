@@ -76,8 +76,8 @@ def test_tensor_rs_meets_the_bar(gpu_ctx, oracle_mod, name):
 
 
 def test_tensor_rs_many_points(gpu_ctx):
-    """70,000 points: 68 TMEM accumulation runs, both accumulator buffers and
-    several FP64 flushes. The plain FP32 RS kernel (relL2 ~1e-6 against FP64)
+    """70,000 points: 69 TMEM accumulation runs folded into the TMEM running
+    sum, with an FP64 flush every 16 runs. The plain FP32 RS kernel (relL2 ~1e-6 against FP64)
     is the reference here."""
     gk = dict(pnx=640, pny=384, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
     v = _box(70000, (2e-3, 2e-3), (0.45, 0.55), 45)
@@ -113,4 +113,19 @@ def test_tensor_rs_single_point_known_answer(gpu_ctx):
     want = amp * (np.sin(k * r) - 1j * np.cos(k * r))
     err = rel_l2(got, want)
     print(f"single point: relL2 {err:.3e}")
+    assert err <= 1e-4
+
+
+@pytest.mark.parametrize("n", [1, 15, 17, 1024, 1030, 2064, 16400])
+def test_tensor_rs_point_counts(gpu_ctx, n):
+    """Point counts at the edges of the kernel's pipeline: partial last
+    stage, a last stage that opens a new accumulation run (1030, 2064), an
+    FP64 flush in the middle (16400 = 17 runs). The plain FP32 RS kernel is
+    the reference."""
+    gk = dict(pnx=256, pny=200, ppx=8e-6, ppy=8e-6, wavelengths=[638e-9])
+    v = _box(n, (1.5e-3, 1.5e-3), (0.35, 0.5), 47 + n)
+    plain = run_generate(gpu_ctx, gk, v, RS, 0)
+    tc = run_generate(gpu_ctx, gk, v, RS, MODE_BF16X3)
+    err = rel_l2(tc, plain)
+    print(f"n={n}: tensor-core RS vs plain relL2 {err:.3e}")
     assert err <= 1e-4
