@@ -75,14 +75,16 @@ constexpr uint64_t kWaitNs = 10ull * 1000 * 1000 * 1000; // 10 s per wait
 constexpr float kCrossScale = 64.f;                      // moves the cross pair into FP16's normal range
 constexpr float kTwoPiF = 6.283185307179586f;
 
-// Per (point, tile) record. The column side reads the first four values only.
-struct __align__(16) TcRsRec {
-    float h, tau, P, bx;   // 1 / rc^2, rc / lambda, 2 dx / rc^2, 1 / (64 wxm)
-    float Q, fc, ac, k2;   // 2 dy / rc^2, frac(rc / lambda), coef / (rc^2 amax) (0: pair not taken), 64 k
+// Per (point, tile) values, stored for two consecutive points side by side
+// so that the factor arithmetic runs on packed FP32 pairs. The column side
+// reads the first four pairs only.
+struct __align__(16) TcRsPair {
+    float2 h, tau, P, bx;   // 1 / rc^2, rc / lambda, 2 dx / rc^2, 1 / (64 wxm)
+    float2 Q, fc, ac, k2;   // 2 dy / rc^2, frac(rc / lambda), coef / (rc^2 amax) (0: pair not taken), 64 k
 };
-static_assert(sizeof(TcRsRec) == 32, "TcRsRec size");
+static_assert(sizeof(TcRsPair) == 64, "TcRsPair size");
 
-constexpr size_t kSmemTc = 1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsRec) * kChunkTc + 256;
+constexpr size_t kSmemTc = 1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsPair) * kChunkTc + 512;
 static_assert(kSmemTc <= 232448, "shared memory per CTA");
 
 struct TcRsArgs {
@@ -105,67 +107,74 @@ __device__ __forceinline__ uint32_t bf2(float lo, float hi) {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&v);
 }
-__device__ __forceinline__ float2 unbf2(uint32_t w) {
-    return __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&w));
-}
 __device__ __forceinline__ uint32_t h2(float lo, float hi) {
     const __half2 v = __floats2half2_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&v);
 }
-__device__ __forceinline__ float reduce_turns_f(float t) {
-    const float m = 12582912.0f;   // 1.5 * 2^23: round to nearest integer
-    return __fsub_rn(t, __fsub_rn(__fadd_rn(t, m), m));
+
+// bf16 pair (low half = first) -> packed FP32 pair
+__device__ __forceinline__ f2::v2 bf2_to_v2(uint32_t w) {
+    return f2::pack(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+}
+__device__ __forceinline__ uint32_t bf2v(f2::v2 v) {
+    float a, b;
+    f2::unpack(v, a, b);
+    return bf2(a, b);
+}
+__device__ __forceinline__ uint32_t h2v(f2::v2 v) {
+    float a, b;
+    f2::unpack(v, a, b);
+    return h2(a, b);
 }
 
-// Factors of 8 points (recs[0..7]) for this thread's row (SIDE_A) or
-// column, written as one 16-byte chunk of every plane of the stage.
+// Factors of 8 points (4 record pairs) for this thread's row (SIDE_A) or
+// column, written as one 16-byte chunk of every plane of the stage. Two
+// points at a time in packed FP32 pairs.
 template <bool SIDE_A>
-__device__ __forceinline__ void produce8(const TcRsRec* recs, float off, float off2, uint32_t ro) {
+__device__ __forceinline__ void produce8(const TcRsPair* prs, float off, float off2, uint32_t ro) {
+    using f2::v2;
+    const v2 offp = f2::splat(off), off2p = f2::splat(off2);
+    const v2 c16 = f2::splat(0.0625f), c8 = f2::splat(-0.125f), c2 = f2::splat(0.5f), one = f2::splat(1.f);
+    const v2 two_pi = f2::splat(kTwoPiF);
     uint32_t w_hr[4], w_hi[4], w_lr[4], w_li[4], w_xr[4], w_xi[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-        float vr[2], vi[2], xr[2], xi[2];
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const TcRsRec& r = recs[q * 2 + e];
-            const float4 r0 = *reinterpret_cast<const float4*>(&r.h);   // h, tau, P, bx
-            float w, ph;
-            if (SIDE_A) {
-                const float4 r1 = *reinterpret_cast<const float4*>(&r.Q);   // Q, fc, ac, k2
-                w = fmaf(r1.x, off, r0.x * off2);
-                const float s3 = fmaf(w, fmaf(w, 0.0625f, -0.125f), 0.5f);   // S(w) / w
-                ph = fmaf(r0.y * w, s3, r1.y);                               // turns
-                ph = reduce_turns_f(ph);
-                float sn, cs;
-                __sincosf(ph * kTwoPiF, &sn, &cs);
-                const float amp = r1.z * fmaf(w, w, 1.f - w);
-                vr[e] = amp * cs;
-                vi[e] = amp * sn;
-                const float kw = r1.w * w;   // i k w_y R
-                xr[e] = -kw * vi[e];
-                xi[e] = kw * vr[e];
-            } else {
-                w = fmaf(r0.z, off, r0.x * off2);
-                const float s3 = fmaf(w, fmaf(w, 0.0625f, -0.125f), 0.5f);
-                ph = (r0.y * w) * s3;
-                ph = reduce_turns_f(ph);
-                float sn, cs;
-                __sincosf(ph * kTwoPiF, &sn, &cs);
-                const float amp = fmaf(w, w, 1.f - w);
-                vr[e] = amp * cs;
-                vi[e] = amp * sn;
-                const float sc = w * r0.w;   // w_x C / (64 wxm)
-                xr[e] = sc * vr[e];
-                xi[e] = sc * vi[e];
-            }
+        const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&prs[q]);
+        const ulonglong2 r0 = R[0];   // h, tau
+        const ulonglong2 r1 = R[1];   // P, bx
+        v2 w, ph;
+        ulonglong2 r2, r3;
+        if (SIDE_A) {
+            r2 = R[2];   // Q, fc
+            r3 = R[3];   // ac, k2
+            w = f2::fma(r2.x, offp, f2::mul(r0.x, off2p));
+        } else {
+            w = f2::fma(r1.x, offp, f2::mul(r0.x, off2p));
         }
-        w_hr[q] = bf2(vr[0], vr[1]);
-        w_hi[q] = bf2(vi[0], vi[1]);
-        const float2 hr = unbf2(w_hr[q]), hi = unbf2(w_hi[q]);
-        w_lr[q] = bf2(vr[0] - hr.x, vr[1] - hr.y);
-        w_li[q] = bf2(vi[0] - hi.x, vi[1] - hi.y);
-        w_xr[q] = h2(xr[0], xr[1]);
-        w_xi[q] = h2(xi[0], xi[1]);
+        const v2 s3 = f2::fma(w, f2::fma(w, c16, c8), c2);   // S(w) / w
+        if (SIDE_A) ph = f2::fma(f2::mul(r0.y, w), s3, r2.y);   // turns
+        else ph = f2::mul(f2::mul(r0.y, w), s3);
+        ph = f2::mul(f2::reduce_turns(ph), two_pi);
+        float p0, p1, s0, c0, s1, c1;
+        f2::unpack(ph, p0, p1);
+        __sincosf(p0, &s0, &c0);
+        __sincosf(p1, &s1, &c1);
+        v2 amp = f2::fma(w, w, f2::sub(one, w));
+        if (SIDE_A) amp = f2::mul(amp, r3.x);
+        const v2 vr = f2::mul(amp, f2::pack(c0, c1)), vi = f2::mul(amp, f2::pack(s0, s1));
+        w_hr[q] = bf2v(vr);
+        w_hi[q] = bf2v(vi);
+        w_lr[q] = bf2v(f2::sub(vr, bf2_to_v2(w_hr[q])));
+        w_li[q] = bf2v(f2::sub(vi, bf2_to_v2(w_hi[q])));
+        if (SIDE_A) {
+            const v2 kw = f2::mul(r3.y, w);   // i k w_y R = (-kw vi, kw vr)
+            w_xr[q] = h2v(f2::mul(kw, vi)) ^ 0x80008000u;
+            w_xi[q] = h2v(f2::mul(kw, vr));
+        } else {
+            const v2 sc = f2::mul(w, r1.y);   // w_x C / (64 wxm)
+            w_xr[q] = h2v(f2::mul(sc, vr));
+            w_xi[q] = h2v(f2::mul(sc, vi));
+        }
     }
 #define ST(plane, w) st_v4(ro + (plane) * kPlane, w[0], w[1], w[2], w[3])
     if (SIDE_A) {
@@ -190,20 +199,24 @@ __device__ __forceinline__ void produce8(const TcRsRec* recs, float off, float o
 #undef ST
 }
 
-// Issues the eight MMAs of stage k (warp 0, lane 0 only): waits until the
-// stage is filled and, when k opens an accumulation run, until the previous
-// run was drained out of D. False on abort.
-__device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* full, uint64_t* empty,
+// Issues the eight MMAs of stage k. Called by lane 0 of the warp that
+// completed the stage last, after an acquire on the stage's arrival counter
+// and tcgen05.fence::after_thread_sync (which order these MMAs after those
+// of earlier stages, issued by other threads). When k opens an accumulation
+// run it first waits until every warp drained the previous run out of D.
+// False on abort.
+__device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* empty,
                                             uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
                                             uint32_t tmem) {
     constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);
     constexpr uint32_t id_h = idesc_f16(0u, false, kRsTcTile, 2 * kRsTcTile);
     const int p = k / kPeriod;
     const bool opens = (k % kPeriod) == 0;
-    if (opens && p >= 1 && !mbar_wait(acc_empty, (uint32_t)(p - 1) & 1u, abort, global_ns() + kWaitNs)) return false;
+    if (opens && p >= 1) {
+        if (!mbar_wait_for(acc_empty, (uint32_t)(p - 1) & 1u, abort, kWaitNs)) return false;
+        tc_fence_after();
+    }
     const int s = k % kStagesTc;
-    if (!mbar_wait(&full[s], (uint32_t)(k / kStagesTc) & 1u, abort, global_ns() + kWaitNs)) return false;
-    tc_fence_after();
     const uint32_t d = tmem;
     const uint32_t st = smem_u32(base + s * kStageBytesTc);
 #define PL(x) sw32_desc(st + (uint32_t)((x) * kPlane))
@@ -217,8 +230,16 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
     umma(d, PL(kA2i), PL(kB2n), id_h, 1u);
 #undef PL
     umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
+    // The tensor core executes a CTA's MMAs in issue order, so the last
+    // stage's completion covers the whole run.
     if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(acc_full);
     return true;
+}
+
+__device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t* p, uint32_t v) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(smem_u32(p)), "r"(v) : "memory");
+    return old;
 }
 
 // Drains run p out of D (warp-collective, every warp): this warp's 32 TMEM
@@ -228,9 +249,10 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
 __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full, uint64_t* acc_empty,
                                           volatile int* abort, uint32_t tmem, int warp, int lane,
                                           const TcRsArgs& a, int ch, int X0, int Y0, float amax, bool& wrote) {
-    bool ok = mbar_wait(acc_full, (uint32_t)p & 1u, abort, global_ns() + kWaitNs);
+    bool ok = true;
+    if (lane == 0) ok = mbar_wait_for(acc_full, (uint32_t)p & 1u, abort, kWaitNs) && !*abort;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
     tc_fence_after();
-    ok = __all_sync(0xffffffffu, ok && !*abort);
     if (!ok) return false;
     const bool fresh = (p % kFlushPeriods) == 0;                      // S holds nothing yet
     const bool flush = (p % kFlushPeriods) == kFlushPeriods - 1 || p == periods - 1;
@@ -291,20 +313,70 @@ __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full
     return true;
 }
 
+// Per (point, tile) values of point idx into record pair slot t of buf
+// (zeros when the pair is not taken). Counts pairs left to the CUDA cores.
+__device__ __forceinline__ void make_record(TcRsPair* buf, int t, int64_t idx, int64_t n, const PointRec* chrec,
+                                            const RsTcTile& tile, double inv_lambda, float inv_amax, int X0, int Y0,
+                                            int& left) {
+    float h = 0.f, tau = 0.f, P = 0.f, bx = 0.f, Q = 0.f, fc = 0.f, ac = 0.f, k2 = 0.f;
+    if (idx < n) {
+        const PointRec p = chrec[idx];
+        const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
+        const int iy0 = max(Y0, p.y_lo), iy1 = min(tile.vy1, p.y_hi);
+        float wxm, wym;
+        if (ix0 < ix1 && iy0 < iy1) {
+            if (rs_tc_eligible(p, tile, &wxm, &wym)) {
+                // FP64: frac(r_c / lambda) only. sqrt from an FP32 seed
+                // refined by two Newton steps.
+                const double dxc = tile.Xc - p.x, dyc = tile.Yc - p.y;
+                const double rc2 = fma(dxc, dxc, fma(dyc, dyc, p.aux));
+                const double y0 = (double)rsqrtf((float)rc2);
+                const double hy = 0.5 * y0;
+                double rcd = rc2 * y0;
+                rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
+                rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
+                const double tc = rcd * inv_lambda;
+                const float hf = 1.0f / (float)rc2;
+                h = hf;
+                tau = (float)tc;
+                P = 2.f * (float)dxc * hf;
+                bx = 1.f / (wxm * kCrossScale);
+                Q = 2.f * (float)dyc * hf;
+                fc = (float)(tc - rint(tc));
+                ac = (float)p.coef * hf * inv_amax;
+                k2 = -1.5707963267948966f * tau * wxm * kCrossScale;
+            } else {
+                ++left;
+            }
+        }
+    }
+    float* f = reinterpret_cast<float*>(&buf[t >> 1]) + (t & 1);
+    f[0] = h;
+    f[2] = tau;
+    f[4] = P;
+    f[6] = bx;
+    f[8] = Q;
+    f[10] = fc;
+    f[12] = ac;
+    f[14] = k2;
+}
+
 // One CTA per 128x128 tile of one channel, 16 warps. Every warp produces
 // factors (warps 0-7 the rows, 8-15 the columns; each 8 of a stage's 16
-// points) and drains the accumulator; warp 0 also allocates TMEM and (lane
-// 0) issues each stage's MMAs one stage after it was filled.
+// points) and drains the accumulator; warp 0 allocates TMEM. The warp that
+// completes a stage last issues its MMAs, so no warp waits for another
+// except through the stage ring. The next chunk's point records are formed
+// one warp at a time during the current chunk (double-buffered).
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    TcRsRec* s_rec = reinterpret_cast<TcRsRec*>(base + kStagesTc * kStageBytesTc);
-    uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
-    uint64_t* empty = full + kStagesTc;
+    TcRsPair* s_rec = reinterpret_cast<TcRsPair*>(base + kStagesTc * kStageBytesTc);   // [2][kChunkTc / 2]
+    uint64_t* empty = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
     uint64_t* acc_full = empty + kStagesTc;   // MMA -> drains: D holds a finished run
     uint64_t* acc_empty = acc_full + 1;       // drains -> MMA: D was read
-    uint64_t* drain_bar = acc_empty + 1;      // abort path: issued MMAs complete
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain_bar + 1);
+    uint64_t* drain_w = acc_empty + 1;        // [16] abort path: a warp's issued MMAs complete
+    uint32_t* cnt = reinterpret_cast<uint32_t*>(drain_w + kWarpsTc);   // [3] stage arrival counters
+    uint32_t* tmem_slot = cnt + kStagesTc;
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
 
@@ -319,21 +391,17 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStagesTc; ++s) {
-            mbar_init(&full[s], kWarpsTc);
             mbar_init(&empty[s], 1);
+            cnt[s] = 0;
         }
         mbar_init(acc_full, 1);
         mbar_init(acc_empty, kWarpsTc);
-        mbar_init(drain_bar, 1);
+        for (int w = 0; w < kWarpsTc; ++w) mbar_init(&drain_w[w], 1);
         *abort = 0;
         *s_left = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) tmem_alloc(tmem_slot, kTmemColsTc);
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *tmem_slot;
 
     const int t = threadIdx.x;
     const bool side_a = t < 256;               // warps 0-7 rows (A), 8-15 columns (B)
@@ -347,104 +415,69 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     const float amax = a.amax[ch];
     const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
     const PointRec* chrec = a.recs + (int64_t)ch * n;
-    bool dead = false;
+    bool dead = false, issued_any = false;
     bool wrote = a.jg.accumulate != 0;
-    int left = 0, drained = 0, issued = 0;
+    int left = 0, drained = 0;
+
+    make_record(s_rec, t, t, n, chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);   // chunk 0
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
 
     for (int c = 0; c < nchunks; ++c) {
-        all_sync();   // the previous chunk's records are no longer read
-        {
-            TcRsRec r;
-            r.h = r.tau = r.P = r.bx = r.Q = r.fc = r.ac = r.k2 = 0.f;
-            const int64_t idx = (int64_t)c * kChunkTc + t;
-            if (!dead && idx < n) {
-                const PointRec p = chrec[idx];
-                const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
-                const int iy0 = max(Y0, p.y_lo), iy1 = min(tile.vy1, p.y_hi);
-                float wxm, wym;
-                if (ix0 < ix1 && iy0 < iy1) {
-                    if (rs_tc_eligible(p, tile, &wxm, &wym)) {
-                        // FP64: frac(r_c / lambda) only. sqrt from an FP32
-                        // seed refined by two Newton steps.
-                        const double dxc = tile.Xc - p.x, dyc = tile.Yc - p.y;
-                        const double rc2 = fma(dxc, dxc, fma(dyc, dyc, p.aux));
-                        const double y0 = (double)rsqrtf((float)rc2);
-                        const double hy = 0.5 * y0;
-                        double rcd = rc2 * y0;
-                        rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
-                        rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
-                        const double tc = rcd * g.inv_lambda;
-                        const float hf = 1.0f / (float)rc2;
-                        r.h = hf;
-                        r.tau = (float)tc;
-                        r.P = 2.f * (float)dxc * hf;
-                        r.bx = 1.f / (wxm * kCrossScale);
-                        r.Q = 2.f * (float)dyc * hf;
-                        r.fc = (float)(tc - rint(tc));
-                        r.ac = (float)p.coef * hf * inv_amax;
-                        r.k2 = -1.5707963267948966f * r.tau * wxm * kCrossScale;
-                    } else {
-                        ++left;
-                    }
-                }
-            }
-            s_rec[t] = r;
-        }
-        all_sync();
+        const TcRsPair* rb = s_rec + (c & 1) * (kChunkTc / 2);
         const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
         for (int it = it0; it < it1; ++it) {
-            // drain the finished run as the next one starts
-            if (!dead && (it % kPeriod) == 1 && it > kPeriod) {
+            // a run is drained (by every warp) before any warp fills the
+            // first stage of the next, so the warp that issues that stage
+            // finds D free
+            if (!dead && (it % kPeriod) == 0 && it > 0) {
                 dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0,
                                   amax, wrote);
                 ++drained;
             }
-            // warp 0 issues the previous stage's MMAs
-            if (warp == 0 && it > 0 && !dead) {
-                bool ok = true;
-                if (lane == 0) ok = issue_stage(it - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
-                ok = __shfl_sync(0xffffffffu, ok, 0);
-                if (ok) issued = it;
-                else dead = true;
-            }
+            // this warp's 32 records of the next chunk, at its own stage
+            if (c + 1 < nchunks && it - it0 == 2 * warp)
+                make_record(s_rec + ((c + 1) & 1) * (kChunkTc / 2), t, (int64_t)(c + 1) * kChunkTc + t, dead ? 0 : n,
+                            chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);
             const int s = it % kStagesTc;
             if (!dead) {
-                const bool ok =
-                    mbar_wait(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, global_ns() + kWaitNs);
-                dead = !__all_sync(0xffffffffu, ok);
+                bool ok = true;
+                if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, kWaitNs);
+                dead = !__shfl_sync(0xffffffffu, ok, 0);
             }
             if (dead) continue;
             const uint32_t ro = smem_u32(base + s * kStageBytesTc) + row_off;
-            const TcRsRec* recs8 = s_rec + (it - it0) * kStagePts + hh * kHalfPts;
+            const TcRsPair* recs8 = rb + ((it - it0) * kStagePts + hh * kHalfPts) / 2;
             if (side_a) produce8<true>(recs8, off, off2, ro);
             else produce8<false>(recs8, off, off2, ro);
             fence_async_smem();   // generic-proxy writes -> visible to the tensor core
             __syncwarp();
-            if (lane == 0) mbar_arrive(&full[s]);
+            bool ok = true;
+            if (lane == 0) {
+                const uint32_t old = atom_add_acq_rel(&cnt[s], 1u);
+                if ((old & (uint32_t)(kWarpsTc - 1)) == (uint32_t)(kWarpsTc - 1)) {   // the stage's last warp
+                    tc_fence_after();
+                    ok = issue_stage(it, total, base, empty, acc_full, acc_empty, abort, tmem);
+                    tc_fence_before();
+                    issued_any = true;
+                }
+            }
+            dead = !__shfl_sync(0xffffffffu, ok, 0);
         }
-    }
-    // When the last stage opens a run, the run before it must be drained
-    // (by every warp, warp 0 included) before warp 0 can issue that stage.
-    const int last_run = (total - 1) / kPeriod;
-    for (; drained < last_run && !dead; ++drained)
-        dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
-    if (warp == 0 && !dead && total > 0) {
-        bool ok = true;
-        if (lane == 0) ok = issue_stage(total - 1, total, base, full, empty, acc_full, acc_empty, abort, tmem);
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (ok) issued = total;
-        else dead = true;
+        all_sync();   // the next chunk's records are complete; this chunk's are no longer read
     }
     // the runs not drained yet (the last one flushes into the field)
     for (int p = drained; p < periods && !dead; ++p)
         dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
     const int wl = __reduce_add_sync(0xffffffffu, left);
     if (lane == 0 && wl) atomicAdd(s_left, wl);
-    if (warp == 0 && lane == 0 && issued > 0 && *abort) {
-        // aborted: wait (bounded) for the MMAs already issued before TMEM is released
-        umma_commit(drain_bar);
+    if (lane == 0 && issued_any && *abort) {
+        // aborted: wait (bounded) for this thread's issued MMAs before TMEM is released
+        umma_commit(&drain_w[warp]);
         const uint64_t dl = global_ns() + 1000ull * 1000 * 1000;
-        while (!mbar_try_wait(drain_bar, 0) && global_ns() < dl) {
+        while (!mbar_try_wait(&drain_w[warp], 0) && global_ns() < dl) {
         }
     }
     tc_fence_before();
