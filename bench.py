@@ -7,11 +7,14 @@ reference ships no dataset). One step = generateHologram(PC_DIFF_RS) for all
 three channels + phase encoding + 8-bit normalisation over all channels.
 
 The headline `value` is RS point x pixel interactions per second over the
-device-timed steps (inputs resident in HBM, L2 flushed between steps);
-`e2e` is the same metric through the host-facing C ABI with host buffers,
-host->device copy of the vertices and device->host copy of the complex
-field and the 8-bit codes inside every timed step. Fresnel (plain FP32
-kernel) is timed the same way and reported beside it.
+device-timed steps (inputs resident in HBM, L2 flushed between steps), with
+RS on the tensor cores (OPHPC_MODE_TENSOR_BF16X3: split-BF16 contraction of
+per-tile row and column factors, relL2 ~1e-5 against FP64, stated in
+`relL2_vs_fp64`); `e2e` is the same metric through the host-facing C ABI
+with host buffers, host->device copy of the vertices and device->host copy
+of the complex field and the 8-bit codes inside every timed step. The plain
+FP32-core RS kernel (`rs_plain`) and Fresnel (plain FP32 kernel and tensor
+cores) are timed the same way and reported beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -58,7 +61,7 @@ def parse():
     ap.add_argument("--profile-case", default=None,
                     help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
                          "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points), "
-                         "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points)")
+                         "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points), tcrs_fhd_full (all 100,000)")
     ap.add_argument("--serving-max-points", type=int, default=100_000,
                     help="largest point count of a serving job (500000 = full)")
     return ap.parse_args()
@@ -319,8 +322,11 @@ def gpu_arm(args, w):
     codes = torch.empty((nch, npx), dtype=torch.uint8, device="cuda")
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")   # > 129 MB L2
 
+    # headline RS path: the tensor-core RS (split-BF16, relL2 ~1e-5 vs FP64)
+    rs_mode = oph.MODE_TENSOR_BF16X3
+
     def step(diff):
-        ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, 0, field.data_ptr(), sp)
+        ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, rs_mode, field.data_ptr(), sp)
         ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
 
     def barrier():
@@ -361,9 +367,14 @@ def gpu_arm(args, w):
     inter = w.interactions
     value = job_value(inter, world, t_step)
 
-    # --- dominant kernel alone (generate = prep + rs kernel) for the roofline
+    # --- dominant kernel alone for the roofline: the tensor-core RS generate
+    # (prep + amax + tc_rs_kernel + CUDA-core complement, which exits at once
+    # when every pair went to the tensor cores)
+    gen_tc = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_RS, rs_mode, field.data_ptr(), sp), 3)
+    t_tc = sum(gen_tc) / len(gen_tc)
+    # the plain FP32-core RS kernel (prep + rs_kernel), reported beside it
     gen_rs = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_RS, 0, field.data_ptr(), sp), 3)
-    t_rs = sum(gen_rs) / len(gen_rs)
+    t_rs = max_over_ranks(sum(gen_rs) / len(gen_rs), dist, "cuda")
     gen_fr = timed(lambda: ctx.generate(cfg, dv.data_ptr(), w.n_points, oph.DIFF_FRESNEL, 0, field.data_ptr(), sp),
                    max(3, args.steps // 2))
     t_fr = max_over_ranks(sum(gen_fr) / len(gen_fr), dist, "cuda")
@@ -411,7 +422,7 @@ def gpu_arm(args, w):
 
     def e2e_step():
         dv2.copy_(hv, non_blocking=True)
-        ctx.generate(cfg, dv2.data_ptr(), w.n_points, oph.DIFF_RS, 0, field.data_ptr(), sp)
+        ctx.generate(cfg, dv2.data_ptr(), w.n_points, oph.DIFF_RS, rs_mode, field.data_ptr(), sp)
         ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
         hfield.copy_(field, non_blocking=True)
         hcodes.copy_(codes, non_blocking=True)
@@ -429,10 +440,16 @@ def gpu_arm(args, w):
     sm_mhz = clocks["sm_mhz"] or 1995.0
     props = torch.cuda.get_device_properties(local)
     sms = props.multi_processor_count
-    # SFU roofline: every interaction needs one sin and one cos (2 MUFU ops);
-    # 16 MUFU results per clock per SM.
+    # plain RS, SFU roofline: every interaction needs one sin and one cos
+    # (2 MUFU ops); 16 MUFU results per clock per SM.
     peak_rs = sms * 16 / 2 * sm_mhz * 1e6
     achieved_rs = inter / t_rs
+    # tensor-core RS, tensor roofline: per interaction four complex MACs
+    # (split-BF16 hi*hi, hi*lo, lo*hi and the FP16 cross pair) = 32 real
+    # flops executed, of which one complex MAC (8 flops) is the useful work
+    peaks = measured_peaks()
+    peak_tensor = peaks.get("bf16_tflops", 1900.0) * 1e12
+    achieved_tc = inter * 32 / t_tc
 
     line = None
     if rank == 0:
@@ -448,7 +465,7 @@ def gpu_arm(args, w):
             sub = w.subset(n_cpu)
             dsub = torch.from_numpy(sub.vertices).cuda()
             fsub = torch.empty_like(field)
-            ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, 0, fsub.data_ptr(), sp)
+            ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, rs_mode, fsub.data_ptr(), sp)
             torch.cuda.synchronize()
             g = fsub.cpu().numpy()
             got = g[..., 0] + 1j * g[..., 1]
@@ -465,7 +482,12 @@ def gpu_arm(args, w):
                 g = fsub.cpu().numpy()
                 got = g[..., 0] + 1j * g[..., 1]
                 rel_fp64[name] = float(np.linalg.norm(got - ref_fr) / np.linalg.norm(ref_fr))
-            rel_fp64["rs"] = rel
+            rel_fp64["rs_tc_bf16x3"] = rel
+            ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, 0, fsub.data_ptr(), sp)
+            torch.cuda.synchronize()
+            g = fsub.cpu().numpy()
+            rel_fp64["rs_plain"] = float(np.linalg.norm(g[..., 0] + 1j * g[..., 1] - ref_field) /
+                                         np.linalg.norm(ref_field))
             rel_fp64["samples"] = f"RS {n_cpu} points, Fresnel {n_fr} points, full {w.pnx}x{w.pny}x{w.n_channels}"
             # all points at seeded pixels: the error at the workload's full
             # size (it grows with the point count: part of it is common to
@@ -475,7 +497,7 @@ def gpu_arm(args, w):
                                  scale=w.scale, distance=w.distance)
             pix = np.sort(np.random.default_rng(17).choice(npx, 256, replace=False))
             full, wants = {}, {}
-            for name, diff, mode in (("rs", 0, 0), ("fresnel_plain", 1, 0),
+            for name, diff, mode in (("rs_tc_bf16x3", 0, rs_mode), ("rs_plain", 0, 0), ("fresnel_plain", 1, 0),
                                      ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3),
                                      ("fresnel_tc_fp16", 1, oph.MODE_TENSOR_FP16)):
                 ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, fsub.data_ptr(), sp)
@@ -498,16 +520,29 @@ def gpu_arm(args, w):
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": w.name, "pnx": pnx, "pny": pny, "pixel_pitch_m": w.pp,
                        "wavelengths_m": list(w.wavelengths), "n_points": w.n_points, "diff": "RS",
-                       "step": "generateHologram(RS, 3 channels) + phase encode + normalise",
+                       "step": "generateHologram(RS, 3 channels; tensor-core RS, split-BF16) + phase encode + "
+                               "normalise",
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{world}"},
             "relL2": rel,
             "relL2_vs_fp64": rel_fp64 or None,
-            "roofline": {"bound": "sfu", "kernel": "rs_kernel", "achieved": achieved_rs, "peak": peak_rs,
-                         "unit": "interactions/s", "frac": achieved_rs / peak_rs,
-                         "traffic": RS_TRAFFIC_BYTES.get(w.name), "traffic_unit": "bytes per launch (DRAM)",
-                         "algorithmic_bytes": w.n_points * nch * 64 + npx * nch * 16,
-                         "peak_basis": f"{sms} SMs x 16 MUFU/clk / 2 MUFU (sin, cos) per interaction x "
-                                       f"{sm_mhz:.0f} MHz median SM clock under load"},
+            "roofline": {"bound": "tensor", "kernel": "tc_rs_kernel", "achieved": achieved_tc / 1e12,
+                         "peak": peak_tensor / 1e12, "unit": "TFLOP/s", "frac": achieved_tc / peak_tensor,
+                         "traffic": TCRS_TRAFFIC_BYTES.get(w.name), "traffic_unit": "bytes per launch (DRAM)",
+                         "algorithmic_flops": inter * 32, "useful_flops": inter * 8,
+                         "useful_frac": achieved_tc / 4 / peak_tensor,
+                         "peak_basis": "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 GEMM, burst): of measured",
+                         "flops_basis": "32 executed flops per point x pixel interaction (four complex MACs: "
+                                        "split-BF16 hi*hi, hi*lo, lo*hi, FP16 cross pair); 8 useful"},
+            "rs_plain": {"value": job_value(inter, world, t_rs), "unit": UNIT, "ms_per_generate": t_rs * 1e3,
+                         "kernel": "rs_kernel (FP32 cores + MUFU)",
+                         "speedup_of_tensor_core_rs": t_rs / t_tc,
+                         "roofline": {"bound": "sfu", "achieved": achieved_rs, "peak": peak_rs,
+                                      "unit": "interactions/s", "frac": achieved_rs / peak_rs,
+                                      "traffic": RS_TRAFFIC_BYTES.get(w.name),
+                                      "traffic_unit": "bytes per launch (DRAM)",
+                                      "algorithmic_bytes": w.n_points * nch * 64 + npx * nch * 16,
+                                      "peak_basis": f"{sms} SMs x 16 MUFU/clk / 2 MUFU (sin, cos) per "
+                                                    f"interaction x {sm_mhz:.0f} MHz median SM clock under load"}},
             "fresnel": {"value": job_value(inter, world, t_fr), "unit": UNIT, "ms_per_generate": t_fr * 1e3,
                         "kernel": "fresnel_kernel (FP32 cores, separable)"},
             "tensor_fresnel": tensor,
@@ -526,6 +561,22 @@ def gpu_arm(args, w):
         dist.destroy_process_group()
     ctx.close()
     return line
+
+
+def measured_peaks() -> dict:
+    """MEASURED_PEAKS.json (HBM copy and cuBLAS bf16 throughput measured on
+    this GPU pool), or {} when absent."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one tc_rs_kernel launch of
+# the workload's tensor-core RS generate, from a 1-pass ncu capture of
+# `bench.py --profile-case tcrs_fhd_full` (profiles/tc_rs_kernel_sphere_fhd.md).
+TCRS_TRAFFIC_BYTES = {"sphere_fhd": 21874176 + 70098176}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one rs_kernel launch of the
@@ -551,6 +602,8 @@ def profile_case(name: str) -> None:
         mode = oph.MODE_TENSOR_FP16 if name == "tc_fp16_4k" else oph.MODE_TENSOR_BF16X3
     elif name == "tcrs_fhd":   # tensor-core RS, sphere_fhd geometry, 20,000 of its points
         w, diff, mode = workloads.sphere_fhd().subset(20_000), 0, oph.MODE_TENSOR_BF16X3
+    elif name == "tcrs_fhd_full":   # the headline step's tensor-core RS generate (~110 MB on the device)
+        w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
     else:
         raise SystemExit(f"unknown profile case {name}")
     ctx = oph.Context(0)
