@@ -55,18 +55,19 @@ namespace {
 
 using namespace tc5;
 
-constexpr int kWarpsTc = 16;
-constexpr int kThreadsTc = 32 * kWarpsTc;                // 512: producers, drains; warp 0 issues the MMAs
+constexpr int kProdWarps = 8;                            // factor producers (and drains)
+constexpr int kProducers = 32 * kProdWarps;              // 256: rows 0-127, then columns 0-127
+constexpr int kMmaWarp = kProdWarps;                     // warp 8: TMEM allocation, MMA issue
+constexpr int kThreadsTc = kProducers + 32;
 constexpr int kStagePts = 16;                            // points per stage: one K=16 MMA step
-constexpr int kHalfPts = kStagePts / 2;                  // points per thread per stage (one 16-byte chunk)
 constexpr int kStagesTc = 3;
 constexpr int kPlane = kRsTcTile * kStagePts * 2;        // 4096 B: 128 rows x 32 B
 // planes of one stage (kB?n: the negated imaginary plane, so that [Bn; Br]
 // and [Br; Bi] are both contiguous N=256 operands)
 enum : int { kAhr = 0, kAhi, kAlr, kAli, kA2r, kA2i, kBhn, kBhr, kBhi, kBln, kBlr, kBli, kB2n, kB2r, kB2i, kPlanes };
 constexpr int kStageBytesTc = kPlanes * kPlane;          // 61,440
-constexpr int kChunkTc = kThreadsTc;                     // points per record round (one per thread)
-constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 32
+constexpr int kChunkTc = kProducers;                     // points per record round (one per producer)
+constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 16
 constexpr int kPeriod = 64;                              // stages per TMEM accumulation run (1024 points)
 constexpr int kFlushPeriods = 16;                        // runs summed in TMEM before an FP64 flush
 constexpr int kDCols = 2 * kRsTcTile;                    // accumulator D: re [0,128), im [128,256)
@@ -98,7 +99,7 @@ struct TcRsArgs {
 };
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void all_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kThreadsTc) : "memory"); }
+__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory"); }
 __device__ __forceinline__ void st_v4(uint32_t addr, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
     asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(w0), "r"(w1), "r"(w2), "r"(w3)
                  : "memory");
@@ -127,18 +128,19 @@ __device__ __forceinline__ uint32_t h2v(f2::v2 v) {
     return h2(a, b);
 }
 
-// Factors of 8 points (4 record pairs) for this thread's row (SIDE_A) or
-// column, written as one 16-byte chunk of every plane of the stage. Two
-// points at a time in packed FP32 pairs.
+// Factors of the 16 points of a stage (8 record pairs) for this thread's
+// row (SIDE_A) or column, written as the row's two 16-byte chunks of every
+// plane of the stage (ro0: points 0-7, ro1: points 8-15). Two points at a
+// time in packed FP32 pairs.
 template <bool SIDE_A>
-__device__ __forceinline__ void produce8(const TcRsPair* prs, float off, float off2, uint32_t ro) {
+__device__ __forceinline__ void produce16(const TcRsPair* prs, float off, float off2, uint32_t ro0, uint32_t ro1) {
     using f2::v2;
     const v2 offp = f2::splat(off), off2p = f2::splat(off2);
     const v2 c16 = f2::splat(0.0625f), c8 = f2::splat(-0.125f), c2 = f2::splat(0.5f), one = f2::splat(1.f);
     const v2 two_pi = f2::splat(kTwoPiF);
-    uint32_t w_hr[4], w_hi[4], w_lr[4], w_li[4], w_xr[4], w_xi[4];
+    uint32_t w_hr[8], w_hi[8], w_lr[8], w_li[8], w_xr[8], w_xi[8];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < 8; ++q) {
         const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&prs[q]);
         const ulonglong2 r0 = R[0];   // h, tau
         const ulonglong2 r1 = R[1];   // P, bx
@@ -176,47 +178,50 @@ __device__ __forceinline__ void produce8(const TcRsPair* prs, float off, float o
             w_xi[q] = h2v(f2::mul(sc, vi));
         }
     }
-#define ST(plane, w) st_v4(ro + (plane) * kPlane, w[0], w[1], w[2], w[3])
-    if (SIDE_A) {
-        ST(kAhr, w_hr);
-        ST(kAhi, w_hi);
-        ST(kAlr, w_lr);
-        ST(kAli, w_li);
-        ST(kA2r, w_xr);
-        ST(kA2i, w_xi);
-    } else {
-        const uint32_t n = 0x80008000u;   // -Bi: flip both sign bits
-        st_v4(ro + kBhn * kPlane, w_hi[0] ^ n, w_hi[1] ^ n, w_hi[2] ^ n, w_hi[3] ^ n);
-        ST(kBhr, w_hr);
-        ST(kBhi, w_hi);
-        st_v4(ro + kBln * kPlane, w_li[0] ^ n, w_li[1] ^ n, w_li[2] ^ n, w_li[3] ^ n);
-        ST(kBlr, w_lr);
-        ST(kBli, w_li);
-        st_v4(ro + kB2n * kPlane, w_xi[0] ^ n, w_xi[1] ^ n, w_xi[2] ^ n, w_xi[3] ^ n);
-        ST(kB2r, w_xr);
-        ST(kB2i, w_xi);
-    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t ro = h ? ro1 : ro0;
+        const int o = 4 * h;
+#define ST(plane, w) st_v4(ro + (plane) * kPlane, w[o], w[o + 1], w[o + 2], w[o + 3])
+        if (SIDE_A) {
+            ST(kAhr, w_hr);
+            ST(kAhi, w_hi);
+            ST(kAlr, w_lr);
+            ST(kAli, w_li);
+            ST(kA2r, w_xr);
+            ST(kA2i, w_xi);
+        } else {
+            const uint32_t n = 0x80008000u;   // -Bi: flip both sign bits
+            st_v4(ro + kBhn * kPlane, w_hi[o] ^ n, w_hi[o + 1] ^ n, w_hi[o + 2] ^ n, w_hi[o + 3] ^ n);
+            ST(kBhr, w_hr);
+            ST(kBhi, w_hi);
+            st_v4(ro + kBln * kPlane, w_li[o] ^ n, w_li[o + 1] ^ n, w_li[o + 2] ^ n, w_li[o + 3] ^ n);
+            ST(kBlr, w_lr);
+            ST(kBli, w_li);
+            st_v4(ro + kB2n * kPlane, w_xi[o] ^ n, w_xi[o + 1] ^ n, w_xi[o + 2] ^ n, w_xi[o + 3] ^ n);
+            ST(kB2r, w_xr);
+            ST(kB2i, w_xi);
+        }
 #undef ST
+    }
 }
 
-// Issues the eight MMAs of stage k. Called by lane 0 of the warp that
-// completed the stage last, after an acquire on the stage's arrival counter
-// and tcgen05.fence::after_thread_sync (which order these MMAs after those
-// of earlier stages, issued by other threads). When k opens an accumulation
-// run it first waits until every warp drained the previous run out of D.
-// False on abort.
-__device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* empty,
+// Issues the eight MMAs of stage k (the MMA warp's lane 0): waits until the
+// producers filled the stage and, when k opens an accumulation run, until
+// every producer warp drained the previous run out of D. Issuing blocks
+// while the tensor core's queue is full (about as long as a stage's MMAs
+// take), which is why a warp of its own does it. False on abort.
+__device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* full, uint64_t* empty,
                                             uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
                                             uint32_t tmem) {
     constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);
     constexpr uint32_t id_h = idesc_f16(0u, false, kRsTcTile, 2 * kRsTcTile);
     const int p = k / kPeriod;
     const bool opens = (k % kPeriod) == 0;
-    if (opens && p >= 1) {
-        if (!mbar_wait_for(acc_empty, (uint32_t)(p - 1) & 1u, abort, kWaitNs)) return false;
-        tc_fence_after();
-    }
+    if (opens && p >= 1 && !mbar_wait_for(acc_empty, (uint32_t)(p - 1) & 1u, abort, kWaitNs)) return false;
     const int s = k % kStagesTc;
+    if (!mbar_wait_for(&full[s], (uint32_t)(k / kStagesTc) & 1u, abort, kWaitNs)) return false;
+    tc_fence_after();
     const uint32_t d = tmem;
     const uint32_t st = smem_u32(base + s * kStageBytesTc);
 #define PL(x) sw32_desc(st + (uint32_t)((x) * kPlane))
@@ -230,20 +235,12 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
     umma(d, PL(kA2i), PL(kB2n), id_h, 1u);
 #undef PL
     umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
-    // The tensor core executes a CTA's MMAs in issue order, so the last
-    // stage's completion covers the whole run.
     if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(acc_full);
     return true;
 }
 
-__device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t* p, uint32_t v) {
-    uint32_t old;
-    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], %2;" : "=r"(old) : "r"(smem_u32(p)), "r"(v) : "memory");
-    return old;
-}
-
-// Drains run p out of D (warp-collective, every warp): this warp's 32 TMEM
-// lanes x (32 columns of D_re + the 32 of D_im) are added into the running
+// Drains run p out of D (warp-collective, every producer warp): this warp's
+// 32 TMEM lanes x (64 columns of D_re + the 64 of D_im) are added into the running
 // sum S (or replace it when S was just flushed); on a flush run the sum goes
 // into the FP64 field instead. False when the CTA is aborting.
 __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full, uint64_t* acc_empty,
@@ -256,13 +253,13 @@ __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full
     if (!ok) return false;
     const bool fresh = (p % kFlushPeriods) == 0;                      // S holds nothing yet
     const bool flush = (p % kFlushPeriods) == kFlushPeriods - 1 || p == periods - 1;
-    const int grp = warp & 3, quarter = warp >> 2;
+    const int grp = warp & 3, half = warp >> 2;
     const uint32_t lanes = (uint32_t)(grp * 32) << 16;
     const ChannelGeom& g = a.jg.ch[ch];
     const int row = Y0 + grp * 32 + lane;
 #pragma unroll 1
-    for (int k = 0; k < 2; ++k) {
-        const uint32_t cre = (uint32_t)(quarter * 32 + k * 16), cim = cre + kRsTcTile;
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t cre = (uint32_t)(half * 64 + k * 16), cim = cre + kRsTcTile;
         uint32_t dr[16], di[16], sr[16], si[16];
         tmem_ld16(tmem + lanes + cre, dr);
         tmem_ld16(tmem + lanes + cim, di);
@@ -361,22 +358,21 @@ __device__ __forceinline__ void make_record(TcRsPair* buf, int t, int64_t idx, i
     f[14] = k2;
 }
 
-// One CTA per 128x128 tile of one channel, 16 warps. Every warp produces
-// factors (warps 0-7 the rows, 8-15 the columns; each 8 of a stage's 16
-// points) and drains the accumulator; warp 0 allocates TMEM. The warp that
-// completes a stage last issues its MMAs, so no warp waits for another
-// except through the stage ring. The next chunk's point records are formed
-// one warp at a time during the current chunk (double-buffered).
+// One CTA per 128x128 tile of one channel. Warps 0-7 produce the factors
+// (threads 0-127 the rows, 128-255 the columns, all 16 points of a stage
+// each) and drain the accumulator; warp 8 allocates TMEM and its lane 0
+// issues the MMAs. The next chunk's point records are formed one producer
+// warp at a time during the current chunk (double-buffered).
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcRsPair* s_rec = reinterpret_cast<TcRsPair*>(base + kStagesTc * kStageBytesTc);   // [2][kChunkTc / 2]
-    uint64_t* empty = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
+    uint64_t* empty = full + kStagesTc;
     uint64_t* acc_full = empty + kStagesTc;   // MMA -> drains: D holds a finished run
     uint64_t* acc_empty = acc_full + 1;       // drains -> MMA: D was read
-    uint64_t* drain_w = acc_empty + 1;        // [16] abort path: a warp's issued MMAs complete
-    uint32_t* cnt = reinterpret_cast<uint32_t*>(drain_w + kWarpsTc);   // [3] stage arrival counters
-    uint32_t* tmem_slot = cnt + kStagesTc;
+    uint64_t* drain_bar = acc_empty + 1;      // abort path: issued MMAs complete
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain_bar + 1);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
 
@@ -391,99 +387,96 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStagesTc; ++s) {
+            mbar_init(&full[s], kProdWarps);
             mbar_init(&empty[s], 1);
-            cnt[s] = 0;
         }
         mbar_init(acc_full, 1);
-        mbar_init(acc_empty, kWarpsTc);
-        for (int w = 0; w < kWarpsTc; ++w) mbar_init(&drain_w[w], 1);
+        mbar_init(acc_empty, kProdWarps);
+        mbar_init(drain_bar, 1);
         *abort = 0;
         *s_left = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 0) tmem_alloc(tmem_slot, kTmemColsTc);
+    if (warp == kMmaWarp) tmem_alloc(tmem_slot, kTmemColsTc);
 
     const int t = threadIdx.x;
-    const bool side_a = t < 256;               // warps 0-7 rows (A), 8-15 columns (B)
-    const int hh = (t >> 7) & 1;               // which 8 of a stage's 16 points
-    const int rc = t & 127;                    // row m or column n of the tile
+    const bool side_a = t < kRsTcTile;         // rows (A) or columns (B)
+    const int rc = t & (kRsTcTile - 1);        // row m or column n of the tile
     const float off = side_a ? (float)((double)(kRsTcHalf - rc) * g.ppY) : (float)((double)(rc - kRsTcHalf) * g.ppX);
     const float off2 = off * off;
     // 32-byte swizzle: rows 4-7 of every 8 swap their two 16-byte halves
-    const uint32_t row_off = (uint32_t)rc * 32u + (((uint32_t)hh ^ (uint32_t)((rc >> 2) & 1)) << 4);
+    const uint32_t swz = (uint32_t)((rc >> 2) & 1);
+    const uint32_t row_off0 = (uint32_t)rc * 32u + (swz << 4), row_off1 = (uint32_t)rc * 32u + ((1u ^ swz) << 4);
     const RsTcTile tile = rs_tc_tile(g, X0, Y0);
     const float amax = a.amax[ch];
     const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
     const PointRec* chrec = a.recs + (int64_t)ch * n;
-    bool dead = false, issued_any = false;
+    bool dead = false;
     bool wrote = a.jg.accumulate != 0;
-    int left = 0, drained = 0;
+    int left = 0, drained = 0, issued = 0;
 
-    make_record(s_rec, t, t, n, chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);   // chunk 0
+    if (warp < kProdWarps) make_record(s_rec, t, t, n, chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);   // chunk 0
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
-    for (int c = 0; c < nchunks; ++c) {
-        const TcRsPair* rb = s_rec + (c & 1) * (kChunkTc / 2);
-        const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
-        for (int it = it0; it < it1; ++it) {
-            // a run is drained (by every warp) before any warp fills the
-            // first stage of the next, so the warp that issues that stage
-            // finds D free
-            if (!dead && (it % kPeriod) == 0 && it > 0) {
-                dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0,
-                                  amax, wrote);
-                ++drained;
-            }
-            // this warp's 32 records of the next chunk, at its own stage
-            if (c + 1 < nchunks && it - it0 == 2 * warp)
-                make_record(s_rec + ((c + 1) & 1) * (kChunkTc / 2), t, (int64_t)(c + 1) * kChunkTc + t, dead ? 0 : n,
-                            chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);
-            const int s = it % kStagesTc;
-            if (!dead) {
-                bool ok = true;
-                if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, kWaitNs);
-                dead = !__shfl_sync(0xffffffffu, ok, 0);
-            }
-            if (dead) continue;
-            const uint32_t ro = smem_u32(base + s * kStageBytesTc) + row_off;
-            const TcRsPair* recs8 = rb + ((it - it0) * kStagePts + hh * kHalfPts) / 2;
-            if (side_a) produce8<true>(recs8, off, off2, ro);
-            else produce8<false>(recs8, off, off2, ro);
-            fence_async_smem();   // generic-proxy writes -> visible to the tensor core
-            __syncwarp();
-            bool ok = true;
-            if (lane == 0) {
-                const uint32_t old = atom_add_acq_rel(&cnt[s], 1u);
-                if ((old & (uint32_t)(kWarpsTc - 1)) == (uint32_t)(kWarpsTc - 1)) {   // the stage's last warp
-                    tc_fence_after();
-                    ok = issue_stage(it, total, base, empty, acc_full, acc_empty, abort, tmem);
-                    tc_fence_before();
-                    issued_any = true;
+    if (warp == kMmaWarp) {
+        if (lane == 0) {
+            for (; issued < total; ++issued)
+                if (!issue_stage(issued, total, base, full, empty, acc_full, acc_empty, abort, tmem)) break;
+            if (issued < total && issued > 0) {
+                // aborted: wait (bounded) for the MMAs already issued before TMEM is released
+                umma_commit(drain_bar);
+                const uint64_t dl = global_ns() + 1000ull * 1000 * 1000;
+                while (!mbar_try_wait(drain_bar, 0) && global_ns() < dl) {
                 }
             }
-            dead = !__shfl_sync(0xffffffffu, ok, 0);
         }
-        all_sync();   // the next chunk's records are complete; this chunk's are no longer read
-    }
-    // the runs not drained yet (the last one flushes into the field)
-    for (int p = drained; p < periods && !dead; ++p)
-        dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
-    const int wl = __reduce_add_sync(0xffffffffu, left);
-    if (lane == 0 && wl) atomicAdd(s_left, wl);
-    if (lane == 0 && issued_any && *abort) {
-        // aborted: wait (bounded) for this thread's issued MMAs before TMEM is released
-        umma_commit(&drain_w[warp]);
-        const uint64_t dl = global_ns() + 1000ull * 1000 * 1000;
-        while (!mbar_try_wait(&drain_w[warp], 0) && global_ns() < dl) {
+    } else {
+        for (int c = 0; c < nchunks; ++c) {
+            const TcRsPair* rb = s_rec + (c & 1) * (kChunkTc / 2);
+            const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
+            for (int it = it0; it < it1; ++it) {
+                // a run is drained (by every producer warp) before any of them
+                // fills the first stage of the next, so the MMA warp finds D
+                // free when it gets there
+                if (!dead && (it % kPeriod) == 0 && it > 0) {
+                    dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0,
+                                      amax, wrote);
+                    ++drained;
+                }
+                // this warp's 32 records of the next chunk, at its own stage
+                if (c + 1 < nchunks && it - it0 == 2 * warp)
+                    make_record(s_rec + ((c + 1) & 1) * (kChunkTc / 2), t, (int64_t)(c + 1) * kChunkTc + t,
+                                dead ? 0 : n, chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);
+                const int s = it % kStagesTc;
+                if (!dead) {
+                    bool ok = true;
+                    if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, kWaitNs);
+                    dead = !__shfl_sync(0xffffffffu, ok, 0);
+                }
+                if (dead) continue;
+                const uint32_t sb = smem_u32(base + s * kStageBytesTc);
+                const TcRsPair* recs16 = rb + ((it - it0) * kStagePts) / 2;
+                if (side_a) produce16<true>(recs16, off, off2, sb + row_off0, sb + row_off1);
+                else produce16<false>(recs16, off, off2, sb + row_off0, sb + row_off1);
+                fence_async_smem();   // generic-proxy writes -> visible to the tensor core
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
+            }
+            producers_sync();   // the next chunk's records are complete; this chunk's are no longer read
         }
+        // the runs not drained yet (the last one flushes into the field)
+        for (int p = drained; p < periods && !dead; ++p)
+            dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
+        const int wl = __reduce_add_sync(0xffffffffu, left);
+        if (lane == 0 && wl) atomicAdd(s_left, wl);
     }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    if (warp == 0) tmem_dealloc(tmem, kTmemColsTc);
+    if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemColsTc);
     if (threadIdx.x == 0) {
         a.left[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x] = *s_left;
         if (*abort) atomicExch(a.error, 1);
