@@ -17,20 +17,22 @@
 // contraction D = sum_j A_j B_j^T over the points, run on the tensor cores:
 //
 //   warps 0-7   producers: per (point, tile) record in FP64 (frac(tau) is the
-//               only FP64 step; k r reaches ~6e6 rad), then per stage of 16
-//               points warps 0-3 write the row factors A (128 rows) and
-//               warps 4-7 the column factors B (128 columns) into shared
-//               memory in the UMMA K-major 32-byte-swizzle layout:
-//               split-BF16 (hi + lo) for R and C, FP16 for the cross pair;
-//   warp 8      allocates 512 TMEM columns; one thread issues per stage
+//               only FP64 step; k r reaches ~6e6 rad), formed for the next
+//               chunk of 256 points one warp at a time; per stage of 16
+//               points threads 0-127 write the row factors A (one row each)
+//               and threads 128-255 the column factors B (one column each)
+//               into shared memory in the UMMA K-major 32-byte-swizzle
+//               layout: split-BF16 (hi + lo) for R and C, FP16 for the cross
+//               pair;
+//   warp 8      allocates 512 TMEM columns; its lane 0 only issues per stage
 //               eight tcgen05.mma kind::f16, M=128, N=256, K=16: the N=256
 //               B operand [Br; Bi] (or [-Bi; Br]) yields D_re and D_im of
 //               one product at once; passes (hi,hi), (hi,lo), (lo,hi) in
 //               BF16 and the cross pair in FP16;
-//   warps 0-7   also drain the TMEM accumulators: every 64 stages (1024
+//   warps 0-7   also drain the TMEM accumulator D: every 64 stages (1024
 //               points; the tensor core's FP32 accumulation loses ~1e-8 of
-//               the sum per point) into FP32 registers, double-buffered, and
-//               every 16 drains into the FP64 field.
+//               the sum per point) into a running sum S in the other 256
+//               TMEM columns, and every 16 drains into the FP64 field.
 //
 // Pairs for which the expansion does not hold (window cuts the tile, the cone
 // test is not passed by the whole tile, |w| or the cross phase too large:

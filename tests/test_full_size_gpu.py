@@ -8,7 +8,7 @@ Workloads (openholo_gb300/workloads.py, seeded synthetic inputs with the
 benchmark's shapes and distributions): rs_1k 1024x1024 / 5,000 points,
 sphere_fhd 1920x1080 x 3 colours / 100,000, box_4k 3840x2160 / 1,000,000,
 box_8k 7680x4320 / 2,000,000. Bars: relL2 <= 1e-4 (plain kernels, tensor
-cores split-BF16)."""
+cores split-BF16 for Fresnel and RS)."""
 import numpy as np
 import pytest
 
@@ -66,6 +66,14 @@ def test_sphere_fhd(gpu_ctx, oracle_mod, diff):
     _check_at(oracle_mod, w, _generate(gpu_ctx, w, diff), diff, _pixels(w.pnx, w.pny, 768, 128, 2))
 
 
+def test_sphere_fhd_tensor_rs(gpu_ctx, oracle_mod):
+    """The headline configuration on the tensor-core RS path."""
+    import openholo_gb300 as oph
+    from openholo_gb300 import workloads
+    w = workloads.sphere_fhd()
+    _check_at(oracle_mod, w, _generate(gpu_ctx, w, 0, oph.MODE_TENSOR_BF16X3), 0, _pixels(w.pnx, w.pny, 768, 128, 2))
+
+
 def test_sphere_fhd_additivity(gpu_ctx):
     """Full size: field(A ∪ B) = field(A) + field(B) for disjoint point sets
     (the sum is linear in the points; only rounding differs)."""
@@ -90,7 +98,8 @@ def test_box_4k(gpu_ctx, oracle_mod):
     w = workloads.box_4k()
     idx = _pixels(w.pnx, w.pny, 256, 64, 3)
     _check_at(oracle_mod, w, _generate(gpu_ctx, w, 0), 0, idx)                         # plain RS
-    _check_at(oracle_mod, w, _generate(gpu_ctx, w, 1, oph.MODE_TENSOR_BF16X3), 1, idx)  # tensor cores
+    _check_at(oracle_mod, w, _generate(gpu_ctx, w, 0, oph.MODE_TENSOR_BF16X3), 0, idx)  # RS, tensor cores
+    _check_at(oracle_mod, w, _generate(gpu_ctx, w, 1, oph.MODE_TENSOR_BF16X3), 1, idx)  # Fresnel, tensor cores
 
 
 def test_box_8k_tensor(gpu_ctx, oracle_mod):
@@ -99,3 +108,5 @@ def test_box_8k_tensor(gpu_ctx, oracle_mod):
     w = workloads.box_8k()
     idx = _pixels(w.pnx, w.pny, 128, 32, 4)
     _check_at(oracle_mod, w, _generate(gpu_ctx, w, 1, oph.MODE_TENSOR_BF16X3), 1, idx)
+    # config 5 is an RS workload: the tensor-core RS at full size (6.6e13 interactions)
+    _check_at(oracle_mod, w, _generate(gpu_ctx, w, 0, oph.MODE_TENSOR_BF16X3), 0, idx)
