@@ -20,7 +20,8 @@
  *   - every generateHologram runs on the GPU (MODE_CPU selects nothing: there
  *     is no CPU path); MODE_FLOAT / MODE_FASTMATH select nothing either — one
  *     kernel per method, FP32 arithmetic with FP64 phase reduction, FP64
- *     output; OPHPC_MODE_TENSOR_* selects the tensor-core Fresnel kernel;
+ *     output; OPHPC_MODE_TENSOR_* selects the tensor-core Fresnel kernel
+ *     and, with PC_DIFF_RS, OPHPC_MODE_TENSOR_BF16X3 the tensor-core RS;
  *   - errors are reported through return values and lastError(), never by
  *     exiting the process;
  *   - encoding() supports ENCODE_PHASE, ENCODE_AMPLITUDE, ENCODE_REAL,
