@@ -418,10 +418,10 @@ ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, co
     };
     const bool split = (mode & OPHPC_MODE_TENSOR_BF16X3) != 0;
     if (!encode_fn()) return fail(OPHPC_ERROR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
-    static std::once_flag attr_once;
-    std::call_once(attr_once, [] {
-        cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
-    });
+    // per call: the attribute belongs to the current device
+    if (cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem) !=
+        cudaSuccess)
+        return fail(OPHPC_ERROR_CUDA, "cudaFuncSetAttribute(tc_gemm_kernel) failed");
     const int pnX = cfg->pixel_number[0], pnY = cfg->pixel_number[1];
     const int64_t plane = (int64_t)pnX * pnY;
     const int nch = (int)cfg->n_channels;

@@ -50,7 +50,6 @@
 
 #include <algorithm>
 #include <cstring>
-#include <mutex>
 
 namespace ophpc {
 namespace {
@@ -507,9 +506,9 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
         if (err) *err = msg;
         return st;
     };
-    static std::once_flag attr_once;
-    std::call_once(attr_once,
-                   [] { cudaFuncSetAttribute(tc_rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTc); });
+    // per call: the attribute belongs to the current device
+    if (cudaFuncSetAttribute(tc_rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTc) != cudaSuccess)
+        return fail(OPHPC_ERROR_CUDA, "cudaFuncSetAttribute(tc_rs_kernel) failed");
     const int nch = jg.n_channels;
     const int pnX = cfg->pixel_number[0], pnY = cfg->pixel_number[1];
     const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
