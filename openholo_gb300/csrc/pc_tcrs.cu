@@ -86,7 +86,8 @@ struct __align__(16) TcRsPair {
 };
 static_assert(sizeof(TcRsPair) == 64, "TcRsPair size");
 
-constexpr size_t kSmemTc = 1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsPair) * kChunkTc + 512;
+constexpr size_t kSmemTc =
+    1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsPair) * kChunkTc + sizeof(PointRec) * kChunkTc + 512;
 static_assert(kSmemTc <= 232448, "shared memory per CTA");
 
 struct TcRsArgs {
@@ -99,6 +100,13 @@ struct TcRsArgs {
     int32_t tiles_x, tiles_y;
 };
 
+// 16-byte asynchronous global -> shared copy (the copying thread sees the
+// data after cp.async.wait_all).
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory"); }
 __device__ __forceinline__ void st_v4(uint32_t addr, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
@@ -313,25 +321,24 @@ __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full
 
 // Per (point, tile) values of point idx into record pair slot t of buf
 // (zeros when the pair is not taken). Counts pairs left to the CUDA cores.
-__device__ __forceinline__ void make_record(TcRsPair* buf, int t, int64_t idx, int64_t n, const PointRec* chrec,
+__device__ __forceinline__ void make_record(TcRsPair* buf, int t, bool valid, const PointRec& p,
                                             const RsTcTile& tile, double inv_lambda, float inv_amax, int X0, int Y0,
                                             int& left) {
     float h = 0.f, tau = 0.f, P = 0.f, bx = 0.f, Q = 0.f, fc = 0.f, ac = 0.f, k2 = 0.f;
-    if (idx < n) {
-        const PointRec p = chrec[idx];
+    if (valid) {
         const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
         const int iy0 = max(Y0, p.y_lo), iy1 = min(tile.vy1, p.y_hi);
         float wxm, wym;
         if (ix0 < ix1 && iy0 < iy1) {
             if (rs_tc_eligible(p, tile, &wxm, &wym)) {
                 // FP64: frac(r_c / lambda) only. sqrt from an FP32 seed
-                // refined by two Newton steps.
+                // refined by one Newton step (relative error ~1e-14: 1e-8
+                // turns at tau ~1e6).
                 const double dxc = tile.Xc - p.x, dyc = tile.Yc - p.y;
                 const double rc2 = fma(dxc, dxc, fma(dyc, dyc, p.aux));
                 const double y0 = (double)rsqrtf((float)rc2);
                 const double hy = 0.5 * y0;
                 double rcd = rc2 * y0;
-                rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
                 rcd = fma(hy, fma(-rcd, rcd, rc2), rcd);
                 const double tc = rcd * inv_lambda;
                 const float hf = 1.0f / (float)rc2;
@@ -368,7 +375,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcRsPair* s_rec = reinterpret_cast<TcRsPair*>(base + kStagesTc * kStageBytesTc);   // [2][kChunkTc / 2]
-    uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
+    PointRec* s_pts = reinterpret_cast<PointRec*>(s_rec + kChunkTc);   // next chunk's points, prefetched
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_pts + kChunkTc);
     uint64_t* empty = full + kStagesTc;
     uint64_t* acc_full = empty + kStagesTc;   // MMA -> drains: D holds a finished run
     uint64_t* acc_empty = acc_full + 1;       // drains -> MMA: D was read
@@ -416,7 +424,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     bool wrote = a.jg.accumulate != 0;
     int left = 0, drained = 0, issued = 0;
 
-    if (warp < kProdWarps) make_record(s_rec, t, t, n, chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);   // chunk 0
+    if (warp < kProdWarps) {   // chunk 0
+        const bool valid = t < n;
+        make_record(s_rec, t, valid, chrec[valid ? t : 0], tile, g.inv_lambda, inv_amax, X0, Y0, left);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -435,8 +446,17 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
             }
         }
     } else {
+        const uint32_t my_pt = smem_u32(&s_pts[t]);
         for (int c = 0; c < nchunks; ++c) {
             const TcRsPair* rb = s_rec + (c & 1) * (kChunkTc / 2);
+            // prefetch this thread's point of the next chunk
+            const int64_t nidx = (int64_t)(c + 1) * kChunkTc + t;
+            const bool nvalid = c + 1 < nchunks && nidx < n;
+            if (nvalid) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) cp_async16(my_pt + 16u * q, reinterpret_cast<const char*>(chrec + nidx) + 16 * q);
+            }
+            cp_async_commit();
             const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
             for (int it = it0; it < it1; ++it) {
                 // a run is drained (by every producer warp) before any of them
@@ -448,9 +468,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                     ++drained;
                 }
                 // this warp's 32 records of the next chunk, at its own stage
-                if (c + 1 < nchunks && it - it0 == 2 * warp)
-                    make_record(s_rec + ((c + 1) & 1) * (kChunkTc / 2), t, (int64_t)(c + 1) * kChunkTc + t,
-                                dead ? 0 : n, chrec, tile, g.inv_lambda, inv_amax, X0, Y0, left);
+                if (c + 1 < nchunks && it - it0 == 2 * warp) {
+                    cp_async_wait_all();
+                    make_record(s_rec + ((c + 1) & 1) * (kChunkTc / 2), t, nvalid && !dead, s_pts[t], tile,
+                                g.inv_lambda, inv_amax, X0, Y0, left);
+                }
                 const int s = it % kStagesTc;
                 if (!dead) {
                     bool ok = true;
