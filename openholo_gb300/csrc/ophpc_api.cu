@@ -196,7 +196,7 @@ ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const 
         return tc_generate_fresnel(ctx->pool, cfg, d_vertices, n_points, mode, d_field, s, &ctx->last_error);
     }
     if (diff_flag == OPHPC_DIFF_RS && (mode & OPHPC_MODE_TENSOR_BF16X3) && !accumulate && color_offset == 0) {
-        return tc_generate_rs(ctx->pool, jg, cfg, d_vertices, n_points, d_field, s, &ctx->last_error);
+        return tc_generate_rs(ctx->pool, jg, cfg, d_vertices, n_points, d_field, ctx->sm_count, s, &ctx->last_error);
     }
     const int bps = diff_flag == OPHPC_DIFF_RS ? ctx->rs_bps : ctx->fr_bps;
     choose_split(jg, ctx->sm_count * bps);

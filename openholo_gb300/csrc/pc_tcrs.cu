@@ -49,6 +49,7 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 namespace ophpc {
@@ -98,6 +99,13 @@ struct TcRsArgs {
     int32_t* left;          // [n_channels][tiles_y][tiles_x]: pairs left to the CUDA cores
     int* error;
     int32_t tiles_x, tiles_y;
+    // The point range of every tile is split into ksplit parts of pps
+    // points (blockIdx.z = channel * ksplit + part) so that the CTA count
+    // fills whole waves; part 0 writes the field, part k > 0 writes
+    // partials[k - 1] (same layout), summed afterwards.
+    int32_t ksplit;
+    int64_t pps;
+    double2* partials;
 };
 
 // 16-byte asynchronous global -> shared copy (the copying thread sees the
@@ -258,7 +266,8 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
 // into the FP64 field instead. False when the CTA is aborting.
 __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full, uint64_t* acc_empty,
                                           volatile int* abort, uint32_t tmem, int warp, int lane,
-                                          const TcRsArgs& a, int ch, int X0, int Y0, float amax, bool& wrote) {
+                                          const TcRsArgs& a, int ch, double2* out, int X0, int Y0, float amax,
+                                          bool& wrote) {
     bool ok = true;
     if (lane == 0) ok = mbar_wait_for(acc_full, (uint32_t)p & 1u, abort, kWaitNs) && !*abort;
     ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -290,7 +299,7 @@ __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full
         if (flush) {
             // field (+)= amax * (-i) (vr + i vi)
             if (row < g.pnY) {
-                double2* dst = a.field + ((int64_t)ch * g.pnY + row) * g.pnX;
+                double2* dst = out + ((int64_t)ch * g.pnY + row) * g.pnX;
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
                     const int col = X0 + (int)cre + i;
@@ -390,10 +399,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ch = blockIdx.z;
+    const int ch = blockIdx.z / a.ksplit, part = blockIdx.z % a.ksplit;
     const ChannelGeom& g = a.jg.ch[ch];
     const int X0 = blockIdx.x * kRsTcTile, Y0 = blockIdx.y * kRsTcTile;
-    const int64_t n = a.jg.n_points;
+    const int64_t p_beg = (int64_t)part * a.pps;
+    const int64_t n = min(a.jg.n_points, p_beg + a.pps) - p_beg;   // this CTA's points: [p_beg, p_beg + n)
+    double2* out = part == 0 ? a.field
+                             : a.partials + (int64_t)(part - 1) * a.jg.n_channels * a.jg.ch[0].pnX * a.jg.ch[0].pnY;
     const int total = (int)((n + kStagePts - 1) / kStagePts);
     const int nchunks = (int)((n + kChunkTc - 1) / kChunkTc);
     const int periods = (total + kPeriod - 1) / kPeriod;
@@ -423,7 +435,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     const RsTcTile tile = rs_tc_tile(g, X0, Y0);
     const float amax = a.amax[ch];
     const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
-    const PointRec* chrec = a.recs + (int64_t)ch * n;
+    const PointRec* chrec = a.recs + (int64_t)ch * a.jg.n_points + p_beg;
     bool dead = false;
     bool wrote = a.jg.accumulate != 0;
     int left = 0, drained = 0, issued = 0;
@@ -467,8 +479,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                 // fills the first stage of the next, so the MMA warp finds D
                 // free when it gets there
                 if (!dead && (it % kPeriod) == 0 && it > 0) {
-                    dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0,
-                                      amax, wrote);
+                    dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out, X0,
+                                      Y0, amax, wrote);
                     ++drained;
                 }
                 // this warp's 32 records of the next chunk, at its own stage
@@ -496,7 +508,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
         }
         // the runs not drained yet (the last one flushes into the field)
         for (int p = drained; p < periods && !dead; ++p)
-            dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, X0, Y0, amax, wrote);
+            dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out, X0, Y0, amax,
+                              wrote);
         const int wl = __reduce_add_sync(0xffffffffu, left);
         if (lane == 0 && wl) atomicAdd(s_left, wl);
     }
@@ -505,7 +518,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     tc_fence_after();
     if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemColsTc);
     if (threadIdx.x == 0) {
-        a.left[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x] = *s_left;
+        if (*s_left) atomicAdd(&a.left[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x], *s_left);
         if (*abort) atomicExch(a.error, 1);
     }
 }
@@ -526,8 +539,8 @@ size_t align_up(size_t v, size_t al) { return (v + al - 1) / al * al; }
 }  // namespace
 
 ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
-                            const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, cudaStream_t s,
-                            std::string* err) {
+                            const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, int sm_count,
+                            cudaStream_t s, std::string* err) {
     auto fail = [&](ophpc_status st, const char* msg) {
         if (err) *err = msg;
         return st;
@@ -540,14 +553,36 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
     const size_t rec_bytes = align_up(sizeof(PointRec) * n_points * nch, 256);
     const size_t left_bytes = align_up(sizeof(int32_t) * (size_t)nch * tiles_x * tiles_y, 256);
+    // One CTA per SM: split every tile's points into k parts so that the
+    // CTA count fills whole waves (each extra part costs a field-sized
+    // partial and a summing pass: demand a 3% gain, at least 1,024 points
+    // a part, at most 2 GiB of partials).
+    const int64_t tiles = (int64_t)tiles_x * tiles_y * nch;
+    const size_t field_bytes = sizeof(double2) * (size_t)nch * pnX * pnY;
+    const int slots = sm_count > 0 ? sm_count : 1;
+    int ksplit = 1;
+    double best = 0.0;
+    for (int k = 1; k <= 8; ++k) {
+        if (k > 1 && ((int64_t)n_points / k < 1024 || (size_t)(k - 1) * field_bytes > ((size_t)2 << 30))) break;
+        const double waves = (double)(tiles * k) / slots;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best + 0.03) {
+            best = eff;
+            ksplit = k;
+        }
+    }
+    const int64_t pps = ((int64_t)n_points + ksplit - 1) / ksplit;   // every part non-empty: n >= 1024 k
+    const size_t part_bytes = align_up(field_bytes * (size_t)(ksplit - 1), 256);
     unsigned char* buf = nullptr;
-    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + 256, pool, s) != cudaSuccess)
+    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + part_bytes + 256, pool, s) != cudaSuccess)
         return fail(OPHPC_ERROR_OUT_OF_MEMORY, "tensor-core RS scratch allocation failed");
     PointRec* recs = (PointRec*)buf;
     int32_t* left = (int32_t*)(buf + rec_bytes);
-    float* amax = (float*)(buf + rec_bytes + left_bytes);   // [3]
+    double2* partials = ksplit > 1 ? (double2*)(buf + rec_bytes + left_bytes) : nullptr;
+    float* amax = (float*)(buf + rec_bytes + left_bytes + part_bytes);   // [3]
     int* errw = (int*)(amax + 4);
     cudaMemsetAsync(amax, 0, 32, s);   // amax[0..3] and the error word
+    cudaMemsetAsync(left, 0, left_bytes, s);
 
     launch_prep(d_vertices, (int64_t)n_points, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window,
                 (int)OPHPC_DIFF_RS, jg, recs, s);
@@ -566,8 +601,14 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     ta.error = errw;
     ta.tiles_x = tiles_x;
     ta.tiles_y = tiles_y;
+    ta.ksplit = ksplit;
+    ta.pps = pps;
+    ta.partials = partials;
     count_launches(1);
-    tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTc, s>>>(ta);
+    tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)(nch * ksplit)), kThreadsTc, kSmemTc, s>>>(ta);
+    JobGeom js = jg;
+    js.ksplit = ksplit;
+    launch_sum_partials(js, (double2*)d_field, partials, s);
 
     // the CUDA-core complement: the pairs the tensor-core kernel left
     JobGeom jc = jg;

@@ -121,10 +121,11 @@ __device__ __forceinline__ bool rs_tc_eligible(const PointRec& p, const RsTcTile
 }
 
 // Host entry (pc_tcrs.cu): RS generate on the tensor cores plus the
-// CUDA-core complement. jg comes from the plain path's geometry; the call
-// synchronises `stream` at the end to read the kernels' error word.
+// CUDA-core complement. jg comes from the plain path's geometry; sm_count
+// sizes the point-range split. The call synchronises `stream` at the end to
+// read the kernels' error word.
 ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
-                            const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field,
+                            const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, int sm_count,
                             cudaStream_t stream, std::string* err);
 
 }  // namespace ophpc

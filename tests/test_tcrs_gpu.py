@@ -63,8 +63,9 @@ def test_tensor_rs_meets_the_bar(gpu_ctx, oracle_mod, name):
     before = oph.lib().ophpc_kernel_launches()
     got = run_generate(gpu_ctx, gk, v, RS, MODE_BF16X3)
     launched = oph.lib().ophpc_kernel_launches() - before
-    # prep, one amax reduction per channel, the tensor-core kernel, the complement
-    assert launched == 3 + len(gk["wavelengths"])
+    # prep, one amax reduction per channel, the tensor-core kernel, the
+    # complement, and the partial-field sum when the points were split
+    assert launched in (3 + len(gk["wavelengths"]), 4 + len(gk["wavelengths"]))
     err = rel_l2(got, ref)
     print(f"{name}: tensor-core RS relL2 = {err:.3e}")
     assert err <= 1e-4
