@@ -30,12 +30,12 @@ def _config(tmp_path, xml):
     return cfg, str(p)
 
 
-def _device_field(ctx, cfg, vertices, diff):
+def _device_field(ctx, cfg, vertices, diff, mode=0):
     import torch
     nch, pny, pnx = cfg.n_channels, cfg.pixel_number[1], cfg.pixel_number[0]
     dv = torch.from_numpy(np.ascontiguousarray(vertices)).cuda()
     f = torch.empty((nch, pny, pnx, 2), dtype=torch.float64, device="cuda")
-    ctx.generate(cfg, dv.data_ptr(), vertices.shape[0], diff, 0, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    ctx.generate(cfg, dv.data_ptr(), vertices.shape[0], diff, mode, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     h = f.cpu().numpy()
     return h[..., 0] + 1j * h[..., 1]
@@ -55,21 +55,26 @@ def _check(ctx, field, d, pre):
         assert exact >= CODE_EXACT and maxd <= 1, (pre, name, exact, maxd)
 
 
-@pytest.mark.parametrize("diff,tag", [(0, "rs"), (1, "fresnel")])
-def test_dice_through_c_abi(tmp_path, gpu_ctx, diff, tag):
+# mode 0x200 (OPHPC_MODE_TENSOR_BF16X3): RS and Fresnel on the tensor cores.
+# The Dice's anti-aliasing windows cut most 128x128 tiles, so for RS most
+# pairs go to the FP32-core complement and the two kernels' split is tested
+# against the reference's own output.
+@pytest.mark.parametrize("diff,tag,mode", [(0, "rs", 0), (1, "fresnel", 0), (0, "rs", 0x200), (1, "fresnel", 0x200)])
+def test_dice_through_c_abi(tmp_path, gpu_ctx, diff, tag, mode):
     d = np.load(os.path.join(GOLD, "dice.npz"))
     cfg, _ = _config(tmp_path, str(d["xml"]))
     assert (cfg.pixel_number[0], cfg.pixel_number[1], cfg.n_channels) == (1920, 1080, 1)
-    _check(gpu_ctx, _device_field(gpu_ctx, cfg, d["vertices"], diff), d, tag + "_")
+    _check(gpu_ctx, _device_field(gpu_ctx, cfg, d["vertices"], diff, mode), d, tag + "_")
 
 
-def test_dice_rgb_through_facade(tmp_path, gpu_ctx):
+@pytest.mark.parametrize("mode", [1, 1 | 0x200])
+def test_dice_rgb_through_facade(tmp_path, gpu_ctx, mode):
     d = np.load(os.path.join(GOLD, "dice_rgb.npz"))
     _, xml = _config(tmp_path, str(d["xml"]))
     with P.PointCloud() as h:
         assert h.readConfig(xml)
         h.setPointCloudModel(d["vertices"])
-        h.SetMode(1)
+        h.SetMode(mode)
         assert h.generateHologram(0) > 0.0, h.lastError()
         field = h.getComplexField()
         assert field.shape == (3, 1080, 1920)

@@ -130,3 +130,21 @@ def test_tensor_rs_point_counts(gpu_ctx, n):
     err = rel_l2(tc, plain)
     print(f"n={n}: tensor-core RS vs plain relL2 {err:.3e}")
     assert err <= 1e-4
+
+
+def test_tensor_rs_offset_scale_viewing_window(gpu_ctx, oracle_mod):
+    """Pixel offsets, per-axis scale, a distance and the viewing-window
+    transform (transVW, ophgen/src/ophGen.cpp:1976-1985) reach the tensor-core
+    path through the same point preparation as the FP32-core kernels."""
+    gk = dict(pnx=320, pny=200, ppx=6e-6, ppy=7e-6, wavelengths=[532e-9, 638e-9],
+              scale=(0.8, 1.2, 1.5), distance=0.1)
+    v = _box(1500, (1e-3, 1e-3), (0.15, 0.3), 48)
+    kw = dict(offset=(5, -3), viewing_window=True, field_length=0.9)
+    g = oracle_mod.Geometry(**{k: gk[k] for k in ("pnx", "pny", "ppx", "ppy", "wavelengths")},
+                            scale=gk["scale"], distance=gk["distance"], offset=kw["offset"],
+                            viewing_window=True, field_length=kw["field_length"])
+    ref = oracle_mod.generate(g, v, RS)
+    got = run_generate(gpu_ctx, gk, v, RS, MODE_BF16X3, **kw)
+    err = rel_l2(got, ref)
+    print(f"offset / scale / viewing window: relL2 {err:.3e}")
+    assert err <= 1e-4
