@@ -249,6 +249,8 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
         hv = torch.from_numpy(w.vertices).pin_memory()
         hc = torch.empty((w.n_channels, w.pny, w.pnx), dtype=torch.uint8).pin_memory()
         prepared.append((make_config(**w.geometry_kwargs()), hv, hc, w.n_points, jb.diff_flag, w.interactions))
+    # RS jobs on the tensor-core RS (split-BF16), Fresnel jobs on the FP32-core kernel
+    mode_of = lambda d: 0x200 if d == 0 else 0   # noqa: E731
     out = {"jobs": n_jobs, "max_points": max_points, "loads": {}}
     rng = np.random.default_rng(seed + 1)
     gaps = rng.exponential(1.0, n_jobs)
@@ -264,7 +266,7 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
                 dt = arrivals[i] - (time.perf_counter() - t0)
                 if dt > 0:
                     time.sleep(dt)
-                tickets[i] = srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0)
+                tickets[i] = srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0, mode_of(d))
 
         th = threading.Thread(target=feeder)
         th.start()
@@ -282,7 +284,7 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
     with Server(0, max_in_flight=16, step_ms=2.0, policy=POLICY_DEADLINE) as srv:
         iso = []
         for cfg, hv, hc, n, d, _ in prepared:
-            r = srv.wait_stats(srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0))
+            r = srv.wait_stats(srv.submit_raw(cfg, hv.data_ptr(), n, d, None, hc.data_ptr(), 0, mode_of(d)))
             iso.append(r.t_done - r.t_submit)
         iso = np.array(iso)
         mean_s = float(iso.mean())
@@ -290,6 +292,7 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
                               "mean": mean_s * 1e3}
         out["policy"] = ("short jobs (< 20 ms estimated) first, the rest by earliest deadline "
                          "(submission + 2 x estimated isolated time)")
+        out["kernels"] = "RS jobs on the tensor-core RS (split-BF16), Fresnel jobs on the FP32-core kernel"
         for load in loads:
             out["loads"][f"{load:.2f}"] = run_load(srv, load, mean_s)
     with Server(0, max_in_flight=16, step_ms=2.0, policy=POLICY_SHORTEST_REMAINING) as srv:

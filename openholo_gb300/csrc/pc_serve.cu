@@ -15,11 +15,16 @@
 // shortest remaining work. Short jobs are not stuck behind long ones and
 // long ones are not starved by a stream of short ones.
 //
+// RS jobs submitted with OPHPC_MODE_TENSOR_BF16X3 run their point-range
+// steps on the tensor-core RS kernel (plus its CUDA-core complement for the
+// same range), sized by its rate.
+//
 // A job's result does not depend on what else runs: its chunking is fixed
 // by the job alone and every chunk adds into the FP64 field in order.
 #include "ophpc_serve.h"
 
 #include "pc_common.cuh"
+#include "pc_tcrs.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -63,6 +68,10 @@ struct ServeJob {
     double* d_field = nullptr;
     uint8_t* d_codes = nullptr;
     unsigned long long* d_mm = nullptr;
+    bool tc = false;            // RS on the tensor cores (OPHPC_MODE_TENSOR_BF16X3)
+    float* d_amax = nullptr;    // tensor-core RS: per-channel amplitude bound
+    int32_t* d_left = nullptr;  // tensor-core RS: per-tile pair counts for the complement
+    int* d_err = nullptr;       // tensor-core RS: kernel timeout word
     double t_submit = 0, t_admit = 0, t_done = 0;
     double remaining = 0;       // interactions left
     double est_s = 0;           // estimated isolated service time
@@ -107,6 +116,8 @@ struct ophpc_server {
     size_t mem_in_use = 0;
     bool stop = false;
     double rate_rs = 2.0e12, rate_fresnel = 2.6e12;   // interactions/s used to size steps
+    double rate_tc_rs = 2.2e13;                        // tensor-core RS
+    int* h_err = nullptr;                              // [slot]: page-locked copies of the jobs' error words
 };
 
 namespace {
@@ -126,7 +137,9 @@ bool job_ok(const ophpc_job* j) {
         if (!(c.wave_length[i] > 0) || c.wave_length[i] >= 2 * c.pixel_pitch[0] || c.wave_length[i] >= 2 * c.pixel_pitch[1])
             return false;
     if (j->diff_flag > 1) return false;
-    if (j->mode & (OPHPC_MODE_TENSOR_FP16 | OPHPC_MODE_TENSOR_BF16X3)) return false;
+    // tensor cores: RS with split-BF16 only
+    if (j->mode & OPHPC_MODE_TENSOR_FP16) return false;
+    if ((j->mode & OPHPC_MODE_TENSOR_BF16X3) && j->diff_flag != OPHPC_DIFF_RS) return false;
     if (j->n_points > 0 && !j->h_vertices) return false;
     if (j->n_points > (uint64_t)INT32_MAX) return false;
     if (j->encode_flag > OPHPC_ENCODE_IMAGINARY) return false;
@@ -161,10 +174,18 @@ JobGeom make_job_geom(const ophpc_config* cfg, int64_t n) {
     return jg;
 }
 
+bool uses_tc(const ophpc_job* j) { return j->diff_flag == OPHPC_DIFF_RS && (j->mode & OPHPC_MODE_TENSOR_BF16X3); }
+
+size_t tc_left_bytes(const ophpc_job* j) {
+    const size_t tiles = (size_t)((j->cfg.pixel_number[0] + kRsTcTile - 1) / kRsTcTile) *
+                         ((j->cfg.pixel_number[1] + kRsTcTile - 1) / kRsTcTile);
+    return align256(sizeof(int32_t) * tiles * j->cfg.n_channels);
+}
+
 size_t job_bytes(const ophpc_job* j) {
     const size_t px = (size_t)j->cfg.pixel_number[0] * j->cfg.pixel_number[1] * j->cfg.n_channels;
     return align256(sizeof(ophpc_vertex) * j->n_points) + align256(sizeof(PointRec) * j->n_points * j->cfg.n_channels) +
-           align256(sizeof(double2) * px) + align256(px) + 256;
+           align256(sizeof(double2) * px) + align256(px) + 256 + (uses_tc(j) ? 256 + tc_left_bytes(j) : 0);
 }
 
 // Enqueues the job's next step on the stream of its slot at the priority
@@ -176,11 +197,14 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
     const int64_t px = (int64_t)d.cfg.pixel_number[0] * d.cfg.pixel_number[1];
     cudaError_t e = cudaSuccess;
     if (j->stage == 0) {
+        if (j->tc) e = cudaMemsetAsync(j->d_amax, 0, 32, st);   // amax[0..3] and the error word
         if (n > 0) {
-            e = cudaMemcpyAsync(j->d_v, d.h_vertices, sizeof(ophpc_vertex) * n, cudaMemcpyHostToDevice, st);
+            if (e == cudaSuccess)
+                e = cudaMemcpyAsync(j->d_v, d.h_vertices, sizeof(ophpc_vertex) * n, cudaMemcpyHostToDevice, st);
             launch_prep(j->d_v, n, d.cfg.scale, d.cfg.distance, d.cfg.field_length, d.cfg.viewing_window,
                         (int)d.diff_flag, j->jg, j->d_recs, st);
-        } else {
+            if (j->tc) launch_rs_amax(j->d_recs, n, (int)d.cfg.n_channels, j->d_amax, st);
+        } else if (e == cudaSuccess) {
             e = cudaMemsetAsync(j->d_field, 0, sizeof(double2) * px * d.cfg.n_channels, st);
         }
         j->stage = n > 0 ? 1 : 2;
@@ -190,7 +214,10 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
         g.p1 = std::min<int64_t>(n, j->next_point + j->chunk_points);
         g.accumulate = j->next_point > 0 ? 1 : 0;
         g.points_per_split = std::max<int64_t>(kChunk, ((g.p1 - g.p0 + kChunk - 1) / kChunk) * kChunk);
-        if (d.diff_flag == OPHPC_DIFF_RS)
+        if (j->tc)
+            e = launch_tc_rs_range(j->jg, j->d_recs, g.p0, g.p1, g.accumulate != 0,
+                                   reinterpret_cast<double2*>(j->d_field), j->d_amax, j->d_left, j->d_err, st);
+        else if (d.diff_flag == OPHPC_DIFF_RS)
             launch_rs(j->d_recs, g, reinterpret_cast<double2*>(j->d_field), nullptr, st);
         else
             launch_fresnel(j->d_recs, g, reinterpret_cast<double2*>(j->d_field), nullptr, st);
@@ -206,6 +233,8 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
         }
         if (d.h_field && e == cudaSuccess)
             e = cudaMemcpyAsync(d.h_field, j->d_field, sizeof(double2) * px * d.cfg.n_channels, cudaMemcpyDeviceToHost, st);
+        if (j->tc && e == cudaSuccess)
+            e = cudaMemcpyAsync(&s->h_err[j->slot], j->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
         j->stage = 3;
     }
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -242,6 +271,14 @@ bool admit(ophpc_server* s, ServeJob* j) {
     j->d_codes = q;
     q += align256(px);
     j->d_mm = (unsigned long long*)q;
+    if (j->tc) {
+        q += 256;
+        j->d_amax = (float*)q;   // [4] floats, then the error word
+        j->d_err = (int*)(q + 16);
+        q += 256;
+        j->d_left = (int32_t*)q;
+        s->h_err[j->slot] = 0;
+    }
     s->mem_in_use += j->bytes;
     j->t_admit = now_s(s);
     return true;
@@ -287,6 +324,8 @@ void worker_main(ophpc_server* s) {
                 if (q != cudaSuccess) {
                     j->status = OPHPC_ERROR_CUDA;
                     j->stage = 3;
+                } else if (j->tc && j->stage == 3 && s->h_err[j->slot] != 0 && j->status == OPHPC_SUCCESS) {
+                    j->status = OPHPC_ERROR_TIMEOUT;   // a tensor-core wait gave up
                 }
             }
             if (!j->in_flight && j->stage == 3) {
@@ -363,6 +402,8 @@ ophpc_status ophpc_server_create(int32_t device, const ophpc_server_options* opt
     pp.location.type = cudaMemLocationTypeDevice;
     pp.location.id = device;
     if (cudaMemPoolCreate(&s->pool, &pp) != cudaSuccess) return OPHPC_ERROR_CUDA;
+    if (cudaHostAlloc((void**)&s->h_err, sizeof(int) * s->opt.max_in_flight, cudaHostAllocDefault) != cudaSuccess)
+        return OPHPC_ERROR_CUDA;
     uint64_t keep = UINT64_MAX;
     cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     int lo = 0, hi = 0;
@@ -393,7 +434,8 @@ ophpc_status ophpc_server_submit(ophpc_server* s, const ophpc_job* job, uint64_t
     if (j->bytes > s->opt.memory_budget) return OPHPC_ERROR_OUT_OF_MEMORY;
     j->jg = make_job_geom(&job->cfg, (int64_t)job->n_points);
     const double px = (double)job->cfg.pixel_number[0] * job->cfg.pixel_number[1] * job->cfg.n_channels;
-    const double rate = job->diff_flag == OPHPC_DIFF_RS ? s->rate_rs : s->rate_fresnel;
+    j->tc = uses_tc(job);
+    const double rate = j->tc ? s->rate_tc_rs : (job->diff_flag == OPHPC_DIFF_RS ? s->rate_rs : s->rate_fresnel);
     int64_t cp = (int64_t)(s->opt.step_ms * 1e-3 * rate / px);
     cp = std::max<int64_t>(kChunk, cp / kChunk * kChunk);
     j->chunk_points = cp;
@@ -457,6 +499,7 @@ ophpc_status ophpc_server_destroy(ophpc_server* s) {
     for (auto& kv : s->jobs)
         if (kv.second->ev) cudaEventDestroy(kv.second->ev);
     cudaMemPoolDestroy(s->pool);
+    if (s->h_err) cudaFreeHost(s->h_err);
     delete s;
     return OPHPC_SUCCESS;
 }

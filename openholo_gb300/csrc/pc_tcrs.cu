@@ -99,10 +99,12 @@ struct TcRsArgs {
     int32_t* left;          // [n_channels][tiles_y][tiles_x]: pairs left to the CUDA cores
     int* error;
     int32_t tiles_x, tiles_y;
-    // The point range of every tile is split into ksplit parts of pps
-    // points (blockIdx.z = channel * ksplit + part) so that the CTA count
-    // fills whole waves; part 0 writes the field, part k > 0 writes
+    // Points [p_base, p_base + p_count) of the records. The range of every
+    // tile is split into ksplit parts of pps points (blockIdx.z = channel *
+    // ksplit + part) so that the CTA count fills whole waves; part 0 writes
+    // (or, with jg.accumulate, adds into) the field, part k > 0 writes
     // partials[k - 1] (same layout), summed afterwards.
+    int64_t p_base, p_count;
     int32_t ksplit;
     int64_t pps;
     double2* partials;
@@ -402,8 +404,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     const int ch = blockIdx.z / a.ksplit, part = blockIdx.z % a.ksplit;
     const ChannelGeom& g = a.jg.ch[ch];
     const int X0 = blockIdx.x * kRsTcTile, Y0 = blockIdx.y * kRsTcTile;
-    const int64_t p_beg = (int64_t)part * a.pps;
-    const int64_t n = min(a.jg.n_points, p_beg + a.pps) - p_beg;   // this CTA's points: [p_beg, p_beg + n)
+    const int64_t p_beg = a.p_base + (int64_t)part * a.pps;
+    const int64_t n = min(a.p_base + a.p_count, p_beg + a.pps) - p_beg;   // this CTA's points: [p_beg, p_beg + n)
     double2* out = part == 0 ? a.field
                              : a.partials + (int64_t)(part - 1) * a.jg.n_channels * a.jg.ch[0].pnX * a.jg.ch[0].pnY;
     const int total = (int)((n + kStagePts - 1) / kStagePts);
@@ -437,7 +439,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
     const PointRec* chrec = a.recs + (int64_t)ch * a.jg.n_points + p_beg;
     bool dead = false;
-    bool wrote = a.jg.accumulate != 0;
+    bool wrote = part == 0 && a.jg.accumulate != 0;
     int left = 0, drained = 0, issued = 0;
 
     if (warp < kProdWarps) {   // chunk 0
@@ -601,6 +603,8 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     ta.error = errw;
     ta.tiles_x = tiles_x;
     ta.tiles_y = tiles_y;
+    ta.p_base = 0;
+    ta.p_count = (int64_t)n_points;
     ta.ksplit = ksplit;
     ta.pps = pps;
     ta.partials = partials;
@@ -631,6 +635,53 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     if (e != cudaSuccess) return fail(OPHPC_ERROR_CUDA, cudaGetErrorString(e));
     if (herr) return fail(OPHPC_ERROR_TIMEOUT, "tensor-core RS kernel wait timed out");
     return OPHPC_SUCCESS;
+}
+
+void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t s) {
+    for (int c = 0; c < n_channels; ++c) {
+        count_launches(1);
+        rs_amax_kernel<<<256, 256, 0, s>>>(d_recs + (int64_t)c * n_points, n_points, d_amax + c);
+    }
+}
+
+cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1, bool accumulate,
+                               double2* d_field, const float* d_amax, int32_t* d_left, int* d_err, cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(tc_rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTc);
+    if (e != cudaSuccess || p1 <= p0) return e;
+    const int nch = jg.n_channels;
+    const int pnX = jg.ch[0].pnX, pnY = jg.ch[0].pnY;
+    const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
+    e = cudaMemsetAsync(d_left, 0, sizeof(int32_t) * (size_t)nch * tiles_x * tiles_y, s);
+    if (e != cudaSuccess) return e;
+    TcRsArgs ta;
+    std::memset(&ta, 0, sizeof(ta));
+    ta.jg = jg;
+    ta.jg.accumulate = accumulate ? 1 : 0;
+    ta.recs = d_recs;
+    ta.field = d_field;
+    ta.amax = d_amax;
+    ta.left = d_left;
+    ta.error = d_err;
+    ta.tiles_x = tiles_x;
+    ta.tiles_y = tiles_y;
+    ta.p_base = p0;
+    ta.p_count = p1 - p0;
+    ta.ksplit = 1;
+    ta.pps = p1 - p0;
+    count_launches(1);
+    tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTc, s>>>(ta);
+    JobGeom jc = jg;
+    jc.ksplit = 1;
+    jc.points_per_split = p1 - p0;
+    jc.p0 = p0;
+    jc.p1 = p1;
+    jc.accumulate = 1;
+    jc.tc_skip = 1;
+    jc.tc_left = d_left;
+    jc.tc_tiles_x = tiles_x;
+    jc.tc_tiles_y = tiles_y;
+    launch_rs(d_recs, jc, d_field, nullptr, s);
+    return cudaGetLastError();
 }
 
 }  // namespace ophpc

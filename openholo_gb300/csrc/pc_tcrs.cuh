@@ -128,4 +128,16 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
                             const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, int sm_count,
                             cudaStream_t stream, std::string* err);
 
+// Building blocks for callers that run a job as point-range steps (the
+// serving engine). launch_rs_amax: per channel the largest coef / z^2 of the
+// RS records into d_amax[0..n_channels) (zeroed by the caller).
+// launch_tc_rs_range: points [p0, p1) of the records on the tensor cores,
+// overwriting the field (accumulate false) or adding into it, then the
+// CUDA-core complement for the same range; d_left holds n_channels x tiles
+// ints (128x128 tiles) of scratch, *d_err is set on a kernel timeout.
+void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t stream);
+cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1, bool accumulate,
+                               double2* d_field, const float* d_amax, int32_t* d_left, int* d_err,
+                               cudaStream_t stream);
+
 }  // namespace ophpc

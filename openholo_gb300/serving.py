@@ -78,7 +78,7 @@ class Server:
         self._keep: Dict[int, tuple] = {}
 
     def submit(self, geometry: dict, vertices: np.ndarray, diff_flag: int, want_field: bool = True,
-               want_codes: bool = False, encode_flag: int = 0, pinned: bool = False) -> int:
+               want_codes: bool = False, encode_flag: int = 0, pinned: bool = False, mode: int = 0) -> int:
         """geometry: make_config keyword arguments. Returns a ticket."""
         v = np.ascontiguousarray(vertices, dtype=np.float64)
         cfg = make_config(**geometry)
@@ -99,7 +99,7 @@ class Server:
             vptr = v.ctypes.data if v.size else None
             fptr = field.ctypes.data if field is not None else None
             cptr = codes.ctypes.data if codes is not None else None
-        j = JobDesc(cfg=cfg, h_vertices=vptr, n_points=v.shape[0], diff_flag=diff_flag, mode=0,
+        j = JobDesc(cfg=cfg, h_vertices=vptr, n_points=v.shape[0], diff_flag=diff_flag, mode=mode,
                     h_field=fptr, h_codes=cptr, encode_flag=encode_flag)
         t = ctypes.c_uint64()
         st = self._L.ophpc_server_submit(self._h, ctypes.byref(j), ctypes.byref(t))
@@ -109,10 +109,11 @@ class Server:
         return t.value
 
     def submit_raw(self, cfg: OphpcConfig, h_vertices: int, n_points: int, diff_flag: int,
-                   h_field: Optional[int] = None, h_codes: Optional[int] = None, encode_flag: int = 0) -> int:
+                   h_field: Optional[int] = None, h_codes: Optional[int] = None, encode_flag: int = 0,
+                   mode: int = 0) -> int:
         """Submit with caller-owned (ideally page-locked) host buffers given as
         addresses; the caller keeps them alive until the job is waited for."""
-        j = JobDesc(cfg=cfg, h_vertices=h_vertices or None, n_points=n_points, diff_flag=diff_flag, mode=0,
+        j = JobDesc(cfg=cfg, h_vertices=h_vertices or None, n_points=n_points, diff_flag=diff_flag, mode=mode,
                     h_field=h_field or None, h_codes=h_codes or None, encode_flag=encode_flag)
         t = ctypes.c_uint64()
         st = self._L.ophpc_server_submit(self._h, ctypes.byref(j), ctypes.byref(t))

@@ -103,3 +103,39 @@ def test_policies_give_identical_results(gpu_ctx):
         assert np.array_equal(a, b)
     with pytest.raises(OphpcError):
         Server(0, policy=7)
+
+
+def test_tensor_rs_jobs_in_the_mix(gpu_ctx, oracle_mod):
+    """RS jobs submitted with OPHPC_MODE_TENSOR_BF16X3 run as point-range
+    steps of the tensor-core RS kernel, beside FP32-core Fresnel jobs: alone
+    and in the mix bit for bit; against the single-call tensor-core generate
+    within relL2 3e-5 (both ~1e-5 from FP64, with the tensor core's FP32
+    accumulation runs starting at different points); against the FP64 oracle
+    within the parity bar."""
+    from openholo_gb300.serving import Server
+    jobs = _jobs(seed=9, n_jobs=8)
+    modes = [0x200 if d == 0 else 0 for (_, _, d) in jobs]
+    with Server(0, max_in_flight=4, step_ms=0.5) as srv:
+        alone = [srv.wait(srv.submit(g, v, d, mode=m)) for (g, v, d), m in zip(jobs, modes)]
+        tickets = [srv.submit(g, v, d, mode=m) for (g, v, d), m in zip(jobs, modes)]
+        mix = [srv.wait(t) for t in tickets]
+    for (g, v, d), m, a, x in zip(jobs, modes, alone, mix):
+        assert a.status == 0 and x.status == 0
+        assert np.array_equal(a.field, x.field)
+        direct = run_generate(gpu_ctx, g, v, d, m)
+        e = rel_l2(x.field, direct)
+        print(f"diff {d} mode {m:#x}: served vs single call relL2 {e:.2e}")
+        assert e <= (3e-5 if m else 1e-6)
+    g, v, d = jobs[2]   # 17,070 points, RS on the tensor cores
+    og = oracle_mod.Geometry(**{x: g[x] for x in ("pnx", "pny", "ppx", "ppy", "wavelengths")})
+    assert rel_l2(mix[2].field, oracle_mod.generate(og, v, d)) <= 1e-4
+
+
+def test_tensor_modes_rejected_where_not_served(gpu_ctx):
+    from openholo_gb300 import OphpcError
+    from openholo_gb300.serving import Server
+    g, v, _ = _jobs(seed=9, n_jobs=1)[0]
+    with Server(0) as srv:
+        for d, m in ((1, 0x200), (0, 0x100), (1, 0x100)):
+            with pytest.raises(OphpcError):
+                srv.submit(g, v, d, mode=m)
