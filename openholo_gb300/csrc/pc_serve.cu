@@ -17,13 +17,17 @@
 //
 // RS jobs submitted with OPHPC_MODE_TENSOR_BF16X3 run their point-range
 // steps on the tensor-core RS kernel (plus its CUDA-core complement for the
-// same range), sized by its rate.
+// same range); Fresnel jobs with either tensor mode run one channel's chunk
+// of points per step on the tensor-core Fresnel (factor tables + GEMM into
+// FP64 sums, the channel's field written after its last chunk). Steps are
+// sized by each path's rate.
 //
 // A job's result does not depend on what else runs: its chunking is fixed
 // by the job alone and every chunk adds into the FP64 field in order.
 #include "ophpc_serve.h"
 
 #include "pc_common.cuh"
+#include "pc_tc.cuh"
 #include "pc_tcrs.cuh"
 
 #include <algorithm>
@@ -69,9 +73,13 @@ struct ServeJob {
     uint8_t* d_codes = nullptr;
     unsigned long long* d_mm = nullptr;
     bool tc = false;            // RS on the tensor cores (OPHPC_MODE_TENSOR_BF16X3)
-    float* d_amax = nullptr;    // tensor-core RS: per-channel amplitude bound
+    bool tcf = false;           // Fresnel on the tensor cores (either tensor mode)
+    float* d_amax = nullptr;    // tensor cores: per-channel amplitude bound
     int32_t* d_left = nullptr;  // tensor-core RS: per-tile pair counts for the complement
-    int* d_err = nullptr;       // tensor-core RS: kernel timeout word
+    int* d_err = nullptr;       // tensor cores: kernel timeout word
+    double* d_sum = nullptr;    // tensor-core Fresnel: [channel][re plane, im plane] FP64 sums
+    TcFresnelPlan plan{};       // tensor-core Fresnel: factor tables of one step's points
+    int cur_ch = 0;             // tensor-core Fresnel: channel being stepped
     double t_submit = 0, t_admit = 0, t_done = 0;
     double remaining = 0;       // interactions left
     double est_s = 0;           // estimated isolated service time
@@ -117,6 +125,7 @@ struct ophpc_server {
     bool stop = false;
     double rate_rs = 2.0e12, rate_fresnel = 2.6e12;   // interactions/s used to size steps
     double rate_tc_rs = 2.2e13;                        // tensor-core RS
+    double rate_tcf_bf16x3 = 4e13, rate_tcf_fp16 = 9e13;   // tensor-core Fresnel
     int* h_err = nullptr;                              // [slot]: page-locked copies of the jobs' error words
 };
 
@@ -137,9 +146,9 @@ bool job_ok(const ophpc_job* j) {
         if (!(c.wave_length[i] > 0) || c.wave_length[i] >= 2 * c.pixel_pitch[0] || c.wave_length[i] >= 2 * c.pixel_pitch[1])
             return false;
     if (j->diff_flag > 1) return false;
-    // tensor cores: RS with split-BF16 only
-    if (j->mode & OPHPC_MODE_TENSOR_FP16) return false;
-    if ((j->mode & OPHPC_MODE_TENSOR_BF16X3) && j->diff_flag != OPHPC_DIFF_RS) return false;
+    // tensor cores: RS with split-BF16, Fresnel with split-BF16 or FP16
+    if ((j->mode & OPHPC_MODE_TENSOR_FP16) && (j->mode & OPHPC_MODE_TENSOR_BF16X3)) return false;
+    if ((j->mode & OPHPC_MODE_TENSOR_FP16) && j->diff_flag == OPHPC_DIFF_RS) return false;
     if (j->n_points > 0 && !j->h_vertices) return false;
     if (j->n_points > (uint64_t)INT32_MAX) return false;
     if (j->encode_flag > OPHPC_ENCODE_IMAGINARY) return false;
@@ -175,6 +184,20 @@ JobGeom make_job_geom(const ophpc_config* cfg, int64_t n) {
 }
 
 bool uses_tc(const ophpc_job* j) { return j->diff_flag == OPHPC_DIFF_RS && (j->mode & OPHPC_MODE_TENSOR_BF16X3); }
+bool uses_tcf(const ophpc_job* j) {
+    return j->diff_flag == OPHPC_DIFF_FRESNEL && (j->mode & (OPHPC_MODE_TENSOR_BF16X3 | OPHPC_MODE_TENSOR_FP16));
+}
+
+// Points per tensor-core Fresnel step: ~step_ms of GPU time for one
+// channel, a multiple of the tables' K granularity, at most 65,536.
+int64_t tcf_step_points(const ophpc_job* j, double step_ms, double rate) {
+    const double plane = (double)j->cfg.pixel_number[0] * j->cfg.pixel_number[1];
+    const int64_t m = tc_fresnel_chunk_multiple();
+    int64_t kc = (int64_t)(step_ms * 1e-3 * rate / plane);
+    kc = std::max<int64_t>(m, std::min<int64_t>(kc, 65536)) / m * m;
+    const int64_t nup = ((int64_t)j->n_points + m - 1) / m * m;
+    return std::max<int64_t>(m, std::min<int64_t>(kc, nup));
+}
 
 size_t tc_left_bytes(const ophpc_job* j) {
     const size_t tiles = (size_t)((j->cfg.pixel_number[0] + kRsTcTile - 1) / kRsTcTile) *
@@ -182,10 +205,18 @@ size_t tc_left_bytes(const ophpc_job* j) {
     return align256(sizeof(int32_t) * tiles * j->cfg.n_channels);
 }
 
-size_t job_bytes(const ophpc_job* j) {
+size_t tcf_bytes(const ophpc_job* j, int64_t kc) {
+    const size_t px = (size_t)j->cfg.pixel_number[0] * j->cfg.pixel_number[1] * j->cfg.n_channels;
+    return 1024 + tc_fresnel_table_bytes(j->cfg.pixel_number[0], j->cfg.pixel_number[1], (int)kc,
+                                         (j->mode & OPHPC_MODE_TENSOR_BF16X3) != 0) +
+           align256(sizeof(double) * 2 * px);
+}
+
+size_t job_bytes(const ophpc_job* j, int64_t tcf_kc) {
     const size_t px = (size_t)j->cfg.pixel_number[0] * j->cfg.pixel_number[1] * j->cfg.n_channels;
     return align256(sizeof(ophpc_vertex) * j->n_points) + align256(sizeof(PointRec) * j->n_points * j->cfg.n_channels) +
-           align256(sizeof(double2) * px) + align256(px) + 256 + (uses_tc(j) ? 256 + tc_left_bytes(j) : 0);
+           align256(sizeof(double2) * px) + align256(px) + 256 + (uses_tc(j) || uses_tcf(j) ? 256 : 0) +
+           (uses_tc(j) ? tc_left_bytes(j) : 0) + (uses_tcf(j) ? tcf_bytes(j, tcf_kc) : 0);
 }
 
 // Enqueues the job's next step on the stream of its slot at the priority
@@ -197,17 +228,36 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
     const int64_t px = (int64_t)d.cfg.pixel_number[0] * d.cfg.pixel_number[1];
     cudaError_t e = cudaSuccess;
     if (j->stage == 0) {
-        if (j->tc) e = cudaMemsetAsync(j->d_amax, 0, 32, st);   // amax[0..3] and the error word
+        if (j->tc || j->tcf) e = cudaMemsetAsync(j->d_amax, 0, 32, st);   // amax[0..3] and the error word
         if (n > 0) {
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(j->d_v, d.h_vertices, sizeof(ophpc_vertex) * n, cudaMemcpyHostToDevice, st);
             launch_prep(j->d_v, n, d.cfg.scale, d.cfg.distance, d.cfg.field_length, d.cfg.viewing_window,
                         (int)d.diff_flag, j->jg, j->d_recs, st);
             if (j->tc) launch_rs_amax(j->d_recs, n, (int)d.cfg.n_channels, j->d_amax, st);
+            if (j->tcf)
+                for (uint32_t c = 0; c < d.cfg.n_channels; ++c)
+                    launch_tc_fresnel_cmax(j->d_recs + (int64_t)c * n, n, j->d_amax + c, st);
         } else if (e == cudaSuccess) {
             e = cudaMemsetAsync(j->d_field, 0, sizeof(double2) * px * d.cfg.n_channels, st);
         }
         j->stage = n > 0 ? 1 : 2;
+    } else if (j->stage == 1 && j->tcf) {
+        // one chunk of one channel: tables + GEMM into the channel's FP64
+        // sums; the channel's last chunk also writes its field
+        const int c = j->cur_ch;
+        const int64_t k0 = j->next_point, kc = std::min<int64_t>(j->chunk_points, n - k0);
+        double* sre = j->d_sum + (int64_t)c * 2 * px;
+        e = launch_tc_fresnel_chunk(j->plan, j->d_recs + (int64_t)c * n, n, j->jg.ch[c], k0, (int)kc, j->d_amax + c,
+                                    sre, sre + px, k0 > 0, j->d_err, st);
+        j->remaining -= (double)kc * px;
+        j->next_point = k0 + kc;
+        if (j->next_point >= n) {
+            launch_tc_fresnel_finalize(sre, sre + px, j->d_amax + c, px,
+                                       reinterpret_cast<double2*>(j->d_field) + (int64_t)c * px, st);
+            j->next_point = 0;
+            if (++j->cur_ch >= (int)d.cfg.n_channels) j->stage = 2;
+        }
     } else if (j->stage == 1) {
         JobGeom g = j->jg;
         g.p0 = j->next_point;
@@ -233,7 +283,7 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
         }
         if (d.h_field && e == cudaSuccess)
             e = cudaMemcpyAsync(d.h_field, j->d_field, sizeof(double2) * px * d.cfg.n_channels, cudaMemcpyDeviceToHost, st);
-        if (j->tc && e == cudaSuccess)
+        if ((j->tc || j->tcf) && e == cudaSuccess)
             e = cudaMemcpyAsync(&s->h_err[j->slot], j->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
         j->stage = 3;
     }
@@ -271,13 +321,24 @@ bool admit(ophpc_server* s, ServeJob* j) {
     j->d_codes = q;
     q += align256(px);
     j->d_mm = (unsigned long long*)q;
-    if (j->tc) {
+    if (j->tc || j->tcf) {
         q += 256;
         j->d_amax = (float*)q;   // [4] floats, then the error word
         j->d_err = (int*)(q + 16);
         q += 256;
-        j->d_left = (int32_t*)q;
         s->h_err[j->slot] = 0;
+    }
+    if (j->tc) j->d_left = (int32_t*)q;
+    if (j->tcf) {
+        unsigned char* tq = (unsigned char*)(((uintptr_t)q + 1023) & ~(uintptr_t)1023);
+        const size_t tb = tc_fresnel_table_bytes(d.cfg.pixel_number[0], d.cfg.pixel_number[1], (int)j->chunk_points,
+                                                 (d.mode & OPHPC_MODE_TENSOR_BF16X3) != 0);
+        if (!tc_fresnel_plan(&j->plan, tq, d.cfg.pixel_number[0], d.cfg.pixel_number[1], (int)j->chunk_points,
+                             (d.mode & OPHPC_MODE_TENSOR_BF16X3) != 0)) {
+            j->status = OPHPC_ERROR_UNSUPPORTED;
+            j->stage = 3;
+        }
+        j->d_sum = (double*)(tq + tb);
     }
     s->mem_in_use += j->bytes;
     j->t_admit = now_s(s);
@@ -430,15 +491,19 @@ ophpc_status ophpc_server_submit(ophpc_server* s, const ophpc_job* job, uint64_t
     if (!job_ok(job)) return OPHPC_ERROR_INVALID_ARGUMENT;
     std::unique_ptr<ServeJob> j(new ServeJob());
     j->desc = *job;
-    j->bytes = job_bytes(job);
+    j->tc = uses_tc(job);
+    j->tcf = uses_tcf(job);
+    const double tcf_rate = (job->mode & OPHPC_MODE_TENSOR_BF16X3) ? s->rate_tcf_bf16x3 : s->rate_tcf_fp16;
+    const int64_t tcf_kc = j->tcf ? tcf_step_points(job, s->opt.step_ms, tcf_rate) : 0;
+    j->bytes = job_bytes(job, tcf_kc);
     if (j->bytes > s->opt.memory_budget) return OPHPC_ERROR_OUT_OF_MEMORY;
     j->jg = make_job_geom(&job->cfg, (int64_t)job->n_points);
     const double px = (double)job->cfg.pixel_number[0] * job->cfg.pixel_number[1] * job->cfg.n_channels;
-    j->tc = uses_tc(job);
-    const double rate = j->tc ? s->rate_tc_rs : (job->diff_flag == OPHPC_DIFF_RS ? s->rate_rs : s->rate_fresnel);
+    const double rate = j->tc ? s->rate_tc_rs
+                              : j->tcf ? tcf_rate : (job->diff_flag == OPHPC_DIFF_RS ? s->rate_rs : s->rate_fresnel);
     int64_t cp = (int64_t)(s->opt.step_ms * 1e-3 * rate / px);
     cp = std::max<int64_t>(kChunk, cp / kChunk * kChunk);
-    j->chunk_points = cp;
+    j->chunk_points = j->tcf ? tcf_kc : cp;
     j->remaining = (double)job->n_points * px;
     const double copy_bytes = (double)sizeof(ophpc_vertex) * job->n_points +
                               (job->h_codes ? px : 0.0) + (job->h_field ? 16.0 * px : 0.0);

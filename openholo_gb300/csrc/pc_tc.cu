@@ -409,6 +409,100 @@ size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
 }  // namespace
 
+static_assert(sizeof(GemmMaps) <= sizeof(((TcFresnelPlan*)nullptr)->maps), "tensor maps fit the plan");
+
+size_t tc_fresnel_table_bytes(int pnX, int pnY, int ld, bool split) {
+    const size_t plane_a = align_up((size_t)pnY * ld * 2, 1024), plane_b = align_up((size_t)pnX * ld * 2, 1024);
+    return (2 * plane_a + 2 * plane_b) * (split ? 2 : 1);
+}
+
+int tc_fresnel_chunk_multiple() { return kBK; }
+
+bool tc_fresnel_plan(TcFresnelPlan* plan, void* table_mem, int pnX, int pnY, int ld, bool split) {
+    if (!encode_fn() || ld <= 0 || ld % kBK != 0) return false;
+    std::memset(plan, 0, sizeof(*plan));
+    plan->pnX = pnX;
+    plan->pnY = pnY;
+    plan->ld = ld;
+    plan->split = split;
+    const size_t plane_a = align_up((size_t)pnY * ld * 2, 1024), plane_b = align_up((size_t)pnX * ld * 2, 1024);
+    unsigned char* q = static_cast<unsigned char*>(table_mem);
+    for (int p = 0; p < (split ? 2 : 1); ++p) {
+        plan->ar[p] = q; q += plane_a;
+        plan->ai[p] = q; q += plane_a;
+        plan->br[p] = q; q += plane_b;
+        plan->bi[p] = q; q += plane_b;
+    }
+    GemmMaps* maps = reinterpret_cast<GemmMaps*>(plan->maps);
+    // pass p: (A plane, B plane) = (hi, hi), (hi, lo), (lo, hi)
+    const int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};
+    bool ok = true;
+    for (int p = 0; p < (split ? 3 : 1); ++p) {
+        ok = ok && make_map(&maps->ar[p], plan->ar[pa[p]], pnY, ld, split) &&
+             make_map(&maps->ai[p], plan->ai[pa[p]], pnY, ld, split) &&
+             make_map(&maps->br[p], plan->br[pb[p]], pnX, ld, split) &&
+             make_map(&maps->bi[p], plan->bi[pb[p]], pnX, ld, split);
+    }
+    return ok;
+}
+
+void launch_tc_fresnel_cmax(const PointRec* d_recs_ch, int64_t n_points, float* d_cmax, cudaStream_t s) {
+    count_launches(1);
+    cmax_kernel<<<256, 256, 0, s>>>(d_recs_ch, n_points, d_cmax);
+}
+
+cudaError_t launch_tc_fresnel_chunk(const TcFresnelPlan& plan, const PointRec* d_recs_ch, int64_t n_points,
+                                    const ChannelGeom& g, int64_t k0, int kc, const float* d_cmax, double* sum_re,
+                                    double* sum_im, bool accumulate, int* d_err, cudaStream_t s) {
+    // per call: the attribute belongs to the current device
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem);
+    if (e != cudaSuccess) return e;
+    TableArgs ta;
+    std::memset(&ta, 0, sizeof(ta));
+    ta.n_points = n_points;
+    ta.k0 = k0;
+    ta.kc = std::min(kc, plan.ld);
+    ta.ld = plan.ld;
+    ta.rows_a = plan.pnY;
+    ta.rows_b = plan.pnX;
+    ta.split = plan.split ? 1 : 0;
+    ta.g = g;
+    ta.cmax = d_cmax;
+    for (int p = 0; p < 2; ++p) {
+        ta.ar[p] = plan.ar[p];
+        ta.ai[p] = plan.ai[p];
+        ta.br[p] = plan.br[p];
+        ta.bi[p] = plan.bi[p];
+    }
+    const int segs = (plan.pnY + kSeg - 1) / kSeg + (plan.pnX + kSeg - 1) / kSeg;
+    const dim3 tgrid((unsigned)((plan.ld + kTablePoints - 1) / kTablePoints), (unsigned)segs);
+    count_launches(2);
+    if (plan.split)
+        tc_table_kernel<__nv_bfloat16><<<tgrid, kTablePoints, 0, s>>>(d_recs_ch, ta);
+    else
+        tc_table_kernel<__half><<<tgrid, kTablePoints, 0, s>>>(d_recs_ch, ta);
+    GemmArgs ga;
+    ga.num_kb = plan.ld / kBK;
+    ga.passes = plan.split ? 3 : 1;
+    ga.pnX = plan.pnX;
+    ga.pnY = plan.pnY;
+    ga.accumulate = accumulate ? 1 : 0;
+    ga.idesc = make_idesc(plan.split ? 1u : 0u, false);
+    ga.idesc_neg = make_idesc(plan.split ? 1u : 0u, true);
+    ga.sum_re = sum_re;
+    ga.sum_im = sum_im;
+    ga.error = d_err;
+    const dim3 ggrid((unsigned)((plan.pnX + kBN - 1) / kBN), (unsigned)((plan.pnY + kBM - 1) / kBM));
+    tc_gemm_kernel<<<ggrid, kGemmThreads, kGemmSmem, s>>>(*reinterpret_cast<const GemmMaps*>(plan.maps), ga);
+    return cudaGetLastError();
+}
+
+void launch_tc_fresnel_finalize(const double* sum_re, const double* sum_im, const float* d_cmax, int64_t plane,
+                                double2* d_field_ch, cudaStream_t s) {
+    count_launches(1);
+    tc_finalize_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, s>>>(sum_re, sum_im, d_cmax, plane, d_field_ch);
+}
+
 ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                                  uint64_t n_points, uint32_t mode, double* d_field, cudaStream_t s,
                                  std::string* err) {
@@ -418,10 +512,6 @@ ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, co
     };
     const bool split = (mode & OPHPC_MODE_TENSOR_BF16X3) != 0;
     if (!encode_fn()) return fail(OPHPC_ERROR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
-    // per call: the attribute belongs to the current device
-    if (cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem) !=
-        cudaSuccess)
-        return fail(OPHPC_ERROR_CUDA, "cudaFuncSetAttribute(tc_gemm_kernel) failed");
     const int pnX = cfg->pixel_number[0], pnY = cfg->pixel_number[1];
     const int64_t plane = (int64_t)pnX * pnY;
     const int nch = (int)cfg->n_channels;
@@ -450,16 +540,13 @@ ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, co
     }
 
     // chunk of points per table build: tables of at most ~2 GiB
-    const size_t elem = 2;
-    const size_t per_point = (size_t)(pnX + pnY) * 2 * elem * (split ? 2 : 1);
+    const size_t per_point = (size_t)(pnX + pnY) * 2 * 2 * (split ? 2 : 1);
     int64_t kc = (int64_t)((size_t)2 << 30) / (int64_t)per_point;
     kc = std::max<int64_t>(kBK, std::min<int64_t>(kc, 65536));
     kc = kc / kBK * kBK;
     kc = std::min<int64_t>(kc, (int64_t)align_up(n_points, kBK));
     const int ld = (int)kc;
-    const size_t plane_a = align_up((size_t)pnY * ld * elem, 1024), plane_b = align_up((size_t)pnX * ld * elem, 1024);
-    const int nplanes = split ? 2 : 1;
-    const size_t table_bytes = (2 * plane_a + 2 * plane_b) * nplanes;
+    const size_t table_bytes = tc_fresnel_table_bytes(pnX, pnY, ld, split);
     const size_t rec_bytes = sizeof(PointRec) * n_points * nch;
     const size_t sum_bytes = sizeof(double) * plane * 2;
 
@@ -470,86 +557,33 @@ ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, co
     unsigned char* q = buf;
     PointRec* recs = (PointRec*)q;
     q += align_up(rec_bytes, 1024);
-    void *ar[2] = {nullptr, nullptr}, *ai[2] = {nullptr, nullptr}, *br[2] = {nullptr, nullptr},
-         *bi[2] = {nullptr, nullptr};
-    for (int p = 0; p < nplanes; ++p) {
-        ar[p] = q; q += plane_a;
-        ai[p] = q; q += plane_a;
-        br[p] = q; q += plane_b;
-        bi[p] = q; q += plane_b;
-    }
+    TcFresnelPlan plan;
+    const bool planned = tc_fresnel_plan(&plan, q, pnX, pnY, ld, split);
+    q += table_bytes;
     double* sre = (double*)q;
     double* sim = sre + plane;
     q += align_up(sum_bytes, 1024);
     float* cmax = (float*)q;
     int* errw = (int*)(q + 16);
-
-    GemmMaps maps;
-    std::memset(&maps, 0, sizeof(maps));
-    // pass p: (A plane, B plane) = (hi, hi), (hi, lo), (lo, hi)
-    const int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};
-    const int passes = split ? 3 : 1;
-    bool ok = true;
-    for (int p = 0; p < passes; ++p) {
-        ok = ok && make_map(&maps.ar[p], ar[pa[p]], pnY, ld, split) && make_map(&maps.ai[p], ai[pa[p]], pnY, ld, split) &&
-             make_map(&maps.br[p], br[pb[p]], pnX, ld, split) && make_map(&maps.bi[p], bi[pb[p]], pnX, ld, split);
-    }
-    if (!ok) {
+    if (!planned) {
         cudaFreeAsync(buf, s);
         return fail(OPHPC_ERROR_CUDA, "tensor map encoding failed");
     }
     cudaMemsetAsync(errw, 0, sizeof(int), s);
     launch_prep(d_vertices, (int64_t)n_points, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window, 1,
                 jg, recs, s);
-    const dim3 ggrid((unsigned)((pnX + kBN - 1) / kBN), (unsigned)((pnY + kBM - 1) / kBM));
-    const int segs = (pnY + kSeg - 1) / kSeg + (pnX + kSeg - 1) / kSeg;
-    for (int c = 0; c < nch; ++c) {
+    cudaError_t e = cudaSuccess;
+    for (int c = 0; c < nch && e == cudaSuccess; ++c) {
         const PointRec* crec = recs + (int64_t)c * n_points;
         cudaMemsetAsync(cmax, 0, sizeof(float), s);
-        count_launches(1);
-        cmax_kernel<<<256, 256, 0, s>>>(crec, (int64_t)n_points, cmax);
-        for (int64_t k0 = 0; k0 < (int64_t)n_points; k0 += kc) {
-            TableArgs ta;
-            std::memset(&ta, 0, sizeof(ta));
-            ta.n_points = (int64_t)n_points;
-            ta.k0 = k0;
-            ta.kc = (int)std::min<int64_t>(kc, (int64_t)n_points - k0);
-            ta.ld = ld;
-            ta.rows_a = pnY;
-            ta.rows_b = pnX;
-            ta.split = split ? 1 : 0;
-            ta.g = jg.ch[c];
-            ta.cmax = cmax;
-            for (int p = 0; p < 2; ++p) {
-                ta.ar[p] = ar[p];
-                ta.ai[p] = ai[p];
-                ta.br[p] = br[p];
-                ta.bi[p] = bi[p];
-            }
-            const dim3 tgrid((unsigned)((ld + kTablePoints - 1) / kTablePoints), (unsigned)segs);
-            count_launches(2);
-            if (split)
-                tc_table_kernel<__nv_bfloat16><<<tgrid, kTablePoints, 0, s>>>(crec, ta);
-            else
-                tc_table_kernel<__half><<<tgrid, kTablePoints, 0, s>>>(crec, ta);
-            GemmArgs ga;
-            ga.num_kb = ld / kBK;
-            ga.passes = passes;
-            ga.pnX = pnX;
-            ga.pnY = pnY;
-            ga.accumulate = k0 > 0 ? 1 : 0;
-            ga.idesc = make_idesc(split ? 1u : 0u, false);
-            ga.idesc_neg = make_idesc(split ? 1u : 0u, true);
-            ga.sum_re = sre;
-            ga.sum_im = sim;
-            ga.error = errw;
-            tc_gemm_kernel<<<ggrid, kGemmThreads, kGemmSmem, s>>>(maps, ga);
-        }
-        count_launches(1);
-        tc_finalize_kernel<<<(unsigned)((plane + 255) / 256), 256, 0, s>>>(sre, sim, cmax, plane,
-                                                                           (double2*)d_field + (int64_t)c * plane);
+        launch_tc_fresnel_cmax(crec, (int64_t)n_points, cmax, s);
+        for (int64_t k0 = 0; k0 < (int64_t)n_points && e == cudaSuccess; k0 += kc)
+            e = launch_tc_fresnel_chunk(plan, crec, (int64_t)n_points, jg.ch[c], k0,
+                                        (int)std::min<int64_t>(kc, (int64_t)n_points - k0), cmax, sre, sim, k0 > 0, errw,
+                                        s);
+        launch_tc_fresnel_finalize(sre, sim, cmax, plane, (double2*)d_field + (int64_t)c * plane, s);
     }
-    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     int herr = 0;
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);

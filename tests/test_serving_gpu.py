@@ -105,16 +105,17 @@ def test_policies_give_identical_results(gpu_ctx):
         Server(0, policy=7)
 
 
-def test_tensor_rs_jobs_in_the_mix(gpu_ctx, oracle_mod):
-    """RS jobs submitted with OPHPC_MODE_TENSOR_BF16X3 run as point-range
-    steps of the tensor-core RS kernel, beside FP32-core Fresnel jobs: alone
+def test_tensor_core_jobs_in_the_mix(gpu_ctx, oracle_mod):
+    """Jobs submitted with OPHPC_MODE_TENSOR_BF16X3 run as steps on the tensor
+    cores (RS: point ranges of the tensor-core RS; Fresnel: one channel's
+    chunk of factor tables + GEMM per step), mixed with FP32-core jobs: alone
     and in the mix bit for bit; against the single-call tensor-core generate
-    within relL2 3e-5 (both ~1e-5 from FP64, with the tensor core's FP32
-    accumulation runs starting at different points); against the FP64 oracle
+    within relL2 3e-5 (both ~1e-5 from FP64; the tensor core's FP32
+    accumulation runs start at other points); against the FP64 oracle
     within the parity bar."""
     from openholo_gb300.serving import Server
     jobs = _jobs(seed=9, n_jobs=8)
-    modes = [0x200 if d == 0 else 0 for (_, _, d) in jobs]
+    modes = [0x200 if k % 4 != 3 else 0 for k in range(len(jobs))]
     with Server(0, max_in_flight=4, step_ms=0.5) as srv:
         alone = [srv.wait(srv.submit(g, v, d, mode=m)) for (g, v, d), m in zip(jobs, modes)]
         tickets = [srv.submit(g, v, d, mode=m) for (g, v, d), m in zip(jobs, modes)]
@@ -124,11 +125,23 @@ def test_tensor_rs_jobs_in_the_mix(gpu_ctx, oracle_mod):
         assert np.array_equal(a.field, x.field)
         direct = run_generate(gpu_ctx, g, v, d, m)
         e = rel_l2(x.field, direct)
-        print(f"diff {d} mode {m:#x}: served vs single call relL2 {e:.2e}")
+        print(f"diff {d} mode {m:#x} ({v.shape[0]} points): served vs single call relL2 {e:.2e}")
         assert e <= (3e-5 if m else 1e-6)
-    g, v, d = jobs[2]   # 17,070 points, RS on the tensor cores
-    og = oracle_mod.Geometry(**{x: g[x] for x in ("pnx", "pny", "ppx", "ppy", "wavelengths")})
-    assert rel_l2(mix[2].field, oracle_mod.generate(og, v, d)) <= 1e-4
+    for k in (1, 2):   # Fresnel (625 points) and RS (17,070 points) on the tensor cores
+        g, v, d = jobs[k]
+        og = oracle_mod.Geometry(**{x: g[x] for x in ("pnx", "pny", "ppx", "ppy", "wavelengths")})
+        assert rel_l2(mix[k].field, oracle_mod.generate(og, v, d)) <= 1e-4
+
+
+def test_tensor_fresnel_fp16_served(gpu_ctx):
+    """FP16 tensor-core Fresnel (one product, ~2.5e-4 from FP64) through the
+    server equals its single-call result within the FP16 tolerance."""
+    from openholo_gb300.serving import Server
+    g, v, d = [j for j in _jobs(seed=9, n_jobs=8) if j[2] == 1][0]
+    with Server(0, step_ms=0.2) as srv:
+        r = srv.wait(srv.submit(g, v, d, mode=0x100))
+    assert r.status == 0
+    assert rel_l2(r.field, run_generate(gpu_ctx, g, v, d, 0)) <= 1e-3
 
 
 def test_tensor_modes_rejected_where_not_served(gpu_ctx):
@@ -136,6 +149,6 @@ def test_tensor_modes_rejected_where_not_served(gpu_ctx):
     from openholo_gb300.serving import Server
     g, v, _ = _jobs(seed=9, n_jobs=1)[0]
     with Server(0) as srv:
-        for d, m in ((1, 0x200), (0, 0x100), (1, 0x100)):
+        for d, m in ((0, 0x100), (0, 0x300), (1, 0x300)):
             with pytest.raises(OphpcError):
                 srv.submit(g, v, d, mode=m)
