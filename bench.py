@@ -240,7 +240,7 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
     import torch
 
     from openholo_gb300 import make_config, workloads
-    from openholo_gb300.serving import POLICY_DEADLINE, POLICY_SHORTEST_REMAINING, Server
+    from openholo_gb300.serving import POLICY_DEADLINE, POLICY_EARLIEST_DEADLINE, POLICY_SHORTEST_REMAINING, Server
 
     jobs = workloads.serving_stream(n_jobs, rate_per_s=1.0, seed=seed, max_points=max_points)
     prepared = []
@@ -298,6 +298,8 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
             out["loads"][f"{load:.2f}"] = run_load(srv, load, mean_s)
     with Server(0, max_in_flight=16, step_ms=2.0, policy=POLICY_SHORTEST_REMAINING) as srv:
         out["shortest_remaining_0.80"] = run_load(srv, 0.8, mean_s)
+    with Server(0, max_in_flight=16, step_ms=2.0, policy=POLICY_EARLIEST_DEADLINE) as srv:
+        out["earliest_deadline_0.80"] = run_load(srv, 0.8, mean_s)
     return out
 
 

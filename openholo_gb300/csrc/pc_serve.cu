@@ -52,6 +52,7 @@ using Clock = std::chrono::steady_clock;
 constexpr int kPrioLevels = 6;   // CUDA exposes six stream priorities on this GPU family
 constexpr double kDeadlineFactor = 2.0;
 constexpr double kShortJobS = 20e-3;     // estimated isolated time below which a job goes first
+constexpr double kEdfSlackS = 20e-3;     // added to every deadline under OPHPC_SERVE_EARLIEST_DEADLINE
 constexpr double kJobFixedS = 3e-3;      // per-job launch, sync and bookkeeping time
 constexpr double kCopyBytesPerS = 20e9;  // host <-> device copies, page-locked
 
@@ -84,6 +85,7 @@ struct ServeJob {
     double remaining = 0;       // interactions left
     double est_s = 0;           // estimated isolated service time
     double deadline = 0;        // t_submit + kDeadlineFactor * est_s
+    double edf_deadline = 0;    // deadline + kEdfSlackS (OPHPC_SERVE_EARLIEST_DEADLINE)
     ophpc_status status = OPHPC_SUCCESS;
     bool finished = false;
 };
@@ -96,6 +98,7 @@ size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 // remaining work first.
 bool before(uint32_t policy, const ServeJob* a, const ServeJob* b) {
     if (policy == OPHPC_SERVE_SHORTEST_REMAINING) return a->remaining < b->remaining;
+    if (policy == OPHPC_SERVE_EARLIEST_DEADLINE) return a->edf_deadline < b->edf_deadline;
     const bool sa = a->est_s < kShortJobS, sb = b->est_s < kShortJobS;
     if (sa != sb) return sa;
     return sa ? a->remaining < b->remaining : a->deadline < b->deadline;
@@ -361,7 +364,7 @@ void worker_main(ophpc_server* s) {
         const uint32_t pol = s->opt.policy;
         while (!s->queue.empty()) {
             auto it = s->queue.begin();   // shortest-remaining: arrival order
-            if (pol == OPHPC_SERVE_DEADLINE)
+            if (pol != OPHPC_SERVE_SHORTEST_REMAINING)
                 it = std::min_element(s->queue.begin(), s->queue.end(),
                                       [pol](const ServeJob* a, const ServeJob* b) { return before(pol, a, b); });
             ServeJob* j = *it;
@@ -447,7 +450,7 @@ ophpc_status ophpc_server_create(int32_t device, const ophpc_server_options* opt
     s->device = device;
     if (options) s->opt = *options;
     if (s->opt.max_in_flight == 0) s->opt.max_in_flight = 16;
-    if (s->opt.policy > OPHPC_SERVE_SHORTEST_REMAINING) return OPHPC_ERROR_INVALID_ARGUMENT;
+    if (s->opt.policy > OPHPC_SERVE_EARLIEST_DEADLINE) return OPHPC_ERROR_INVALID_ARGUMENT;
     if (s->opt.step_ms <= 0) s->opt.step_ms = 2.0;
     if (s->opt.reserve_bytes == 0) s->opt.reserve_bytes = (size_t)512 << 20;
     if (s->opt.memory_budget == 0) {
@@ -517,6 +520,7 @@ ophpc_status ophpc_server_submit(ophpc_server* s, const ophpc_job* job, uint64_t
     j->ticket = s->next_ticket++;
     j->t_submit = now_s(s);
     j->deadline = j->t_submit + kDeadlineFactor * j->est_s;
+    j->edf_deadline = j->deadline + kEdfSlackS;
     *ticket = j->ticket;
     s->queue.push_back(j.get());
     s->jobs.emplace(j->ticket, std::move(j));

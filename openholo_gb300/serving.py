@@ -11,6 +11,7 @@ from ._abi import OphpcConfig, OphpcError, lib, make_config
 
 POLICY_DEADLINE = 0
 POLICY_SHORTEST_REMAINING = 1
+POLICY_EARLIEST_DEADLINE = 2
 
 
 class ServerOptions(ctypes.Structure):
