@@ -16,9 +16,11 @@
 // a complex rank-2 update per point. The tile's field is then the complex
 // contraction D = sum_j A_j B_j^T over the points, run on the tensor cores:
 //
-//   warps 0-7   producers: per (point, tile) record in FP64 (frac(tau) is the
-//               only FP64 step; k r reaches ~6e6 rad), formed for the next
-//               chunk of 256 points one warp at a time; per stage of 16
+//   warps 9-11  per (point, tile) records of the next chunk of 256 points
+//               (FP64 for frac(tau) only; k r reaches ~6e6 rad) into a
+//               double-buffered record ring, off the stage pipeline's
+//               critical path;
+//   warps 0-7   producers: per stage of 16
 //               points threads 0-127 write the row factors A (one row each)
 //               and threads 128-255 the column factors B (one column each)
 //               into shared memory in the UMMA K-major 32-byte-swizzle
@@ -60,7 +62,9 @@ using namespace tc5;
 constexpr int kProdWarps = 8;                            // factor producers (and drains)
 constexpr int kProducers = 32 * kProdWarps;              // 256: rows 0-127, then columns 0-127
 constexpr int kMmaWarp = kProdWarps;                     // warp 8: TMEM allocation, MMA issue
-constexpr int kThreadsTc = kProducers + 32;
+constexpr int kRecWarps = 3;                             // warps 9-11: point records
+constexpr int kRecThreads = 32 * kRecWarps;
+constexpr int kThreadsTc = kProducers + 32 + kRecThreads;   // 384: 12 warps, 168 registers each
 constexpr int kStagePts = 16;                            // points per stage: one K=16 MMA step
 constexpr int kStagesTc = 3;
 constexpr int kPlane = kRsTcTile * kStagePts * 2;        // 4096 B: 128 rows x 32 B
@@ -87,8 +91,7 @@ struct __align__(16) TcRsPair {
 };
 static_assert(sizeof(TcRsPair) == 64, "TcRsPair size");
 
-constexpr size_t kSmemTc =
-    1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsPair) * kChunkTc + sizeof(PointRec) * kChunkTc + 512;
+constexpr size_t kSmemTc = 1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsPair) * kChunkTc + 512;
 static_assert(kSmemTc <= 232448, "shared memory per CTA");
 
 struct TcRsArgs {
@@ -110,15 +113,7 @@ struct TcRsArgs {
     double2* partials;
 };
 
-// 16-byte asynchronous global -> shared copy (the copying thread sees the
-// data after cp.async.wait_all).
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void* src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, %0;" ::"n"(kProducers) : "memory"); }
 __device__ __forceinline__ void st_v4(uint32_t addr, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3) {
     asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(w0), "r"(w1), "r"(w2), "r"(w3)
                  : "memory");
@@ -384,19 +379,20 @@ __device__ __forceinline__ void make_record(TcRsPair* buf, int t, bool valid, co
 // One CTA per 128x128 tile of one channel. Warps 0-7 produce the factors
 // (threads 0-127 the rows, 128-255 the columns, all 16 points of a stage
 // each) and drain the accumulator; warp 8 allocates TMEM and its lane 0
-// issues the MMAs. The next chunk's point records are formed one producer
-// warp at a time during the current chunk (double-buffered).
+// issues the MMAs; warps 9-11 form the point records of the chunks, one
+// chunk ahead of the producers (double-buffered, an mbarrier pair per buffer).
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     TcRsPair* s_rec = reinterpret_cast<TcRsPair*>(base + kStagesTc * kStageBytesTc);   // [2][kChunkTc / 2]
-    PointRec* s_pts = reinterpret_cast<PointRec*>(s_rec + kChunkTc);   // next chunk's points, prefetched
-    uint64_t* full = reinterpret_cast<uint64_t*>(s_pts + kChunkTc);
+    uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
     uint64_t* empty = full + kStagesTc;
     uint64_t* acc_full = empty + kStagesTc;   // MMA -> drains: D holds a finished run
     uint64_t* acc_empty = acc_full + 1;       // drains -> MMA: D was read
     uint64_t* drain_bar = acc_empty + 1;      // abort path: issued MMAs complete
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain_bar + 1);
+    uint64_t* rec_full = drain_bar + 1;       // [2] record warps -> producers: a chunk's records are formed
+    uint64_t* rec_empty = rec_full + 2;       // [2] producers -> record warps: a chunk's records were read
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(rec_empty + 2);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
 
@@ -420,6 +416,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
         mbar_init(acc_full, 1);
         mbar_init(acc_empty, kProdWarps);
         mbar_init(drain_bar, 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&rec_full[b], kRecWarps);
+            mbar_init(&rec_empty[b], kProdWarps);
+        }
         *abort = 0;
         *s_left = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -442,10 +442,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     bool wrote = part == 0 && a.jg.accumulate != 0;
     int left = 0, drained = 0, issued = 0;
 
-    if (warp < kProdWarps) {   // chunk 0
-        const bool valid = t < n;
-        make_record(s_rec, t, valid, chrec[valid ? t : 0], tile, g.inv_lambda, inv_amax, X0, Y0, left);
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -463,41 +459,43 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                 }
             }
         }
-    } else {
-        const uint32_t my_pt = smem_u32(&s_pts[t]);
-        for (int c = 0; c < nchunks; ++c) {
-            const TcRsPair* rb = s_rec + (c & 1) * (kChunkTc / 2);
-            // prefetch this thread's point of the next chunk
-            const int64_t nidx = (int64_t)(c + 1) * kChunkTc + t;
-            const bool nvalid = c + 1 < nchunks && nidx < n;
-            if (nvalid) {
-#pragma unroll
-                for (int q = 0; q < 4; ++q) cp_async16(my_pt + 16u * q, reinterpret_cast<const char*>(chrec + nidx) + 16 * q);
+    } else if (warp > kMmaWarp) {
+        // records of chunk c into buffer c & 1, once the producers released
+        // the chunk that used it before (c - 2)
+        const int rt = t - (kProducers + 32);
+        for (int c = 0; c < nchunks && !dead; ++c) {
+            const int b = c & 1;
+            if (c >= 2) {
+                const bool ok = mbar_wait_for(&rec_empty[b], (uint32_t)((c >> 1) - 1) & 1u, abort, kWaitNs);
+                dead = !__all_sync(0xffffffffu, ok);
+                if (dead) break;
             }
-            cp_async_commit();
+            TcRsPair* buf = s_rec + b * (kChunkTc / 2);
+            for (int j = rt; j < kChunkTc; j += kRecThreads) {
+                const int64_t idx = (int64_t)c * kChunkTc + j;
+                const bool valid = idx < n;
+                make_record(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda, inv_amax, X0, Y0, left);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&rec_full[b]);
+        }
+        const int wl = __reduce_add_sync(0xffffffffu, left);
+        if (lane == 0 && wl) atomicAdd(s_left, wl);
+    } else {
+        for (int c = 0; c < nchunks && !dead; ++c) {
+            const int b = c & 1;
+            // every lane waits: each one acquires the record warps' stores
+            const bool rok = mbar_wait_for(&rec_full[b], (uint32_t)(c >> 1) & 1u, abort, kWaitNs);
+            dead = !__all_sync(0xffffffffu, rok);
+            if (dead) break;
+            const TcRsPair* rb = s_rec + b * (kChunkTc / 2);
             const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
             for (int it = it0; it < it1; ++it) {
-                // a run is drained (by every producer warp) before any of them
-                // fills the first stage of the next, so the MMA warp finds D
-                // free when it gets there
-                if (!dead && (it % kPeriod) == 0 && it > 0) {
-                    dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out, X0,
-                                      Y0, amax, wrote);
-                    ++drained;
-                }
-                // this warp's 32 records of the next chunk, at its own stage
-                if (c + 1 < nchunks && it - it0 == 2 * warp) {
-                    cp_async_wait_all();
-                    make_record(s_rec + ((c + 1) & 1) * (kChunkTc / 2), t, nvalid && !dead, s_pts[t], tile,
-                                g.inv_lambda, inv_amax, X0, Y0, left);
-                }
                 const int s = it % kStagesTc;
-                if (!dead) {
-                    bool ok = true;
-                    if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, kWaitNs);
-                    dead = !__shfl_sync(0xffffffffu, ok, 0);
-                }
-                if (dead) continue;
+                bool ok = true;
+                if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, kWaitNs);
+                dead = !__shfl_sync(0xffffffffu, ok, 0);
+                if (dead) break;
                 const uint32_t sb = smem_u32(base + s * kStageBytesTc);
                 const TcRsPair* recs16 = rb + ((it - it0) * kStagePts) / 2;
                 if (side_a) produce16<true>(recs16, off, off2, sb + row_off0, sb + row_off1);
@@ -505,15 +503,23 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                 fence_async_smem();   // generic-proxy writes -> visible to the tensor core
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[s]);
+                // the previous run is drained (by every producer warp) once
+                // the first stage of the next one is filled: the MMA warp
+                // needs D free only to issue that stage
+                if ((it % kPeriod) == 0 && it > 0) {
+                    dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out, X0,
+                                      Y0, amax, wrote);
+                    ++drained;
+                    if (dead) break;
+                }
             }
-            producers_sync();   // the next chunk's records are complete; this chunk's are no longer read
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&rec_empty[b]);   // this chunk's records are no longer read
         }
         // the runs not drained yet (the last one flushes into the field)
         for (int p = drained; p < periods && !dead; ++p)
             dead = !drain_run(p, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out, X0, Y0, amax,
                               wrote);
-        const int wl = __reduce_add_sync(0xffffffffu, left);
-        if (lane == 0 && wl) atomicAdd(s_left, wl);
     }
     tc_fence_before();
     __syncthreads();
