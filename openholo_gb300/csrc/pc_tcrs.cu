@@ -21,8 +21,8 @@
 //               double-buffered record ring, off the stage pipeline's
 //               critical path;
 //   warps 0-7   producers: per stage of 16
-//               points threads 0-127 write the row factors A (one row each)
-//               and threads 128-255 the column factors B (one column each)
+//               points threads 0-127 write the row factors A (two rows x 8
+//               points each) and threads 128-255 the column factors B
 //               into shared memory in the UMMA K-major 32-byte-swizzle
 //               layout: split-BF16 (hi + lo) for R and C, FP16 for the cross
 //               pair;
@@ -142,20 +142,24 @@ __device__ __forceinline__ uint32_t h2v(f2::v2 v) {
     return h2(a, b);
 }
 
-// Factors of the 16 points of a stage (8 record pairs) for this thread's
-// row (SIDE_A) or column, written as the row's two 16-byte chunks of every
-// plane of the stage (ro0: points 0-7, ro1: points 8-15). Two points at a
-// time in packed FP32 pairs.
+// Factors of 8 points of a stage (4 record pairs: one 16-byte chunk of a
+// row of every plane) for two rows (SIDE_A) or columns of this thread, at
+// offsets offa and offb, written at ro0 and ro1. A lane pair covers the two
+// chunks of a row, so that one st.shared.v4 of a warp fills 16 whole rows.
+// Two points at a time in packed FP32 pairs.
 template <bool SIDE_A>
-__device__ __forceinline__ void produce16(const TcRsPair* prs, float off, float off2, uint32_t ro0, uint32_t ro1) {
+__device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, float offb, uint32_t ro0, uint32_t ro1) {
     using f2::v2;
-    const v2 offp = f2::splat(off), off2p = f2::splat(off2);
+    const v2 offpa = f2::splat(offa), off2pa = f2::splat(offa * offa);
+    const v2 offpb = f2::splat(offb), off2pb = f2::splat(offb * offb);
     const v2 c16 = f2::splat(0.0625f), c8 = f2::splat(-0.125f), c2 = f2::splat(0.5f), one = f2::splat(1.f);
     const v2 two_pi = f2::splat(kTwoPiF);
     uint32_t w_hr[8], w_hi[8], w_lr[8], w_li[8], w_xr[8], w_xi[8];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&prs[q]);
+    for (int qq = 0; qq < 8; ++qq) {
+        const int q = (qq & 1) * 4 + (qq >> 1);   // output slot: row (qq & 1), pair qq >> 1
+        const v2 offp = (qq & 1) ? offpb : offpa, off2p = (qq & 1) ? off2pb : off2pa;
+        const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&prs[qq >> 1]);
         const ulonglong2 r0 = R[0];   // h, tau
         const ulonglong2 r1 = R[1];   // P, bx
         v2 w, ph;
@@ -377,8 +381,8 @@ __device__ __forceinline__ void make_record(TcRsPair* buf, int t, bool valid, co
 }
 
 // One CTA per 128x128 tile of one channel. Warps 0-7 produce the factors
-// (threads 0-127 the rows, 128-255 the columns, all 16 points of a stage
-// each) and drain the accumulator; warp 8 allocates TMEM and its lane 0
+// (threads 0-127 the rows, 128-255 the columns: two rows or columns and 8
+// points of a stage each) and drain the accumulator; warp 8 allocates TMEM and its lane 0
 // issues the MMAs; warps 9-11 form the point records of the chunks, one
 // chunk ahead of the producers (double-buffered, an mbarrier pair per buffer).
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
@@ -428,12 +432,15 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
 
     const int t = threadIdx.x;
     const bool side_a = t < kRsTcTile;         // rows (A) or columns (B)
-    const int rc = t & (kRsTcTile - 1);        // row m or column n of the tile
+    // rows (columns) rc and rc + 64 of the tile, points 8 kc .. 8 kc + 7 of every stage
+    const int rc = (t & (kRsTcTile - 1)) >> 1, kc = t & 1;
     const float off = side_a ? (float)((double)(kRsTcHalf - rc) * g.ppY) : (float)((double)(rc - kRsTcHalf) * g.ppX);
-    const float off2 = off * off;
+    const float offb = side_a ? (float)((double)(kRsTcHalf - rc - 64) * g.ppY)
+                              : (float)((double)(rc + 64 - kRsTcHalf) * g.ppX);
     // 32-byte swizzle: rows 4-7 of every 8 swap their two 16-byte halves
+    // (rows rc and rc + 64 alike)
     const uint32_t swz = (uint32_t)((rc >> 2) & 1);
-    const uint32_t row_off0 = (uint32_t)rc * 32u + (swz << 4), row_off1 = (uint32_t)rc * 32u + ((1u ^ swz) << 4);
+    const uint32_t row_off0 = (uint32_t)rc * 32u + (((uint32_t)kc ^ swz) << 4), row_off1 = row_off0 + 64u * 32u;
     const RsTcTile tile = rs_tc_tile(g, X0, Y0);
     const float amax = a.amax[ch];
     const float inv_amax = amax > 0.f ? 1.f / amax : 0.f;
@@ -497,9 +504,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
                 dead = !__shfl_sync(0xffffffffu, ok, 0);
                 if (dead) break;
                 const uint32_t sb = smem_u32(base + s * kStageBytesTc);
-                const TcRsPair* recs16 = rb + ((it - it0) * kStagePts) / 2;
-                if (side_a) produce16<true>(recs16, off, off2, sb + row_off0, sb + row_off1);
-                else produce16<false>(recs16, off, off2, sb + row_off0, sb + row_off1);
+                const TcRsPair* recs8 = rb + ((it - it0) * kStagePts) / 2 + 4 * kc;
+                if (side_a) produce_stage<true>(recs8, off, offb, sb + row_off0, sb + row_off1);
+                else produce_stage<false>(recs8, off, offb, sb + row_off0, sb + row_off1);
                 fence_async_smem();   // generic-proxy writes -> visible to the tensor core
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[s]);
