@@ -10,19 +10,18 @@
  * cudaMemGetInfo, then runs every admitted job as a sequence of steps of
  * ~step_ms of GPU time on its own stream, so that admitted jobs overlap on
  * the device. The policy orders admission and the streams' priorities:
- *   OPHPC_SERVE_DEADLINE (default): jobs whose estimated isolated service
- *     time (interactions at the kernels' rate + copies + a fixed per-job
- *     cost) is under 20 ms first, least remaining work first among them;
- *     then the others by earliest deadline, a job's deadline being its
- *     submission time + 2 x its estimated isolated time. Short jobs overtake
- *     long ones, but a long job's priority rises as its deadline nears
- *     instead of starving behind other long ones;
+ *   OPHPC_SERVE_EARLIEST_DEADLINE (default, 0): every job by earliest
+ *     deadline, a job's deadline being its submission time + 2 x its
+ *     estimated isolated service time (interactions at the kernels' rate +
+ *     copies + a fixed per-job cost) + 20 ms. A long job's priority rises as
+ *     its deadline nears, so it is not kept waiting by a stream of short
+ *     ones; the lowest tail of the three on mixed streams;
  *   OPHPC_SERVE_SHORTEST_REMAINING: admission in arrival order, priority by
  *     remaining work (best median latency, worst tail);
- *   OPHPC_SERVE_EARLIEST_DEADLINE: every job by earliest deadline, a job's
- *     deadline being its submission time + 2 x its estimated isolated time
- *     + 20 ms (no short-job rule: long jobs are not kept waiting by a
- *     stream of short ones once their deadline is the nearest).
+ *   OPHPC_SERVE_DEADLINE: jobs whose estimated isolated service time is
+ *     under 20 ms first, least remaining work first among them; then the
+ *     others by earliest deadline (submission + 2 x estimated isolated
+ *     time). Short jobs always overtake long ones.
  * Admission never skips the first job in policy order that does not fit, so
  * a large job cannot be starved of memory by smaller ones behind it.
  * A job's result does not depend on the other jobs: its chunking is fixed
@@ -44,13 +43,13 @@ extern "C" {
 
 typedef struct ophpc_server ophpc_server;
 
-#define OPHPC_SERVE_DEADLINE 0u
+#define OPHPC_SERVE_EARLIEST_DEADLINE 0u
 #define OPHPC_SERVE_SHORTEST_REMAINING 1u
-#define OPHPC_SERVE_EARLIEST_DEADLINE 2u
+#define OPHPC_SERVE_DEADLINE 2u
 
 typedef struct ophpc_server_options {
     uint32_t max_in_flight;    /* admitted jobs at once (0 = 16) */
-    uint32_t policy;           /* OPHPC_SERVE_DEADLINE (0), _SHORTEST_REMAINING or _EARLIEST_DEADLINE */
+    uint32_t policy;           /* OPHPC_SERVE_EARLIEST_DEADLINE (0), _SHORTEST_REMAINING or _DEADLINE */
     uint64_t memory_budget;    /* bytes of device memory for jobs (0 = half the free memory) */
     uint64_t reserve_bytes;    /* free device memory always left untouched (0 = 512 MiB) */
     double step_ms;            /* target GPU time of one scheduling step (<= 0: 2 ms) */

@@ -22,9 +22,14 @@
 // stays accurate to ~1e-5 rad there) needs no per-pixel reduction. A pixel
 // costs 7 FP32 issue slots and two MUFU (sin, cos); two pixels of each 4x4
 // block instead take the phase in turns, reduce it, and evaluate sin/cos as
-// polynomials on the FMA pipe, which relieves the MUFU (the kernel's bound). Tiles the window cuts, or with large |w|, go to the
+// polynomials on the FMA pipe, which relieves the MUFU (the kernel's bound).
+// Points whose tile-local phase offsets exceed +-16 turns (off-axis points
+// close to the SLM) stay in the FAST class with the phase carried in turns
+// and reduced to [-0.5, 0.5] per pixel before the MUFU: three more FP32
+// slots, the same two MUFU. Tiles the window cuts, or with large |w|, go to the
 // EXACT class: integer rectangle test, the reference's cone test (FP32 with
-// a margin, FP64 replica of ophGen.cpp:415-428 when inside the margin) and
+// a margin, FP64 replica of ophGen.cpp:415-428 when inside the margin;
+// skipped when the window and the cone test hold for the whole tile) and
 // the exact r_p. Sums run in FP32 per chunk and are folded into FP64
 // shared-memory sums after every chunk; every pixel is stored once.
 #include "pc_common.cuh"
@@ -38,10 +43,10 @@ struct __align__(16) RsSRec {
     float P, Q, h, g;        // FAST: 2dxc/rc2, 2dyc/rc2, 1/rc2, pi rc/lambda. EXACT: 2dxc, 2dyc, rc2, rc
     float fc, ac, dxc, dyc;  // FAST: 2 pi frac(rc/lambda), coef/rc2, -pi rc/(4 lambda), -
                              // EXACT: frac(rc/lambda) in [-.5,.5], coef, dxc, dyc
-    float zz, mabs;          // EXACT: z^2, absolute margin of the FP32 cone test
+    float zz, mabs;          // FAST: rc/(2 lambda), -rc/(8 lambda) (turns). EXACT: z^2, margin of the FP32 cone test
     int32_t idx;             // EXACT: point index (FP64 fallback)
     int32_t xl, xh, yl, yh;  // EXACT: window rectangle relative to the tile origin
-    int32_t pad;
+    int32_t whole;           // EXACT: 1 when the window and the cone test hold for the whole tile; 2: FAST, reduced phase
 };
 static_assert(sizeof(RsSRec) == 64, "RsSRec size");
 
@@ -63,6 +68,180 @@ constexpr float kPi = 3.14159265358979f;
 constexpr unsigned kPolyMask = 0x8001u;
 
 
+// One FAST point's terms for the thread's 4x4 pixels. REDUCE: the phase in
+// turns, reduced to [-0.5, 0.5], then the MUFU sin/cos of 2 pi t; else the
+// phase in radians straight into the MUFU (tile-local offsets within +-16
+// turns). The pixels of kPolyMask always take the reduced phase and the
+// FMA-pipe polynomials.
+template <bool REDUCE>
+__device__ __forceinline__ void fast_point(const RsSRec& rec, const float (&u)[kPixW], const float (&uu)[kPixW],
+                                           const float (&v)[kPixH], const float (&vv)[kPixH],
+                                           float (&sr)[kPixH * kPixW], float (&si)[kPixH * kPixW]) {
+    const float4 a = *reinterpret_cast<const float4*>(&rec.P);    // P, Q, h, pi tc
+    const float4 b = *reinterpret_cast<const float4*>(&rec.fc);   // 2 pi fc, ac, -pi tc/4, fc
+    const float2 tq = *reinterpret_cast<const float2*>(&rec.zz);   // tc/2, -tc/8 (turns)
+    float A[kPixW], B[kPixH];
+#pragma unroll
+    for (int c = 0; c < kPixW; ++c) A[c] = fmaf(a.x, u[c], a.z * uu[c]);
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) B[r] = fmaf(a.y, v[r], a.z * vv[r]);
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) {
+#pragma unroll
+        for (int c = 0; c < kPixW; ++c) {
+            const float w = A[c] + B[r];
+            const int k = r * kPixW + c;
+            float s, co;
+            if ((kPolyMask >> k) & 1u) {
+                const float tt = reduce_turns(fmaf(w, fmaf(w, tq.y, tq.x), b.w));
+                sincos_turns_poly(tt, &s, &co);
+            } else if (REDUCE) {
+                const float tt = reduce_turns(fmaf(w, fmaf(w, tq.y, tq.x), b.w));
+                __sincosf(tt * kTwoPi, &s, &co);
+            } else {
+                const float ph = fmaf(w, fmaf(w, b.z, a.w), b.x);   // radians, |ph| < ~103
+                __sincosf(ph, &s, &co);
+            }
+            const float amp = fmaf(-b.y, w, b.y);
+            sr[k] = fmaf(amp, s, sr[k]);
+            si[k] = fmaf(amp, co, si[k]);
+        }
+    }
+}
+
+// The thread's offsets u = X - Xc, v = Y - Yc of its 4x4 pixels from the
+// tile centre, and their squares.
+__device__ __forceinline__ void pixel_offsets(const ChannelGeom& g, float (&u)[kPixW], float (&uu)[kPixW],
+                                              float (&v)[kPixH], float (&vv)[kPixH]) {
+    const int tx = threadIdx.x % kThreadsX, ty = threadIdx.x / kThreadsX;
+#pragma unroll
+    for (int c = 0; c < kPixW; ++c) {
+        u[c] = (float)((double)(tx * kPixW + c - kTileW / 2) * g.ppX);
+        uu[c] = u[c] * u[c];
+    }
+#pragma unroll
+    for (int r = 0; r < kPixH; ++r) {
+        v[r] = (float)((double)(kTileH / 2 - (ty * kPixH + r)) * g.ppY);
+        vv[r] = v[r] * v[r];
+    }
+}
+
+// The paths below are out of line, so that the FAST loop keeps the
+// registers it has without them; a CTA calls them only for chunks that have
+// such records. Both add into acc (re [0, 16), im [16, 32)).
+
+// FAST records whose tile-local phase offsets exceed +-16 turns (whole ==
+// 2 among the n records stored from the back of the chunk): the phase in
+// turns, reduced per pixel.
+__device__ __noinline__ void reduced_records(const RsSRec* recs, int n, const ChannelGeom g, float* acc) {
+    float u[kPixW], uu[kPixW], v[kPixH], vv[kPixH];
+    pixel_offsets(g, u, uu, v, vv);
+    float sr[kPixH * kPixW], si[kPixH * kPixW];
+#pragma unroll
+    for (int k = 0; k < kPixH * kPixW; ++k) {
+        sr[k] = acc[k];
+        si[k] = acc[kPixH * kPixW + k];
+    }
+#pragma unroll 1
+    for (int j = 0; j < n; ++j) {
+        const RsSRec& e = recs[kChunk - 1 - j];
+        if (e.whole == 2) fast_point<true>(e, u, uu, v, vv, sr, si);   // uniform over the CTA
+    }
+#pragma unroll
+    for (int k = 0; k < kPixH * kPixW; ++k) {
+        acc[k] = sr[k];
+        acc[kPixH * kPixW + k] = si[k];
+    }
+}
+
+// EXACT records (window cuts the tile, or |w| too large for the series:
+// whole < 2 among the n records stored from the back of the chunk).
+__device__ __noinline__ void exact_records(const RsSRec* recs, int n, const ChannelGeom g, const PointRec* chrec,
+                                           int X0, int Y0, float* acc) {
+    const int tx = threadIdx.x % kThreadsX, ty = threadIdx.x / kThreadsX;
+    float u[kPixW], uu[kPixW], v[kPixH], vv[kPixH];
+    pixel_offsets(g, u, uu, v, vv);
+    const float inv_lambda_f = (float)g.inv_lambda;
+    const float detx_f = (float)g.detx, dety_f = (float)g.dety;
+    float sr[kPixH * kPixW], si[kPixH * kPixW];
+#pragma unroll
+    for (int k = 0; k < kPixH * kPixW; ++k) {
+        sr[k] = acc[k];
+        si[k] = acc[kPixH * kPixW + k];
+    }
+#pragma unroll 1
+    for (int j = 0; j < n; ++j) {
+        const RsSRec& e = recs[kChunk - 1 - j];
+        if (e.whole == 2) continue;   // uniform over the CTA
+        bool inx[kPixW], iny[kPixH];
+        float dx[kPixW], dy[kPixH], nx[kPixW], ny[kPixH];
+#pragma unroll
+        for (int c = 0; c < kPixW; ++c) {
+            const int cl = tx * kPixW + c;
+            inx[c] = cl >= e.xl && cl < e.xh;
+            dx[c] = e.dxc + u[c];
+            nx[c] = u[c] * (e.P + u[c]);
+        }
+#pragma unroll
+        for (int r = 0; r < kPixH; ++r) {
+            const int rl = ty * kPixH + r;
+            iny[r] = rl >= e.yl && rl < e.yh;
+            dy[r] = e.dyc + v[r];
+            ny[r] = v[r] * (e.Q + v[r]);
+        }
+#pragma unroll
+        for (int r = 0; r < kPixH; ++r) {
+#pragma unroll
+            for (int c = 0; c < kPixW; ++c) {
+                if (!(inx[c] && iny[r])) continue;
+                // cone test (ophGen.cpp:415-428): |X-x| < detx*sqrt((Y-y)^2+z^2)
+                // and |Y-y| < dety*sqrt((X-x)^2+z^2), unless it holds for the whole tile
+                bool inside = true;
+                if (!e.whole) {
+                    const float lx = fabsf(dx[c]), rx = detx_f * sqrtf(fmaf(dy[r], dy[r], e.zz));
+                    const float ly = fabsf(dy[r]), ry = dety_f * sqrtf(fmaf(dx[c], dx[c], e.zz));
+                    const float mx = 1e-5f * (lx + rx) + e.mabs, my = 1e-5f * (ly + ry) + e.mabs;
+                    const bool xpass = rx - lx > mx, xfail = lx - rx > mx;
+                    const bool ypass = ry - ly > my, yfail = ly - ry > my;
+                    if (xfail || yfail) {
+                        inside = false;
+                    } else if (xpass && ypass) {
+                        inside = true;
+                    } else {
+                        // FP64 replica of the reference decision
+                        const PointRec p = chrec[e.idx];
+                        const double xxx = pixel_x(g, X0 + tx * kPixW + c);
+                        const double yyy = pixel_y(g, Y0 + ty * kPixH + r);
+                        const double ddy = __dsub_rn(yyy, p.y), ddx = __dsub_rn(xxx, p.x);
+                        const double hx = fabs(__dmul_rn(g.detx, sqrt(__dadd_rn(__dmul_rn(ddy, ddy), p.aux))));
+                        const double hy = fabs(__dmul_rn(g.dety, sqrt(__dadd_rn(__dmul_rn(ddx, ddx), p.aux))));
+                        inside = (xxx < __dadd_rn(p.x, hx)) && (xxx > __dsub_rn(p.x, hx)) &&
+                                 (yyy < __dadd_rn(p.y, hy)) && (yyy > __dsub_rn(p.y, hy));
+                    }
+                }
+                if (!inside) continue;
+                const float nn = nx[c] + ny[r];
+                const float rp2 = e.h + nn;
+                const float ri = rsqrtf(rp2);
+                const float rp = rp2 * ri;
+                const float dt = __fdividef(nn * inv_lambda_f, rp + e.g);
+                const float t = reduce_turns(e.fc + dt);
+                float s, co;
+                __sincosf(t * kTwoPi, &s, &co);
+                const float amp = e.ac * ri * ri;
+                const int k = r * kPixW + c;
+                sr[k] = fmaf(amp, s, sr[k]);
+                si[k] = fmaf(amp, co, si[k]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < kPixH * kPixW; ++k) {
+        acc[k] = sr[k];
+        acc[kPixH * kPixW + k] = si[k];
+    }
+}
+
 __device__ __forceinline__ int warp_prefix(unsigned ballot) {
     return __popc(ballot & ((1u << (threadIdx.x & 31)) - 1u));
 }
@@ -74,7 +253,7 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
     RsSRec* s_rec = reinterpret_cast<RsSRec*>(s_raw);
     // FP64 running sums, [pixel][thread]: consecutive threads hit consecutive 16-byte words
     double2* s_acc = reinterpret_cast<double2*>(s_raw + sizeof(RsSRec) * kChunk);
-    __shared__ int s_cnt[2][2][kThreads / 32];   // [fast|exact][q][warp]
+    __shared__ int s_cnt[2][2][kThreads / 32];   // [fast|back][q][warp]
 
     const int ch = blockIdx.z / jg.ksplit;
     const int part = blockIdx.z % jg.ksplit;
@@ -110,7 +289,6 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
         v[r] = (float)((double)(kTileH / 2 - (ty * kPixH + r)) * g.ppY);
         vv[r] = v[r] * v[r];
     }
-    const float inv_lambda_f = (float)g.inv_lambda;
     const float detx_f = (float)g.detx, dety_f = (float)g.dety;
 
 #pragma unroll
@@ -128,7 +306,7 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
         RsSRec tmp[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
-            cls[q] = 0;  // 0 skip, 1 fast, 2 exact
+            cls[q] = 0;  // 0 skip, 1 fast, 2 exact, 3 fast with the reduced phase
             const int64_t idx = cb + threadIdx.x + q * kThreads;
             if (idx < p_end) {
                 const PointRec p = chrec[idx];
@@ -164,12 +342,13 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                     const float nmax = fmaf(2.f * fabsf(dxf), uext_f, uext_f * uext_f) +
                                        fmaf(2.f * fabsf(dyf), vext_f, vext_f * vext_f);
                     const float wmax = nmax * hf;
-                    const bool series_ok = wmax < kMaxW && tcf * wmax * wmax * wmax * (1.f / 16.f) < kSeriesTol &&
-                                           tcf * wmax * fmaf(0.125f, wmax, 0.5f) < kMaxTurns;
+                    const bool series_ok = wmax < kMaxW && tcf * wmax * wmax * wmax * (1.f / 16.f) < kSeriesTol;
+                    const bool turns_ok = tcf * wmax * fmaf(0.125f, wmax, 0.5f) < kMaxTurns;
                     RsSRec& t = tmp[q];
                     t.fc = fc;
                     if (rect_full && cone_full && series_ok) {
-                        cls[q] = 1;
+                        cls[q] = turns_ok ? 1 : 3;
+                        t.whole = 2;   // tells the cls 3 records apart at the back of the chunk
                         t.P = 2.f * dxf * hf;
                         t.Q = 2.f * dyf * hf;
                         t.h = hf;
@@ -199,40 +378,42 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
                         t.xh = p.x_hi - X0;
                         t.yl = p.y_lo - Y0;
                         t.yh = p.y_hi - Y0;
+                        t.whole = rect_full && cone_full ? 1 : 0;
                     }
                 }
             }
         }
-        // ---- deterministic compaction: FAST from the front, EXACT from the back
+        // ---- deterministic compaction: FAST from the front, the rest (EXACT,
+        // and FAST with the reduced phase) from the back
         unsigned bf[2], be[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             bf[q] = __ballot_sync(0xffffffffu, cls[q] == 1);
-            be[q] = __ballot_sync(0xffffffffu, cls[q] == 2);
+            be[q] = __ballot_sync(0xffffffffu, cls[q] >= 2);
             if ((threadIdx.x & 31) == 0) {
                 s_cnt[0][q][warp] = __popc(bf[q]);
                 s_cnt[1][q][warp] = __popc(be[q]);
             }
         }
         __syncthreads();
-        int n_fast = 0, n_exact = 0;
-        int off_f[2], off_e[2];
+        int n_fast = 0, n_back = 0;
+        int off_f[2], off_b[2];
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
 #pragma unroll
             for (int w = 0; w < kThreads / 32; ++w) {
                 if (w == warp) {
                     off_f[q] = n_fast;
-                    off_e[q] = n_exact;
+                    off_b[q] = n_back;
                 }
                 n_fast += s_cnt[0][q][w];
-                n_exact += s_cnt[1][q][w];
+                n_back += s_cnt[1][q][w];
             }
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             if (cls[q] == 1) s_rec[off_f[q] + warp_prefix(bf[q])] = tmp[q];
-            else if (cls[q] == 2) s_rec[kChunk - 1 - (off_e[q] + warp_prefix(be[q]))] = tmp[q];
+            else if (cls[q] >= 2) s_rec[kChunk - 1 - (off_b[q] + warp_prefix(be[q]))] = tmp[q];
         }
         __syncthreads();
 
@@ -241,97 +422,22 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
 #pragma unroll
         for (int k = 0; k < kPixH * kPixW; ++k) sr[k] = si[k] = 0.f;
 #pragma unroll 1
-        for (int j = 0; j < n_fast; ++j) {
-            const float4 a = *reinterpret_cast<const float4*>(&s_rec[j].P);    // P, Q, h, pi tc
-            const float4 b = *reinterpret_cast<const float4*>(&s_rec[j].fc);   // 2 pi fc, ac, -pi tc/4, fc
-            const float2 tq = *reinterpret_cast<const float2*>(&s_rec[j].zz);   // tc/2, -tc/8 (turns)
-            float A[kPixW], B[kPixH];
+        for (int j = 0; j < n_fast; ++j) fast_point<false>(s_rec[j], u, uu, v, vv, sr, si);
+        // ---- the records at the back (FAST with the reduced phase, EXACT):
+        // out of line, uniform over the CTA
+        if (n_back > 0) {
+            float acc[2 * kPixH * kPixW];
 #pragma unroll
-            for (int c = 0; c < kPixW; ++c) A[c] = fmaf(a.x, u[c], a.z * uu[c]);
-#pragma unroll
-            for (int r = 0; r < kPixH; ++r) B[r] = fmaf(a.y, v[r], a.z * vv[r]);
-#pragma unroll
-            for (int r = 0; r < kPixH; ++r) {
-#pragma unroll
-                for (int c = 0; c < kPixW; ++c) {
-                    const float w = A[c] + B[r];
-                    const int k = r * kPixW + c;
-                    float s, co;
-                    if ((kPolyMask >> k) & 1u) {
-                        const float tt = reduce_turns(fmaf(w, fmaf(w, tq.y, tq.x), b.w));
-                        sincos_turns_poly(tt, &s, &co);
-                    } else {
-                        const float ph = fmaf(w, fmaf(w, b.z, a.w), b.x);   // radians, |ph| < ~103
-                        __sincosf(ph, &s, &co);
-                    }
-                    const float amp = fmaf(-b.y, w, b.y);
-                    sr[k] = fmaf(amp, s, sr[k]);
-                    si[k] = fmaf(amp, co, si[k]);
-                }
+            for (int k = 0; k < kPixH * kPixW; ++k) {
+                acc[k] = sr[k];
+                acc[kPixH * kPixW + k] = si[k];
             }
-        }
-        // ---- EXACT: window cuts the tile, or |w| too large for the series ---
-#pragma unroll 1
-        for (int j = 0; j < n_exact; ++j) {
-            const RsSRec& e = s_rec[kChunk - 1 - j];
-            bool inx[kPixW], iny[kPixH];
-            float dx[kPixW], dy[kPixH], nx[kPixW], ny[kPixH];
+            reduced_records(s_rec, n_back, g, acc);
+            exact_records(s_rec, n_back, g, chrec, X0, Y0, acc);
 #pragma unroll
-            for (int c = 0; c < kPixW; ++c) {
-                const int cl = tx * kPixW + c;
-                inx[c] = cl >= e.xl && cl < e.xh;
-                dx[c] = e.dxc + u[c];
-                nx[c] = u[c] * (e.P + u[c]);
-            }
-#pragma unroll
-            for (int r = 0; r < kPixH; ++r) {
-                const int rl = ty * kPixH + r;
-                iny[r] = rl >= e.yl && rl < e.yh;
-                dy[r] = e.dyc + v[r];
-                ny[r] = v[r] * (e.Q + v[r]);
-            }
-#pragma unroll
-            for (int r = 0; r < kPixH; ++r) {
-#pragma unroll
-                for (int c = 0; c < kPixW; ++c) {
-                    if (!(inx[c] && iny[r])) continue;
-                    // cone test (ophGen.cpp:415-428): |X-x| < detx*sqrt((Y-y)^2+z^2)
-                    // and |Y-y| < dety*sqrt((X-x)^2+z^2)
-                    const float lx = fabsf(dx[c]), rx = detx_f * sqrtf(fmaf(dy[r], dy[r], e.zz));
-                    const float ly = fabsf(dy[r]), ry = dety_f * sqrtf(fmaf(dx[c], dx[c], e.zz));
-                    const float mx = 1e-5f * (lx + rx) + e.mabs, my = 1e-5f * (ly + ry) + e.mabs;
-                    const bool xpass = rx - lx > mx, xfail = lx - rx > mx;
-                    const bool ypass = ry - ly > my, yfail = ly - ry > my;
-                    bool inside;
-                    if (xfail || yfail) {
-                        inside = false;
-                    } else if (xpass && ypass) {
-                        inside = true;
-                    } else {
-                        // FP64 replica of the reference decision
-                        const PointRec p = chrec[e.idx];
-                        const double xxx = pixel_x(g, X0 + tx * kPixW + c);
-                        const double yyy = pixel_y(g, Y0 + ty * kPixH + r);
-                        const double ddy = __dsub_rn(yyy, p.y), ddx = __dsub_rn(xxx, p.x);
-                        const double hx = fabs(__dmul_rn(g.detx, sqrt(__dadd_rn(__dmul_rn(ddy, ddy), p.aux))));
-                        const double hy = fabs(__dmul_rn(g.dety, sqrt(__dadd_rn(__dmul_rn(ddx, ddx), p.aux))));
-                        inside = (xxx < __dadd_rn(p.x, hx)) && (xxx > __dsub_rn(p.x, hx)) &&
-                                 (yyy < __dadd_rn(p.y, hy)) && (yyy > __dsub_rn(p.y, hy));
-                    }
-                    if (!inside) continue;
-                    const float nn = nx[c] + ny[r];
-                    const float rp2 = e.h + nn;
-                    const float ri = rsqrtf(rp2);
-                    const float rp = rp2 * ri;
-                    const float dt = __fdividef(nn * inv_lambda_f, rp + e.g);
-                    const float t = reduce_turns(e.fc + dt);
-                    float s, co;
-                    __sincosf(t * kTwoPi, &s, &co);
-                    const float amp = e.ac * ri * ri;
-                    const int k = r * kPixW + c;
-                    sr[k] = fmaf(amp, s, sr[k]);
-                    si[k] = fmaf(amp, co, si[k]);
-                }
+            for (int k = 0; k < kPixH * kPixW; ++k) {
+                sr[k] = acc[k];
+                si[k] = acc[kPixH * kPixW + k];
             }
         }
 #pragma unroll

@@ -9,9 +9,9 @@
 // stream. Jobs therefore overlap on the device; a job that arrives while
 // others run is admitted as soon as a slot and memory free up and its
 // kernels interleave with theirs at CTA granularity. Steps are issued on
-// streams whose priority follows the policy's order: by default short jobs
-// first (least remaining work first among them), then the others by
-// earliest deadline (submission + 2 x estimated isolated time); or purely
+// streams whose priority follows the policy's order: by default every job
+// by earliest deadline (submission + 2 x estimated isolated time + 20 ms);
+// or short jobs first, then the others by earliest deadline; or purely
 // shortest remaining work. Short jobs are not stuck behind long ones and
 // long ones are not starved by a stream of short ones.
 //
@@ -92,10 +92,11 @@ struct ServeJob {
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-// Policy order, OPHPC_SERVE_DEADLINE: short jobs (estimated isolated time
-// under kShortJobS) first, least remaining work first among them; then the
-// others by earliest deadline. OPHPC_SERVE_SHORTEST_REMAINING: least
-// remaining work first.
+// Policy order. OPHPC_SERVE_EARLIEST_DEADLINE (default): earliest deadline
+// + kEdfSlackS first. OPHPC_SERVE_SHORTEST_REMAINING: least remaining work
+// first. OPHPC_SERVE_DEADLINE: short jobs (estimated isolated time under
+// kShortJobS) first, least remaining work first among them; then the others
+// by earliest deadline.
 bool before(uint32_t policy, const ServeJob* a, const ServeJob* b) {
     if (policy == OPHPC_SERVE_SHORTEST_REMAINING) return a->remaining < b->remaining;
     if (policy == OPHPC_SERVE_EARLIEST_DEADLINE) return a->edf_deadline < b->edf_deadline;
@@ -450,7 +451,9 @@ ophpc_status ophpc_server_create(int32_t device, const ophpc_server_options* opt
     s->device = device;
     if (options) s->opt = *options;
     if (s->opt.max_in_flight == 0) s->opt.max_in_flight = 16;
-    if (s->opt.policy > OPHPC_SERVE_EARLIEST_DEADLINE) return OPHPC_ERROR_INVALID_ARGUMENT;
+    if (s->opt.policy != OPHPC_SERVE_EARLIEST_DEADLINE && s->opt.policy != OPHPC_SERVE_SHORTEST_REMAINING &&
+        s->opt.policy != OPHPC_SERVE_DEADLINE)
+        return OPHPC_ERROR_INVALID_ARGUMENT;
     if (s->opt.step_ms <= 0) s->opt.step_ms = 2.0;
     if (s->opt.reserve_bytes == 0) s->opt.reserve_bytes = (size_t)512 << 20;
     if (s->opt.memory_budget == 0) {

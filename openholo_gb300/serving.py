@@ -9,9 +9,9 @@ import numpy as np
 
 from ._abi import OphpcConfig, OphpcError, lib, make_config
 
-POLICY_DEADLINE = 0
+POLICY_EARLIEST_DEADLINE = 0   # default
 POLICY_SHORTEST_REMAINING = 1
-POLICY_EARLIEST_DEADLINE = 2
+POLICY_DEADLINE = 2            # short jobs first, then earliest deadline
 
 
 class ServerOptions(ctypes.Structure):
@@ -68,7 +68,7 @@ class Server:
     """Continuous-batching hologram server on one GPU."""
 
     def __init__(self, device: int = 0, max_in_flight: int = 16, memory_budget: int = 0, step_ms: float = 2.0,
-                 reserve_bytes: int = 0, policy: int = POLICY_DEADLINE):
+                 reserve_bytes: int = 0, policy: int = POLICY_EARLIEST_DEADLINE):
         self._L = _L()
         o = ServerOptions(max_in_flight=max_in_flight, policy=policy, memory_budget=memory_budget,
                           reserve_bytes=reserve_bytes, step_ms=step_ms)

@@ -176,3 +176,52 @@ def test_misaligned_buffers_are_rejected(gpu_ctx):
     gpu_ctx.generate(cfg, v.data_ptr(), 8, 0, 0, f.data_ptr(), s)              # aligned: fine
     torch.cuda.synchronize()
     assert torch.isfinite(f).all()
+
+
+def _reduced_class_pairs(pnx, pny, pp, lam, v):
+    """(point, 64x32 tile) pairs that the FP32-core RS kernel keeps in its
+    FAST class with the per-pixel reduced phase: tile inside the window and
+    the cone, series error below 2e-8 turns, tile-local phase offsets above
+    16 turns (pc_rs.cu). Approximate tile geometry; only counts them."""
+    tan = (lam / (2 * pp)) / np.sqrt(1 - (lam / (2 * pp)) ** 2)
+    X0 = np.arange(0, pnx, 64)
+    Y0 = np.arange(0, pny, 32)
+    Xc = ((X0 + 32) - pnx / 2) * pp
+    Yc = (pny / 2 - (Y0 + 16)) * pp
+    ue, ve = 32 * pp, 16 * pp
+    dx = np.abs(Xc[None, None, :] - v[:, 0, None, None])
+    dy = np.abs(Yc[None, :, None] - v[:, 1, None, None])
+    zz = v[:, 2, None, None] ** 2
+    rc2 = dx ** 2 + dy ** 2 + zz
+    w = (2 * dx * ue + ue * ue + 2 * dy * ve + ve * ve) / rc2
+    tc = np.sqrt(rc2) / lam
+    inside = (dx + ue < tan * np.sqrt(np.maximum(dy - ve, 0) ** 2 + zz)) & \
+             (dy + ve < tan * np.sqrt(np.maximum(dx - ue, 0) ** 2 + zz))
+    fast = inside & (w < 1e-3) & (tc * w ** 3 / 16 < 2e-8)
+    return int(np.sum(fast & (tc * w * (0.5 + w / 8) >= 16))), int(fast.size)
+
+
+def test_rs_offaxis_near_reduced_phase(gpu_ctx, oracle_mod):
+    """2048x2048 at 8 um, 532 nm, points ~0.3 m away and up to ~12 mm off
+    axis: tile-local phase offsets of up to ~25 turns, which the FP32-core
+    kernel carries in turns and reduces per pixel (and the tensor-core path
+    leaves most of these pairs to it: the cross phase is too large). Both
+    modes against the FP64 oracle at seeded pixels, corners included."""
+    import openholo_gb300 as oph
+    pnx = pny = 2048
+    pp, lam = 8e-6, 532e-9
+    v = _box(300, (4e-3, 4e-3), (0.29, 0.33), 19)
+    n_red, n_all = _reduced_class_pairs(pnx, pny, pp, lam, v)
+    print(f"reduced-phase FAST pairs: {n_red} of {n_all}")
+    assert n_red > 0.02 * n_all
+    gk = dict(pnx=pnx, pny=pny, ppx=pp, ppy=pp, wavelengths=[lam])
+    rng = np.random.default_rng(20)
+    corners = [y * pnx + x for y in (0, 1, pny - 2, pny - 1) for x in range(0, pnx, 97)]
+    idx = np.unique(np.concatenate([rng.choice(pnx * pny, 6000, replace=False), corners]))
+    g = oracle_mod.Geometry(pnx=pnx, pny=pny, ppx=pp, ppy=pp, wavelengths=[lam])
+    want = oracle_mod.field_at(g, v, 0, 0, idx)
+    for mode in (0, oph.MODE_TENSOR_BF16X3):
+        got = run_generate(gpu_ctx, gk, v, 0, mode)[0].ravel()[idx]
+        err = rel_l2(got, want)
+        print(f"mode {mode:#x}: relL2 {err:.3e} on {idx.size} pixels")
+        assert err <= FIELD_TOL

@@ -89,18 +89,20 @@ def test_memory_admission_serialises_jobs(gpu_ctx):
 
 
 def test_policies_give_identical_results(gpu_ctx):
-    """Earliest-deadline and shortest-remaining scheduling reorder steps, not
-    arithmetic: every job's field is the same under both."""
+    """The three policies (earliest deadline, the default; shortest remaining
+    work; short jobs first) reorder steps, not arithmetic: every job's field
+    is the same under each."""
     from openholo_gb300 import OphpcError
-    from openholo_gb300.serving import POLICY_DEADLINE, POLICY_SHORTEST_REMAINING, Server
+    from openholo_gb300.serving import POLICY_DEADLINE, POLICY_EARLIEST_DEADLINE, POLICY_SHORTEST_REMAINING, Server
     jobs = _jobs(seed=7)
     fields = {}
-    for pol in (POLICY_DEADLINE, POLICY_SHORTEST_REMAINING):
+    for pol in (POLICY_EARLIEST_DEADLINE, POLICY_SHORTEST_REMAINING, POLICY_DEADLINE):
         with Server(0, max_in_flight=4, step_ms=0.5, policy=pol) as srv:
             tickets = [srv.submit(g, v, d) for g, v, d in jobs]
             fields[pol] = [srv.wait(t).field for t in tickets]
-    for a, b in zip(fields[POLICY_DEADLINE], fields[POLICY_SHORTEST_REMAINING]):
-        assert np.array_equal(a, b)
+    for other in (POLICY_SHORTEST_REMAINING, POLICY_DEADLINE):
+        for a, b in zip(fields[POLICY_EARLIEST_DEADLINE], fields[other]):
+            assert np.array_equal(a, b)
     with pytest.raises(OphpcError):
         Server(0, policy=7)
 
