@@ -65,6 +65,13 @@ struct JobGeom {
     int32_t tc_skip;
     const int32_t* tc_left;
     int32_t tc_tiles_x, tc_tiles_y;
+    // When set: per 128x128 tile, one bit per point of the launch's range
+    // (bit i of word i / 32, i relative to p0; tc_mask_words words a tile,
+    // [ch][ty][tx][word]) for the pairs that kernel left; the complement
+    // reads these instead of re-testing eligibility, and skips the rest
+    // without loading them.
+    const uint32_t* tc_mask;
+    int64_t tc_mask_words;
 };
 
 // Pixel-centre coordinates, exactly as the reference forms them

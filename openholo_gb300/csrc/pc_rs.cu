@@ -51,9 +51,11 @@ struct __align__(16) RsSRec {
 static_assert(sizeof(RsSRec) == 64, "RsSRec size");
 
 constexpr float kTwoPi = 6.283185307179586f;
-// FAST requires (rc/lambda) * |w|^3 / 16 below this many turns (series error)
-// and |w| below kMaxW (the dropped amplitude term is w^2).
-constexpr float kSeriesTol = 2e-8f;
+// FAST requires (rc/lambda) * |w|^3 / 16 below this many turns (series error,
+// below the FP32 rounding of the phase itself: ~1.5e-6 turns at the 25
+// turns the tile-local offsets reach) and |w| below kMaxW (the dropped
+// amplitude term is w^2).
+constexpr float kSeriesTol = 1e-7f;
 constexpr float kMaxW = 1e-3f;
 // FAST also requires the tile-local phase offset (tc/2)|w| + (tc/8)w^2 below
 // this many turns: the FP32 phase in radians then stays under ~103 rad.
@@ -267,6 +269,12 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
         return;
     RsTcTile tct;
     if (jg.tc_skip) tct = rs_tc_tile(g, tcX0, tcY0);
+    // the tensor-core kernel's bits for the pairs it left (relative to p0)
+    const uint32_t* left_mask =
+        jg.tc_skip && jg.tc_mask
+            ? jg.tc_mask + (((int64_t)ch * jg.tc_tiles_y + tcY0 / kRsTcTile) * jg.tc_tiles_x + tcX0 / kRsTcTile) *
+                               jg.tc_mask_words
+            : nullptr;
     const int vx1 = min(X0 + kTileW, g.pnX), vy1 = min(Y0 + kTileH, g.pnY);
     const int xc = X0 + kTileW / 2, yc = Y0 + kTileH / 2;
     const double Xc = pixel_x(g, xc), Yc = pixel_y(g, yc);
@@ -308,12 +316,13 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
         for (int q = 0; q < 2; ++q) {
             cls[q] = 0;  // 0 skip, 1 fast, 2 exact, 3 fast with the reduced phase
             const int64_t idx = cb + threadIdx.x + q * kThreads;
-            if (idx < p_end) {
+            const int64_t rel = idx - jg.p0;
+            if (idx < p_end && (!left_mask || ((left_mask[rel >> 5] >> (rel & 31)) & 1u))) {
                 const PointRec p = chrec[idx];
                 const int ix0 = max(X0, p.x_lo), ix1 = min(vx1, p.x_hi);
                 const int iy0 = max(Y0, p.y_lo), iy1 = min(vy1, p.y_hi);
                 float wxm_t, wym_t;
-                if (ix0 < ix1 && iy0 < iy1 && !(jg.tc_skip && rs_tc_eligible(p, tct, &wxm_t, &wym_t))) {
+                if (ix0 < ix1 && iy0 < iy1 && (left_mask || !(jg.tc_skip && rs_tc_eligible(p, tct, &wxm_t, &wym_t)))) {
                     // FP64: only frac(r_c / lambda). sqrt from an FP32 seed
                     // refined by two Newton steps (relative error < 1e-20).
                     const double dxc = Xc - p.x, dyc = Yc - p.y;

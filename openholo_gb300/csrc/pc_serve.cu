@@ -77,6 +77,7 @@ struct ServeJob {
     bool tcf = false;           // Fresnel on the tensor cores (either tensor mode)
     float* d_amax = nullptr;    // tensor cores: per-channel amplitude bound
     int32_t* d_left = nullptr;  // tensor-core RS: per-tile pair counts for the complement
+    uint32_t* d_mask = nullptr; // tensor-core RS: per-tile bits of the pairs left to the complement
     int* d_err = nullptr;       // tensor cores: kernel timeout word
     double* d_sum = nullptr;    // tensor-core Fresnel: [channel][re plane, im plane] FP64 sums
     TcFresnelPlan plan{};       // tensor-core Fresnel: factor tables of one step's points
@@ -203,10 +204,13 @@ int64_t tcf_step_points(const ophpc_job* j, double step_ms, double rate) {
     return std::max<int64_t>(m, std::min<int64_t>(kc, nup));
 }
 
-size_t tc_left_bytes(const ophpc_job* j) {
-    const size_t tiles = (size_t)((j->cfg.pixel_number[0] + kRsTcTile - 1) / kRsTcTile) *
-                         ((j->cfg.pixel_number[1] + kRsTcTile - 1) / kRsTcTile);
-    return align256(sizeof(int32_t) * tiles * j->cfg.n_channels);
+size_t tc_tiles(const ophpc_job* j) {
+    return (size_t)((j->cfg.pixel_number[0] + kRsTcTile - 1) / kRsTcTile) *
+           ((j->cfg.pixel_number[1] + kRsTcTile - 1) / kRsTcTile) * j->cfg.n_channels;
+}
+size_t tc_left_bytes(const ophpc_job* j) { return align256(sizeof(int32_t) * tc_tiles(j)); }
+size_t tc_mask_bytes(const ophpc_job* j) {
+    return align256(sizeof(uint32_t) * tc_tiles(j) * (size_t)tc_rs_mask_words((int64_t)j->n_points));
 }
 
 size_t tcf_bytes(const ophpc_job* j, int64_t kc) {
@@ -220,7 +224,7 @@ size_t job_bytes(const ophpc_job* j, int64_t tcf_kc) {
     const size_t px = (size_t)j->cfg.pixel_number[0] * j->cfg.pixel_number[1] * j->cfg.n_channels;
     return align256(sizeof(ophpc_vertex) * j->n_points) + align256(sizeof(PointRec) * j->n_points * j->cfg.n_channels) +
            align256(sizeof(double2) * px) + align256(px) + 256 + (uses_tc(j) || uses_tcf(j) ? 256 : 0) +
-           (uses_tc(j) ? tc_left_bytes(j) : 0) + (uses_tcf(j) ? tcf_bytes(j, tcf_kc) : 0);
+           (uses_tc(j) ? tc_left_bytes(j) + tc_mask_bytes(j) : 0) + (uses_tcf(j) ? tcf_bytes(j, tcf_kc) : 0);
 }
 
 // Enqueues the job's next step on the stream of its slot at the priority
@@ -270,7 +274,8 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
         g.points_per_split = std::max<int64_t>(kChunk, ((g.p1 - g.p0 + kChunk - 1) / kChunk) * kChunk);
         if (j->tc)
             e = launch_tc_rs_range(j->jg, j->d_recs, g.p0, g.p1, g.accumulate != 0,
-                                   reinterpret_cast<double2*>(j->d_field), j->d_amax, j->d_left, j->d_err, st);
+                                   reinterpret_cast<double2*>(j->d_field), j->d_amax, j->d_left, j->d_mask,
+                                   tc_rs_mask_words((int64_t)d.n_points), j->d_err, st);
         else if (d.diff_flag == OPHPC_DIFF_RS)
             launch_rs(j->d_recs, g, reinterpret_cast<double2*>(j->d_field), nullptr, st);
         else
@@ -332,7 +337,10 @@ bool admit(ophpc_server* s, ServeJob* j) {
         q += 256;
         s->h_err[j->slot] = 0;
     }
-    if (j->tc) j->d_left = (int32_t*)q;
+    if (j->tc) {
+        j->d_left = (int32_t*)q;
+        j->d_mask = (uint32_t*)(q + tc_left_bytes(&d));
+    }
     if (j->tcf) {
         unsigned char* tq = (unsigned char*)(((uintptr_t)q + 1023) & ~(uintptr_t)1023);
         const size_t tb = tc_fresnel_table_bytes(d.cfg.pixel_number[0], d.cfg.pixel_number[1], (int)j->chunk_points,

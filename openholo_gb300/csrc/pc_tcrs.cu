@@ -109,8 +109,12 @@ struct TcRsArgs {
     // partials[k - 1] (same layout), summed afterwards.
     int64_t p_base, p_count;
     int32_t ksplit;
-    int64_t pps;
+    int64_t pps;            // a multiple of kChunkTc
     double2* partials;
+    // per tile, one bit per point of [p_base, p_base + p_count) for the
+    // pairs left to the CUDA cores (word (i - p_base) / 32); mask_words words a tile
+    uint32_t* mask;
+    int64_t mask_words;
 };
 
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -334,10 +338,13 @@ __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full
 }
 
 // Per (point, tile) values of point idx into record pair slot t of buf
-// (zeros when the pair is not taken). Counts pairs left to the CUDA cores.
-__device__ __forceinline__ void make_record(TcRsPair* buf, int t, bool valid, const PointRec& p,
+// (zeros when the pair is not taken). True (and counted in left) for a pair
+// left to the CUDA cores: the window overlaps the tile, the expansion does
+// not hold.
+__device__ __forceinline__ bool make_record(TcRsPair* buf, int t, bool valid, const PointRec& p,
                                             const RsTcTile& tile, double inv_lambda, float inv_amax, int X0, int Y0,
                                             int& left) {
+    bool is_left = false;
     float h = 0.f, tau = 0.f, P = 0.f, bx = 0.f, Q = 0.f, fc = 0.f, ac = 0.f, k2 = 0.f;
     if (valid) {
         const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
@@ -366,6 +373,7 @@ __device__ __forceinline__ void make_record(TcRsPair* buf, int t, bool valid, co
                 k2 = -1.5707963267948966f * tau * wxm * kCrossScale;
             } else {
                 ++left;
+                is_left = true;
             }
         }
     }
@@ -378,6 +386,7 @@ __device__ __forceinline__ void make_record(TcRsPair* buf, int t, bool valid, co
     f[10] = fc;
     f[12] = ac;
     f[14] = k2;
+    return is_left;
 }
 
 // One CTA per 128x128 tile of one channel. Warps 0-7 produce the factors
@@ -470,6 +479,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
         // records of chunk c into buffer c & 1, once the producers released
         // the chunk that used it before (c - 2)
         const int rt = t - (kProducers + 32);
+        const int64_t mask_base = (((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x) * a.mask_words;
         for (int c = 0; c < nchunks && !dead; ++c) {
             const int b = c & 1;
             if (c >= 2) {
@@ -481,7 +491,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
             for (int j = rt; j < kChunkTc; j += kRecThreads) {
                 const int64_t idx = (int64_t)c * kChunkTc + j;
                 const bool valid = idx < n;
-                make_record(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda, inv_amax, X0, Y0, left);
+                const bool l = make_record(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda, inv_amax, X0,
+                                           Y0, left);
+                // the warp's 32 consecutive points -> one word of the left-pair
+                // mask (this CTA alone writes it: pps is a multiple of kChunkTc)
+                const uint32_t bits = __ballot_sync(0xffffffffu, l);
+                if (lane == 0 && a.mask)
+                    a.mask[mask_base + (((int64_t)part * a.pps + idx) >> 5)] = bits;
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&rec_full[b]);
@@ -571,14 +587,22 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     // One CTA per SM: split every tile's points into k parts so that the
     // CTA count fills whole waves (each extra part costs a field-sized
     // partial and a summing pass: demand a 3% gain, at least 1,024 points
-    // a part, at most 2 GiB of partials).
+    // a part, at most 2 GiB of partials). Parts are whole chunks of
+    // kChunkTc points (the left-pair mask words of a part are its own), and
+    // none is empty.
     const int64_t tiles = (int64_t)tiles_x * tiles_y * nch;
     const size_t field_bytes = sizeof(double2) * (size_t)nch * pnX * pnY;
     const int slots = sm_count > 0 ? sm_count : 1;
+    auto part_points = [&](int k) {
+        const int64_t p = ((int64_t)n_points + k - 1) / k;
+        return (p + kChunkTc - 1) / kChunkTc * kChunkTc;
+    };
     int ksplit = 1;
     double best = 0.0;
     for (int k = 1; k <= 8; ++k) {
-        if (k > 1 && ((int64_t)n_points / k < 1024 || (size_t)(k - 1) * field_bytes > ((size_t)2 << 30))) break;
+        if (k > 1 && ((int64_t)n_points / k < 1024 || (size_t)(k - 1) * field_bytes > ((size_t)2 << 30) ||
+                      (int64_t)n_points - (k - 1) * part_points(k) < 1))
+            break;
         const double waves = (double)(tiles * k) / slots;
         const double eff = waves / std::ceil(waves);
         if (eff > best + 0.03) {
@@ -586,15 +610,23 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
             ksplit = k;
         }
     }
-    const int64_t pps = ((int64_t)n_points + ksplit - 1) / ksplit;   // every part non-empty: n >= 1024 k
+    const int64_t pps = part_points(ksplit);
     const size_t part_bytes = align_up(field_bytes * (size_t)(ksplit - 1), 256);
+    // left-pair mask: one bit per (tile, point); without room for it the
+    // complement re-tests eligibility instead
+    static_assert(kChunkTc == 256, "tc_rs_mask_words assumes chunks of 256 points");
+    const int64_t mask_words = tc_rs_mask_words((int64_t)n_points);
+    size_t mask_bytes = align_up(sizeof(uint32_t) * (size_t)tiles * (size_t)mask_words, 256);
+    if (mask_bytes > ((size_t)4 << 30)) mask_bytes = 0;
     unsigned char* buf = nullptr;
-    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + part_bytes + 256, pool, s) != cudaSuccess)
+    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + part_bytes + mask_bytes + 256, pool, s) !=
+        cudaSuccess)
         return fail(OPHPC_ERROR_OUT_OF_MEMORY, "tensor-core RS scratch allocation failed");
     PointRec* recs = (PointRec*)buf;
     int32_t* left = (int32_t*)(buf + rec_bytes);
     double2* partials = ksplit > 1 ? (double2*)(buf + rec_bytes + left_bytes) : nullptr;
-    float* amax = (float*)(buf + rec_bytes + left_bytes + part_bytes);   // [3]
+    uint32_t* mask = mask_bytes ? (uint32_t*)(buf + rec_bytes + left_bytes + part_bytes) : nullptr;
+    float* amax = (float*)(buf + rec_bytes + left_bytes + part_bytes + mask_bytes);   // [3]
     int* errw = (int*)(amax + 4);
     cudaMemsetAsync(amax, 0, 32, s);   // amax[0..3] and the error word
     cudaMemsetAsync(left, 0, left_bytes, s);
@@ -621,6 +653,8 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     ta.ksplit = ksplit;
     ta.pps = pps;
     ta.partials = partials;
+    ta.mask = mask;
+    ta.mask_words = mask_words;
     count_launches(1);
     tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)(nch * ksplit)), kThreadsTc, kSmemTc, s>>>(ta);
     JobGeom js = jg;
@@ -638,6 +672,8 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     jc.tc_left = left;
     jc.tc_tiles_x = tiles_x;
     jc.tc_tiles_y = tiles_y;
+    jc.tc_mask = mask;
+    jc.tc_mask_words = mask_words;
     launch_rs(recs, jc, (double2*)d_field, nullptr, s);
 
     cudaError_t e = cudaGetLastError();
@@ -658,9 +694,11 @@ void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, fl
 }
 
 cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1, bool accumulate,
-                               double2* d_field, const float* d_amax, int32_t* d_left, int* d_err, cudaStream_t s) {
+                               double2* d_field, const float* d_amax, int32_t* d_left, uint32_t* d_mask,
+                               int64_t mask_words, int* d_err, cudaStream_t s) {
     cudaError_t e = cudaFuncSetAttribute(tc_rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTc);
     if (e != cudaSuccess || p1 <= p0) return e;
+    if (d_mask && tc_rs_mask_words(p1 - p0) > mask_words) return cudaErrorInvalidValue;
     const int nch = jg.n_channels;
     const int pnX = jg.ch[0].pnX, pnY = jg.ch[0].pnY;
     const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
@@ -681,6 +719,8 @@ cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_
     ta.p_count = p1 - p0;
     ta.ksplit = 1;
     ta.pps = p1 - p0;
+    ta.mask = d_mask;
+    ta.mask_words = mask_words;
     count_launches(1);
     tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTc, s>>>(ta);
     JobGeom jc = jg;
@@ -693,6 +733,8 @@ cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_
     jc.tc_left = d_left;
     jc.tc_tiles_x = tiles_x;
     jc.tc_tiles_y = tiles_y;
+    jc.tc_mask = d_mask;
+    jc.tc_mask_words = mask_words;
     launch_rs(d_recs, jc, d_field, nullptr, s);
     return cudaGetLastError();
 }

@@ -22,7 +22,7 @@ constexpr int kRsTcHalf = kRsTcTile / 2;
 // Expansion limits (see pc_tcrs.cu): |w_x| + |w_y| bound, the dropped
 // cross-term error, and the phase terms left out of the factors (turns).
 constexpr float kRsTcMaxW = 1e-3f;
-constexpr float kRsTcMaxCross = 4e-3f;       // radians, first-order e^{i theta}: error theta^2/2
+constexpr float kRsTcMaxCross = 8e-3f;       // radians, first-order e^{i theta}: error theta^2/2 <= 3.2e-5
 constexpr float kRsTcMaxDropped = 2e-7f;     // turns
 
 // Constants of one 128x128 tile (origin X0, Y0) that the eligibility test
@@ -134,10 +134,14 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
 // launch_tc_rs_range: points [p0, p1) of the records on the tensor cores,
 // overwriting the field (accumulate false) or adding into it, then the
 // CUDA-core complement for the same range; d_left holds n_channels x tiles
-// ints (128x128 tiles) of scratch, *d_err is set on a kernel timeout.
+// ints (128x128 tiles) of scratch; d_mask (optional) n_channels x tiles x
+// mask_words words, mask_words >= tc_rs_mask_words(p1 - p0), through which
+// the complement finds the pairs left to it; *d_err is set on a kernel
+// timeout.
 void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t stream);
+inline int64_t tc_rs_mask_words(int64_t n_points) { return (n_points + 255) / 256 * 8; }
 cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1, bool accumulate,
-                               double2* d_field, const float* d_amax, int32_t* d_left, int* d_err,
-                               cudaStream_t stream);
+                               double2* d_field, const float* d_amax, int32_t* d_left, uint32_t* d_mask,
+                               int64_t mask_words, int* d_err, cudaStream_t stream);
 
 }  // namespace ophpc

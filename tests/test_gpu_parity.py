@@ -181,7 +181,7 @@ def test_misaligned_buffers_are_rejected(gpu_ctx):
 def _reduced_class_pairs(pnx, pny, pp, lam, v):
     """(point, 64x32 tile) pairs that the FP32-core RS kernel keeps in its
     FAST class with the per-pixel reduced phase: tile inside the window and
-    the cone, series error below 2e-8 turns, tile-local phase offsets above
+    the cone, series error below 1e-7 turns, tile-local phase offsets above
     16 turns (pc_rs.cu). Approximate tile geometry; only counts them."""
     tan = (lam / (2 * pp)) / np.sqrt(1 - (lam / (2 * pp)) ** 2)
     X0 = np.arange(0, pnx, 64)
@@ -197,7 +197,7 @@ def _reduced_class_pairs(pnx, pny, pp, lam, v):
     tc = np.sqrt(rc2) / lam
     inside = (dx + ue < tan * np.sqrt(np.maximum(dy - ve, 0) ** 2 + zz)) & \
              (dy + ve < tan * np.sqrt(np.maximum(dx - ue, 0) ** 2 + zz))
-    fast = inside & (w < 1e-3) & (tc * w ** 3 / 16 < 2e-8)
+    fast = inside & (w < 1e-3) & (tc * w ** 3 / 16 < 1e-7)
     return int(np.sum(fast & (tc * w * (0.5 + w / 8) >= 16))), int(fast.size)
 
 
