@@ -194,6 +194,32 @@ ophpc_status ophpc_generate_static_scratch(const ophpc_config* cfg, const ophpc_
 ophpc_status ophpc_normalize(ophpc_context* ctx, const double* d_encoded, uint32_t n_channels,
                              uint64_t n_pixels, uint8_t* d_normalized, void* stream);
 
+/* Plans: one ophpc_generate (and, unless encode_flag is
+ * OPHPC_PLAN_NO_ENCODE, one ophpc_encode of its field) captured once into a
+ * CUDA graph and replayed by ophpc_plan_launch. This entry point has no
+ * counterpart in the reference. It is for callers that generate the same
+ * shapes over and over (successive frames of a moving point cloud, many
+ * small jobs): one graph launch replaces the host work and kernel launches
+ * of every call. The buffers are fixed at creation and must stay valid;
+ * each replay reads the vertices currently in d_vertices, so the caller
+ * writes the next frame's points there (on the replay's stream, or before
+ * it) and launches again. Scratch is allocated and freed inside the graph.
+ * Replays of one plan must not overlap in time (wait for one before the
+ * next on another stream); ophpc_plan_wait synchronises `stream` and
+ * reports the tensor-core kernels' timeout word of the last replay
+ * (OPHPC_ERROR_TIMEOUT), which ophpc_generate reports itself. Results are
+ * bit-identical to the direct calls. ophpc_kernel_launches counts a plan's
+ * kernels once, at creation. */
+#define OPHPC_PLAN_NO_ENCODE 0xffffffffu
+typedef struct ophpc_plan ophpc_plan;
+ophpc_status ophpc_plan_create(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
+                               uint64_t n_points, uint32_t diff_flag, uint32_t mode, double* d_field,
+                               uint32_t encode_flag, double* d_encoded, uint8_t* d_normalized,
+                               ophpc_plan** out);
+ophpc_status ophpc_plan_launch(ophpc_plan* plan, void* stream);
+ophpc_status ophpc_plan_wait(ophpc_plan* plan, void* stream);
+ophpc_status ophpc_plan_destroy(ophpc_plan* plan);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,8 +23,10 @@ __all__ = [
     "Context", "OphpcConfig", "OphpcError", "make_config", "lib", "lib_path",
     "DIFF_RS", "DIFF_FRESNEL", "MODE_CPU", "MODE_GPU", "MODE_DOUBLE", "MODE_FLOAT", "MODE_FASTMATH",
     "MODE_TENSOR_FP16", "MODE_TENSOR_BF16X3", "ENCODE_PHASE", "ENCODE_AMPLITUDE", "ENCODE_REAL",
-    "ENCODE_IMAGINARY", "ENCODE_SIMPLENI", "ENCODE_BURCKHARDT", "ENCODE_TWOPHASE",
+    "ENCODE_IMAGINARY", "ENCODE_SIMPLENI", "ENCODE_BURCKHARDT", "ENCODE_TWOPHASE", "Plan", "PLAN_NO_ENCODE",
 ]
+
+PLAN_NO_ENCODE = 0xFFFFFFFF
 
 
 class Context:
@@ -86,6 +88,50 @@ class Context:
                                     encode_flag, ctypes.c_void_p(d_encoded or 0), ctypes.c_void_p(d_normalized or 0),
                                     ctypes.c_void_p(stream))
         self._check(st, "ophpc_encode")
+
+    def plan(self, cfg: OphpcConfig, d_vertices: int, n_points: int, diff_flag: int, mode: int, d_field: int,
+             encode_flag: int = PLAN_NO_ENCODE, d_encoded: Optional[int] = None,
+             d_normalized: Optional[int] = None) -> "Plan":
+        """generate (+ encode) captured once into a CUDA graph (ophpc_plan_create)."""
+        h = ctypes.c_void_p()
+        st = self._lib.ophpc_plan_create(self._h, ctypes.byref(cfg), ctypes.c_void_p(d_vertices),
+                                         ctypes.c_uint64(n_points), diff_flag, mode, ctypes.c_void_p(d_field),
+                                         encode_flag, ctypes.c_void_p(d_encoded or 0),
+                                         ctypes.c_void_p(d_normalized or 0), ctypes.byref(h))
+        self._check(st, "ophpc_plan_create")
+        return Plan(self, h)
+
+
+class Plan:
+    """A captured generate (+ encode); launch() replays it, wait() synchronises
+    the stream and raises on a kernel timeout."""
+
+    def __init__(self, ctx: Context, handle: ctypes.c_void_p):
+        self._ctx = ctx
+        self._h = handle
+
+    def launch(self, stream: int = 0) -> None:
+        self._ctx._check(self._ctx._lib.ophpc_plan_launch(self._h, ctypes.c_void_p(stream)), "ophpc_plan_launch")
+
+    def wait(self, stream: int = 0) -> None:
+        self._ctx._check(self._ctx._lib.ophpc_plan_wait(self._h, ctypes.c_void_p(stream)), "ophpc_plan_wait")
+
+    def close(self) -> None:
+        if self._h:
+            self._ctx._lib.ophpc_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):  # pragma: no cover - interpreter shutdown order
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def build(force: bool = False) -> str:

@@ -98,6 +98,14 @@ def _declare(L: ctypes.CDLL) -> None:
     L.ophpc_generate_host.restype = ctypes.c_int
     L.ophpc_encode.argtypes = [vp, vp, u32, u64, u32, vp, vp, vp]
     L.ophpc_encode.restype = ctypes.c_int
+    L.ophpc_plan_create.argtypes = [vp, ctypes.POINTER(OphpcConfig), vp, u64, u32, u32, vp, u32, vp, vp,
+                                    ctypes.POINTER(vp)]
+    L.ophpc_plan_create.restype = ctypes.c_int
+    for fn in ("ophpc_plan_launch", "ophpc_plan_wait"):
+        getattr(L, fn).argtypes = [vp, vp]
+        getattr(L, fn).restype = ctypes.c_int
+    L.ophpc_plan_destroy.argtypes = [vp]
+    L.ophpc_plan_destroy.restype = ctypes.c_int
 
 
 def lib() -> ctypes.CDLL:

@@ -19,6 +19,7 @@
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 
@@ -179,9 +180,12 @@ cudaError_t pool_alloc(ophpc_context* ctx, T** p, size_t bytes, cudaStream_t s) 
 
 // Device-side generate shared by the device and host entry points.
 // accumulate: add into d_field instead of overwriting it (plain kernels only).
+// d_err_out: the tensor-core paths copy their kernels' timeout word there
+// instead of waiting for the stream (graph capture).
 ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                              uint64_t n_points, uint32_t diff_flag, uint32_t mode, double* d_field,
-                             cudaStream_t s, int color_offset = 0, bool accumulate = false) {
+                             cudaStream_t s, int color_offset = 0, bool accumulate = false,
+                             int* d_err_out = nullptr) {
     JobGeom jg = make_geom(cfg, (int64_t)n_points);
     jg.accumulate = accumulate ? 1 : 0;
     const int64_t plane = (int64_t)cfg->pixel_number[0] * cfg->pixel_number[1];
@@ -193,10 +197,12 @@ ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const 
         return e == cudaSuccess ? OPHPC_SUCCESS : cuda_fail(ctx, e, "cudaMemsetAsync(field)");
     }
     if (tensor && !accumulate) {
-        return tc_generate_fresnel(ctx->pool, cfg, d_vertices, n_points, mode, d_field, s, &ctx->last_error);
+        return tc_generate_fresnel(ctx->pool, cfg, d_vertices, n_points, mode, d_field, s, &ctx->last_error,
+                                   d_err_out);
     }
     if (diff_flag == OPHPC_DIFF_RS && (mode & OPHPC_MODE_TENSOR_BF16X3) && !accumulate && color_offset == 0) {
-        return tc_generate_rs(ctx->pool, jg, cfg, d_vertices, n_points, d_field, ctx->sm_count, s, &ctx->last_error);
+        return tc_generate_rs(ctx->pool, jg, cfg, d_vertices, n_points, d_field, ctx->sm_count, s, &ctx->last_error,
+                              d_err_out);
     }
     const int bps = diff_flag == OPHPC_DIFF_RS ? ctx->rs_bps : ctx->fr_bps;
     choose_split(jg, ctx->sm_count * bps);
@@ -263,6 +269,36 @@ ophpc_status generate_accumulate(ophpc_context* ctx, const ophpc_config* cfg, co
 }
 
 }  // namespace ophpc
+
+namespace {
+
+// ophpc_encode after validation (also captured into plans).
+ophpc_status encode_device(ophpc_context* ctx, const double* d_field, uint32_t n_channels, uint64_t n_pixels,
+                           uint32_t encode_flag, double* d_encoded, uint8_t* d_normalized, cudaStream_t s) {
+    unsigned long long* d_mm = nullptr;
+    cudaError_t e = pool_alloc(ctx, &d_mm, 8 * sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation (min/max)");
+    double* d_tmp = nullptr;
+    if (encode_flag >= OPHPC_ENCODE_SIMPLENI && !d_encoded) {
+        const size_t bytes = sizeof(double) * (size_t)n_channels * (size_t)n_pixels;
+        e = pool_alloc(ctx, &d_tmp, bytes, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(d_tmp, 0, bytes, s);
+        if (e != cudaSuccess) {
+            if (d_tmp) cudaFreeAsync(d_tmp, s);
+            cudaFreeAsync(d_mm, s);
+            return cuda_fail(ctx, e, "scratch allocation (encoded)");
+        }
+    }
+    launch_encode((const double2*)d_field, (int)n_channels, (int64_t)n_pixels, (int)encode_flag,
+                  d_tmp ? d_tmp : d_encoded, d_normalized, d_mm, s);
+    e = cudaGetLastError();
+    if (d_tmp) cudaFreeAsync(d_tmp, s);
+    cudaFreeAsync(d_mm, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "encode launch");
+    return OPHPC_SUCCESS;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -437,28 +473,8 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_normalized must be device memory");
     if (!aligned(d_field, 16) || !aligned(d_encoded, 8))
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_encoded 8-byte aligned");
-    cudaStream_t s = (cudaStream_t)stream;
-    unsigned long long* d_mm = nullptr;
-    cudaError_t e = pool_alloc(ctx, &d_mm, 8 * sizeof(unsigned long long), s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation (min/max)");
-    double* d_tmp = nullptr;
-    if (encode_flag >= OPHPC_ENCODE_SIMPLENI && !d_encoded) {
-        const size_t bytes = sizeof(double) * (size_t)n_channels * (size_t)n_pixels;
-        e = pool_alloc(ctx, &d_tmp, bytes, s);
-        if (e == cudaSuccess) e = cudaMemsetAsync(d_tmp, 0, bytes, s);
-        if (e != cudaSuccess) {
-            if (d_tmp) cudaFreeAsync(d_tmp, s);
-            cudaFreeAsync(d_mm, s);
-            return cuda_fail(ctx, e, "scratch allocation (encoded)");
-        }
-    }
-    launch_encode((const double2*)d_field, (int)n_channels, (int64_t)n_pixels, (int)encode_flag,
-                  d_tmp ? d_tmp : d_encoded, d_normalized, d_mm, s);
-    e = cudaGetLastError();
-    if (d_tmp) cudaFreeAsync(d_tmp, s);
-    cudaFreeAsync(d_mm, s);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "encode launch");
-    return OPHPC_SUCCESS;
+    return encode_device(ctx, d_field, n_channels, n_pixels, encode_flag, d_encoded, d_normalized,
+                         (cudaStream_t)stream);
 }
 
 ophpc_status ophpc_normalize(ophpc_context* ctx, const double* d_encoded, uint32_t n_channels, uint64_t n_pixels,
@@ -486,4 +502,118 @@ ophpc_status ophpc_normalize(ophpc_context* ctx, const double* d_encoded, uint32
     return OPHPC_SUCCESS;
 }
 
+// ---- plans: one generate (+ encode) captured into a CUDA graph ---------------
+
+struct ophpc_plan {
+    ophpc_context* ctx = nullptr;
+    int device = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int* d_err = nullptr;   // the tensor-core kernels' timeout word of the last replay
+};
+
+ophpc_status ophpc_plan_create(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
+                               uint64_t n_points, uint32_t diff_flag, uint32_t mode, double* d_field,
+                               uint32_t encode_flag, double* d_encoded, uint8_t* d_normalized, ophpc_plan** out) {
+    if (!ctx || !out) return OPHPC_ERROR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    ophpc_status st = check_job(ctx, cfg, n_points, diff_flag, mode);
+    if (st != OPHPC_SUCCESS) return st;
+    DeviceGuard guard(ctx->device);
+    if (!d_field || !is_device_ptr(d_field))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be device memory");
+    if (n_points > 0 && (!d_vertices || !is_device_ptr(d_vertices)))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_vertices must be device memory");
+    if (!aligned(d_field, 16) || !aligned(d_vertices, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_vertices 8-byte aligned");
+    const bool enc = encode_flag != OPHPC_PLAN_NO_ENCODE;
+    const uint64_t n_pixels = (uint64_t)cfg->pixel_number[0] * cfg->pixel_number[1];
+    if (enc) {
+        if (encode_flag > OPHPC_ENCODE_TWOPHASE)
+            return fail(ctx, OPHPC_ERROR_UNSUPPORTED,
+                        "encode_flag: phase, amplitude, real, imaginary, SimpleNI, Burckhardt or TwoPhase only");
+        if ((d_encoded && !is_device_ptr(d_encoded)) || (d_normalized && !is_device_ptr(d_normalized)))
+            return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded and d_normalized must be device memory");
+        if (!aligned(d_encoded, 8)) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded must be 8-byte aligned");
+    }
+    std::unique_ptr<ophpc_plan> plan(new ophpc_plan());
+    plan->ctx = ctx;
+    plan->device = ctx->device;
+    cudaError_t e = cudaMalloc((void**)&plan->d_err, sizeof(int));
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaMalloc(plan error word)");
+    auto release = [&]() {
+        if (plan->exec) cudaGraphExecDestroy(plan->exec);
+        if (plan->graph) cudaGraphDestroy(plan->graph);
+        cudaFree(plan->d_err);
+    };
+    cudaStream_t cs = nullptr;
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        release();
+        return cuda_fail(ctx, e, "cudaStreamCreate(capture)");
+    }
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        e = cudaMemsetAsync(plan->d_err, 0, sizeof(int), cs);
+        if (e == cudaSuccess)
+            st = generate_device(ctx, cfg, d_vertices, n_points, diff_flag, mode, d_field, cs, 0, false, plan->d_err);
+        if (e == cudaSuccess && st == OPHPC_SUCCESS && enc && n_pixels > 0)
+            st = encode_device(ctx, d_field, cfg->n_channels, n_pixels, encode_flag, d_encoded, d_normalized, cs);
+        // end the capture whatever happened, so that the stream is usable
+        const cudaError_t ee = cudaStreamEndCapture(cs, &plan->graph);
+        if (e == cudaSuccess) e = ee;
+    }
+    cudaStreamDestroy(cs);
+    if (st != OPHPC_SUCCESS) {
+        release();
+        return st;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&plan->exec, plan->graph, 0);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        release();
+        return cuda_fail(ctx, e, "graph capture");
+    }
+    *out = plan.release();
+    return OPHPC_SUCCESS;
+}
+
+ophpc_status ophpc_plan_launch(ophpc_plan* plan, void* stream) {
+    if (!plan) return OPHPC_ERROR_INVALID_ARGUMENT;
+    DeviceGuard guard(plan->device);
+    const cudaError_t e = cudaGraphLaunch(plan->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        std::lock_guard<std::mutex> lk(plan->ctx->mu);
+        return cuda_fail(plan->ctx, e, "cudaGraphLaunch");
+    }
+    return OPHPC_SUCCESS;
+}
+
+ophpc_status ophpc_plan_wait(ophpc_plan* plan, void* stream) {
+    if (!plan) return OPHPC_ERROR_INVALID_ARGUMENT;
+    DeviceGuard guard(plan->device);
+    int herr = 0;
+    cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, plan->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    std::lock_guard<std::mutex> lk(plan->ctx->mu);
+    if (e != cudaSuccess) return cuda_fail(plan->ctx, e, "plan wait");
+    if (herr) return fail(plan->ctx, OPHPC_ERROR_TIMEOUT, "tensor-core kernel wait timed out");
+    return OPHPC_SUCCESS;
+}
+
+ophpc_status ophpc_plan_destroy(ophpc_plan* plan) {
+    if (!plan) return OPHPC_ERROR_INVALID_ARGUMENT;
+    DeviceGuard guard(plan->device);
+    cudaGraphExecDestroy(plan->exec);
+    cudaGraphDestroy(plan->graph);
+    cudaFree(plan->d_err);
+    delete plan;
+    return OPHPC_SUCCESS;
+}
+
 }  // extern "C"
+
+
+

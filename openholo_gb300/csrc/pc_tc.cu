@@ -505,7 +505,7 @@ void launch_tc_fresnel_finalize(const double* sum_re, const double* sum_im, cons
 
 ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                                  uint64_t n_points, uint32_t mode, double* d_field, cudaStream_t s,
-                                 std::string* err) {
+                                 std::string* err, int* d_err_out) {
     auto fail = [&](ophpc_status st, const char* msg) {
         if (err) *err = msg;
         return st;
@@ -585,8 +585,12 @@ ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, co
     }
     if (e == cudaSuccess) e = cudaGetLastError();
     int herr = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (d_err_out) {   // read later by the caller (graph capture: nothing here may wait)
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_err_out, errw, sizeof(int), cudaMemcpyDeviceToDevice, s);
+    } else {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
     cudaFreeAsync(buf, s);
     if (e != cudaSuccess) return fail(OPHPC_ERROR_CUDA, cudaGetErrorString(e));
     if (herr) return fail(OPHPC_ERROR_TIMEOUT, "tensor-core kernel wait timed out");

@@ -34,8 +34,11 @@ cudaError_t launch_tc_fresnel_chunk(const TcFresnelPlan& plan, const PointRec* d
 void launch_tc_fresnel_finalize(const double* sum_re, const double* sum_im, const float* d_cmax, int64_t plane,
                                 double2* d_field_ch, cudaStream_t stream);
 
+// Tensor-core Fresnel generate. Synchronises `stream` at the end to read the
+// kernels' error word, unless d_err_out is given: then that device word
+// receives it (stream-ordered) and nothing waits (graph capture).
 ophpc_status tc_generate_fresnel(cudaMemPool_t pool, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                                  uint64_t n_points, uint32_t mode, double* d_field, cudaStream_t stream,
-                                 std::string* err);
+                                 std::string* err, int* d_err_out = nullptr);
 
 }  // namespace ophpc

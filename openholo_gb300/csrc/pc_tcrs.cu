@@ -571,7 +571,7 @@ size_t align_up(size_t v, size_t al) { return (v + al - 1) / al * al; }
 
 ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
                             const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, int sm_count,
-                            cudaStream_t s, std::string* err) {
+                            cudaStream_t s, std::string* err, int* d_err_out) {
     auto fail = [&](ophpc_status st, const char* msg) {
         if (err) *err = msg;
         return st;
@@ -678,8 +678,14 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
 
     cudaError_t e = cudaGetLastError();
     int herr = 0;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (d_err_out) {
+        // the caller reads the timeout word later (graph capture: nothing
+        // here may wait for the stream)
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_err_out, errw, sizeof(int), cudaMemcpyDeviceToDevice, s);
+    } else {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
     cudaFreeAsync(buf, s);
     if (e != cudaSuccess) return fail(OPHPC_ERROR_CUDA, cudaGetErrorString(e));
     if (herr) return fail(OPHPC_ERROR_TIMEOUT, "tensor-core RS kernel wait timed out");

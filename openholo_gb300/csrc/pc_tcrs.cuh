@@ -123,10 +123,12 @@ __device__ __forceinline__ bool rs_tc_eligible(const PointRec& p, const RsTcTile
 // Host entry (pc_tcrs.cu): RS generate on the tensor cores plus the
 // CUDA-core complement. jg comes from the plain path's geometry; sm_count
 // sizes the point-range split. The call synchronises `stream` at the end to
-// read the kernels' error word.
+// read the kernels' error word, unless d_err_out is given: then that device
+// word receives it (stream-ordered) and nothing waits, so that the call can
+// be captured into a CUDA graph.
 ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
                             const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field, int sm_count,
-                            cudaStream_t stream, std::string* err);
+                            cudaStream_t stream, std::string* err, int* d_err_out = nullptr);
 
 // Building blocks for callers that run a job as point-range steps (the
 // serving engine). launch_rs_amax: per channel the largest coef / z^2 of the
