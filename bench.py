@@ -302,6 +302,47 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
     return out
 
 
+def plan_leg(ctx, sp, reps: int = 50):
+    """Small repeated jobs: host wall time of one synchronised generate +
+    phase encode through the direct calls and through a plan (the same calls
+    captured once into a CUDA graph and replayed; ophpc_plan_*), 512x512,
+    2,000 points, per tensor-core path."""
+    import torch
+
+    import openholo_gb300 as oph
+    n, pnx, pny = 2000, 512, 512
+    rng = np.random.default_rng(11)
+    v = np.zeros((n, 7))
+    v[:, 0:2] = rng.uniform(-1e-3, 1e-3, (n, 2))
+    v[:, 2] = rng.uniform(0.45, 0.55, n)
+    v[:, 3:6] = 1.0 - rng.uniform(0.0, 1.0, (n, 3))
+    cfg = oph.make_config(pnx=pnx, pny=pny, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    dv = torch.from_numpy(v).cuda()
+    f = torch.empty((1, pny, pnx, 2), dtype=torch.float64, device="cuda")
+    codes = torch.empty((1, pnx * pny), dtype=torch.uint8, device="cuda")
+    out = {"workload": "512x512, 2,000 points, 532 nm, generate + phase encode, synchronised"}
+    for name, diff in (("rs_tc_bf16x3", oph.DIFF_RS), ("fresnel_tc_bf16x3", oph.DIFF_FRESNEL)):
+        def direct():
+            ctx.generate(cfg, dv.data_ptr(), n, diff, oph.MODE_TENSOR_BF16X3, f.data_ptr(), sp)
+            ctx.encode(f.data_ptr(), 1, pnx * pny, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
+            torch.cuda.synchronize()
+        with ctx.plan(cfg, dv.data_ptr(), n, diff, oph.MODE_TENSOR_BF16X3, f.data_ptr(), oph.ENCODE_PHASE, None,
+                      codes.data_ptr()) as plan:
+            def replay():
+                plan.launch(sp)
+                plan.wait(sp)
+            ms = {}
+            for key, fn in (("direct_ms", direct), ("plan_ms", replay)):
+                for _ in range(5):
+                    fn()
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    fn()
+                ms[key] = (time.perf_counter() - t0) / reps * 1e3
+        out[name] = ms
+    return out
+
+
 # ------------------------------------------------------------------ GPU arm
 
 def gpu_arm(args, w):
@@ -418,6 +459,7 @@ def gpu_arm(args, w):
     serving = None
     if os.environ.get("OPHPC_BENCH_SKIP_SERVING") != "1" and world == 1:
         serving = serving_leg(args.serving_jobs, args.serving_max_points)
+    plan_replay = plan_leg(ctx, sp)
 
     # --- end to end through the host-facing ABI ------------------------------
     hv = torch.from_numpy(w.vertices).pin_memory()
@@ -552,6 +594,7 @@ def gpu_arm(args, w):
                         "kernel": "fresnel_kernel (FP32 cores, separable)"},
             "tensor_fresnel": tensor,
             "serving": serving,
+            "plan_replay": plan_replay,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": t_e2e * 1e3},
             "gpu_launches": int(launches),
