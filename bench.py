@@ -467,12 +467,19 @@ def gpu_arm(args, w):
     hcodes = torch.empty((nch, npx), dtype=torch.uint8).pin_memory()
     dv2 = torch.empty_like(dv)
 
+    # the field download runs on a second stream once the generate is done,
+    # overlapping the encode
+    side = torch.cuda.Stream()
+
     def e2e_step():
         dv2.copy_(hv, non_blocking=True)
         ctx.generate(cfg, dv2.data_ptr(), w.n_points, oph.DIFF_RS, rs_mode, field.data_ptr(), sp)
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            hfield.copy_(field, non_blocking=True)
         ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
-        hfield.copy_(field, non_blocking=True)
         hcodes.copy_(codes, non_blocking=True)
+        torch.cuda.current_stream().wait_stream(side)
 
     e2e_step()
     torch.cuda.synchronize()
