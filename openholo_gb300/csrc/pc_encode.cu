@@ -241,6 +241,183 @@ __global__ void __launch_bounds__(256) encode_normalised_kernel(const double2* _
     }
 }
 
+
+// ---- phase / amplitude codes without the FP64 values -----------------------
+// With no m_lpEncoded wanted, the codes come from FP32 estimates of the
+// encoded values; FP64 (the functions above) only where an estimate cannot
+// decide. The codes are the FP64 path's, bit for bit:
+//   - the exact min/max: pixels whose estimate lies within twice its error
+//     bound of the estimated min/max (the pixel that holds the exact one is
+//     always among them) and pixels without a usable estimate, in FP64;
+//   - a code: from the estimate unless it lies within its error bound of a
+//     code boundary, else in FP64.
+// Error bounds, in units of the encoded value: phase 1e-6 (inputs truncated
+// to 20 mantissa bits: <= 9.5e-7 rad; atan2f: <= 3 ulp of pi; the FP32
+// offset and scale: <= 3.3e-7 rad; / 2 pi = 3.2e-7, bound taken 3x),
+// amplitude 4e-6 relative (<= 9.5e-7 from the inputs + 4 ulp, bound 3x).
+constexpr float kPhaseErr = 1e-6f;
+constexpr float kAmpErrRel = 4e-6f;
+
+// FP32 image of a double from its high word: sign, exponent, the top 20
+// mantissa bits (truncated: relative error < 2^-20). ok turns false where
+// the image cannot stand in: subnormal, or outside 2^-62 .. 2^62 (squares
+// stay normal floats), infinite or NaN.
+__device__ __forceinline__ float hi_float(double d, bool& ok) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned hi = (unsigned)(b >> 32);
+    const int ex = (int)((hi >> 20) & 0x7ffu);
+    const unsigned sign = hi & 0x80000000u;
+    if (ex == 0) {
+        if ((hi & 0xfffffu) | (unsigned)b) ok = false;   // subnormal
+        return __int_as_float((int)sign);                  // signed zero, as atan2 sees it
+    }
+    if (ex < 1023 - 62 || ex > 1023 + 62) {
+        ok = false;
+        return 0.f;
+    }
+    return __int_as_float((int)(sign | ((unsigned)(ex - 1023 + 127) << 23) | ((hi & 0xfffffu) << 3)));
+}
+
+template <int FLAG>
+__device__ __forceinline__ float estimate(double2 h, bool& ok) {
+    ok = true;
+    const float x = hi_float(h.x, ok), y = hi_float(h.y, ok);
+    if (FLAG == 0) return (atan2f(y, x) + 3.14159265f) * 0.159154943f;
+    return sqrtf(x * x + y * y);
+}
+
+__device__ __forceinline__ unsigned ordered32(float f) {
+    const unsigned b = (unsigned)__float_as_int(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float from_ordered32(unsigned b) {
+    return __int_as_float((int)((b & 0x80000000u) ? (b & 0x7fffffffu) : ~b));
+}
+
+// exact min/max words [0], [1]; estimated min/max (ordered 32-bit) in the
+// two halves of word [2]
+__global__ void init_est_minmax_kernel(unsigned long long* minmax) {
+    minmax[0] = ordered_bits(kMaxDouble);
+    minmax[1] = ordered_bits(kMinDouble);
+    unsigned* w = reinterpret_cast<unsigned*>(minmax + 2);
+    w[0] = ordered32(__int_as_float(0x7f800000));    // +inf
+    w[1] = ordered32(__int_as_float((int)0xff800000u));   // -inf
+}
+
+// block reduction of a min and a max pair of doubles into the exact words
+__device__ __forceinline__ void fold_exact(double mn, double mx, unsigned long long* minmax) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    __shared__ double s_mn[8], s_mx[8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_mn[w] = mn;
+        s_mx[w] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
+            mn = fmin(mn, s_mn[k]);
+            mx = fmax(mx, s_mx[k]);
+        }
+        if (mn != kMaxDouble) atomicMin(&minmax[0], ordered_bits(mn));
+        if (mx != kMinDouble) atomicMax(&minmax[1], ordered_bits(mx));
+    }
+}
+
+// pass 1: estimated min/max; pixels without an estimate go to the exact words
+template <int FLAG>
+__global__ void __launch_bounds__(256) est_minmax_kernel(const double2* __restrict__ field, int64_t n,
+                                                         unsigned long long* __restrict__ minmax) {
+    float mn = __int_as_float(0x7f800000), mx = -mn;
+    double emn = kMaxDouble, emx = kMinDouble;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 h = field[i];
+        bool ok;
+        const float e = estimate<FLAG>(h, ok);
+        if (ok) {
+            mn = fminf(mn, e);
+            mx = fmaxf(mx, e);
+        } else {
+            const double x = encode_value(h, FLAG);
+            if (x < emn) emn = x;
+            if (x > emx) emx = x;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    unsigned* w = reinterpret_cast<unsigned*>(minmax + 2);
+    if ((threadIdx.x & 31) == 0) {
+        atomicMin(&w[0], ordered32(mn));
+        atomicMax(&w[1], ordered32(mx));
+    }
+    fold_exact(emn, emx, minmax);
+}
+
+template <int FLAG>
+__device__ __forceinline__ float est_band(float mx_est) {
+    return FLAG == 0 ? 2.f * kPhaseErr : 2.f * kAmpErrRel * fabsf(mx_est);
+}
+
+// pass 2: the exact value of every pixel whose estimate is within the band
+// of the estimated min or max
+template <int FLAG>
+__global__ void __launch_bounds__(256) refine_minmax_kernel(const double2* __restrict__ field, int64_t n,
+                                                            unsigned long long* __restrict__ minmax) {
+    const unsigned* w = reinterpret_cast<const unsigned*>(minmax + 2);
+    const float mn_e = from_ordered32(w[0]), mx_e = from_ordered32(w[1]);
+    const float band = est_band<FLAG>(mx_e);
+    double emn = kMaxDouble, emx = kMinDouble;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 h = field[i];
+        bool ok;
+        const float e = estimate<FLAG>(h, ok);
+        if (ok && (e <= mn_e + band || e >= mx_e - band)) {
+            const double x = encode_value(h, FLAG);
+            if (x < emn) emn = x;
+            if (x > emx) emx = x;
+        }
+    }
+    fold_exact(emn, emx, minmax);
+}
+
+// pass 3: the codes
+template <int FLAG>
+__global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restrict__ field, int64_t n,
+                                                        const unsigned long long* __restrict__ minmax,
+                                                        uint8_t* __restrict__ out) {
+    const double mn = from_ordered(minmax[0]);
+    const double mx = from_ordered(minmax[1]);
+    const double gap = __dsub_rn(mx, mn);
+    const bool usable = gap > 0.0 && gap < 1e30 && mn > -1e30 && mn < 1e30;
+    const float mn_f = (float)mn, sc_f = usable ? (float)(255.0 / gap) : 0.f;
+    const float err = FLAG == 0 ? kPhaseErr : kAmpErrRel * (float)fmax(fabs(mx), fabs(mn));
+    // estimate error in code units, the FP32 rounding of the code itself on top
+    const float margin = 2.f * err * sc_f + 1e-4f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 h = field[i];
+        bool ok;
+        const float e = estimate<FLAG>(h, ok);
+        const float v = (e - mn_f) * sc_f + 0.5f;
+        const float fl = floorf(v);
+        uint8_t code;
+        if (usable && ok && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f) {
+            code = (uint8_t)(int)fl;
+        } else {
+            const double x = encode_value(h, FLAG);
+            const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(x, mn), gap), 255.0), 0.5);
+            code = (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
+        }
+        out[i] = code;
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -282,6 +459,21 @@ void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int
         if (d_normalized) {
             minmax_kernel<<<blocks, threads, 0, stream>>>(d_encoded, n, d_minmax);
             normalize_kernel<<<blocks, threads, 0, stream>>>(nullptr, d_encoded, n, 0, d_minmax, d_normalized);
+        }
+        return;
+    }
+    if (!d_encoded && d_normalized && (encode_flag == 0 || encode_flag == 1)) {
+        // codes only: FP32 estimates, FP64 where they cannot decide
+        count_launches(4);
+        init_est_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
+        if (encode_flag == 0) {
+            est_minmax_kernel<0><<<blocks, threads, 0, stream>>>(d_field, n, d_minmax);
+            refine_minmax_kernel<0><<<blocks, threads, 0, stream>>>(d_field, n, d_minmax);
+            est_codes_kernel<0><<<blocks, threads, 0, stream>>>(d_field, n, d_minmax, d_normalized);
+        } else {
+            est_minmax_kernel<1><<<blocks, threads, 0, stream>>>(d_field, n, d_minmax);
+            refine_minmax_kernel<1><<<blocks, threads, 0, stream>>>(d_field, n, d_minmax);
+            est_codes_kernel<1><<<blocks, threads, 0, stream>>>(d_field, n, d_minmax, d_normalized);
         }
         return;
     }
