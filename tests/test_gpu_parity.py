@@ -1,6 +1,6 @@
 """GPU parity: libophpc (through the C ABI) against the CPU oracle.
 
-Tolerances (spec bar, stated here): complex field relative L2 error
+Tolerances (the accuracy bar, stated here): complex field relative L2 error
 <= 1e-4 against the FP64 oracle, and the 8-bit encoded hologram exact on
 >= 99.9% of pixels and within +-1 LSB elsewhere (phase codes compared
 circularly, 255 and 0 being neighbours). The oracle restates the reference CPU

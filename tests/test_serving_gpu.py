@@ -1,6 +1,6 @@
 """Serving engine: continuous batching of mixed hologram jobs.
 
-The bar (the benchmark spec): a job's result is the same alone and in the mix, and
+The bar: a job's result is the same alone and in the mix, and
 jobs that arrive while others run are admitted and overlap on the device.
 Alone-vs-mix results are compared bit for bit (each job's chunking and FP64
 accumulation order are fixed by the job alone); against the single-call

@@ -2,7 +2,7 @@
 
 Tolerances, stated per precision:
   split-BF16 (hi/lo, three products, FP32 accumulation): relL2 <= 1e-4, the
-      spec bar, and the 8-bit phase encoding exact on >= 99.9% of pixels
+      accuracy bar, and the 8-bit phase encoding exact on >= 99.9% of pixels
       within +-1 LSB;
   FP16 (one product): relL2 <= 1e-3 — an 11-bit significand leaves ~1e-4 per
       table entry, so FP16 cannot reach 1e-4 and the measured error is

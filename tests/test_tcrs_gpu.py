@@ -5,7 +5,7 @@ Within each 128x128 tile the RS term is expanded into a row factor times a
 column factor plus a first-order cross pair, and contracted over the points
 on the tensor cores in split-BF16 (the cross pair in FP16) with FP32
 accumulation; pairs the expansion does not hold for are added by the
-CUDA-core RS kernel. Tolerances: relL2 <= 1e-4 against FP64 (the north-star
+CUDA-core RS kernel. Tolerances: relL2 <= 1e-4 against FP64 (the accuracy
 bar), 8-bit phase codes exact on >= 99.9% of pixels and within +-1 LSB.
 """
 import numpy as np
