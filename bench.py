@@ -632,7 +632,7 @@ def measured_peaks() -> dict:
 # dram__bytes_read.sum + dram__bytes_write.sum of one tc_rs_kernel launch of
 # the workload's tensor-core RS generate, from a 1-pass ncu capture of
 # `bench.py --profile-case tcrs_fhd_full` (profiles/tc_rs_kernel_sphere_fhd.md).
-TCRS_TRAFFIC_BYTES = {"sphere_fhd": 20485888 + 261314816}
+TCRS_TRAFFIC_BYTES = {"sphere_fhd": 21441280 + 255688192}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one rs_kernel launch of the

@@ -27,10 +27,12 @@
 //               layout: split-BF16 (hi + lo) for R and C, FP16 for the cross
 //               pair;
 //   warp 8      allocates 512 TMEM columns; its lane 0 only issues per stage
-//               eight tcgen05.mma kind::f16, M=128, N=256, K=16: the N=256
-//               B operand [Br; Bi] (or [-Bi; Br]) yields D_re and D_im of
-//               one product at once; passes (hi,hi), (hi,lo), (lo,hi) in
-//               BF16 and the cross pair in FP16;
+//               twelve tcgen05.mma kind::f16, M=128, K=16, three per complex
+//               product: Ar x [Br; Bi] (N=256: D_re and D_im at once), then
+//               D_re -= Ai Bi (N=128, the instruction's negate-A bit) and
+//               D_im += Ai Br (N=128), so that no negated plane is stored;
+//               products (hi,hi), (hi,lo), (lo,hi) in BF16 and the cross
+//               pair in FP16;
 //   warps 0-7   also drain the TMEM accumulator D: every 64 stages (1024
 //               points; the tensor core's FP32 accumulation loses ~1e-8 of
 //               the sum per point) into a running sum S in the other 256
@@ -68,9 +70,8 @@ constexpr int kThreadsTc = kProducers + 32 + kRecThreads;   // 384: 12 warps, 16
 constexpr int kStagePts = 16;                            // points per stage: one K=16 MMA step
 constexpr int kStagesTc = 3;
 constexpr int kPlane = kRsTcTile * kStagePts * 2;        // 4096 B: 128 rows x 32 B
-// planes of one stage (kB?n: the negated imaginary plane, so that [Bn; Br]
-// and [Br; Bi] are both contiguous N=256 operands)
-enum : int { kAhr = 0, kAhi, kAlr, kAli, kA2r, kA2i, kBhn, kBhr, kBhi, kBln, kBlr, kBli, kB2n, kB2r, kB2i, kPlanes };
+// planes of one stage ([Br; Bi] of each B part contiguous: one N=256 operand)
+enum : int { kAhr = 0, kAhi, kAlr, kAli, kA2r, kA2i, kBhr, kBhi, kBlr, kBli, kB2r, kB2i, kPlanes };
 constexpr int kStageBytesTc = kPlanes * kPlane;          // 61,440
 constexpr int kChunkTc = kProducers;                     // points per record round (one per producer)
 constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 16
@@ -217,14 +218,10 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
             ST(kA2r, w_xr);
             ST(kA2i, w_xi);
         } else {
-            const uint32_t n = 0x80008000u;   // -Bi: flip both sign bits
-            st_v4(ro + kBhn * kPlane, w_hi[o] ^ n, w_hi[o + 1] ^ n, w_hi[o + 2] ^ n, w_hi[o + 3] ^ n);
             ST(kBhr, w_hr);
             ST(kBhi, w_hi);
-            st_v4(ro + kBln * kPlane, w_li[o] ^ n, w_li[o + 1] ^ n, w_li[o + 2] ^ n, w_li[o + 3] ^ n);
             ST(kBlr, w_lr);
             ST(kBli, w_li);
-            st_v4(ro + kB2n * kPlane, w_xi[o] ^ n, w_xi[o + 1] ^ n, w_xi[o + 2] ^ n, w_xi[o + 3] ^ n);
             ST(kB2r, w_xr);
             ST(kB2i, w_xi);
         }
@@ -232,7 +229,7 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
     }
 }
 
-// Issues the eight MMAs of stage k (the MMA warp's lane 0): waits until the
+// Issues the twelve MMAs of stage k (the MMA warp's lane 0): waits until the
 // producers filled the stage and, when k opens an accumulation run, until
 // every producer warp drained the previous run out of D. Issuing blocks
 // while the tensor core's queue is full (about as long as a stage's MMAs
@@ -240,8 +237,12 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
 __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* full, uint64_t* empty,
                                             uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
                                             uint32_t tmem) {
-    constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);
-    constexpr uint32_t id_h = idesc_f16(0u, false, kRsTcTile, 2 * kRsTcTile);
+    constexpr uint32_t id_bf256 = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);   // BF16, N=256
+    constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, kRsTcTile);          // BF16, N=128
+    constexpr uint32_t id_bfn = idesc_f16(1u, true, kRsTcTile, kRsTcTile);          // BF16, N=128, -A
+    constexpr uint32_t id_h256 = idesc_f16(0u, false, kRsTcTile, 2 * kRsTcTile);    // FP16, ...
+    constexpr uint32_t id_h = idesc_f16(0u, false, kRsTcTile, kRsTcTile);
+    constexpr uint32_t id_hn = idesc_f16(0u, true, kRsTcTile, kRsTcTile);
     const int p = k / kPeriod;
     const bool opens = (k % kPeriod) == 0;
     if (opens && p >= 1 && !mbar_wait_for(acc_empty, (uint32_t)(p - 1) & 1u, abort, kWaitNs)) return false;
@@ -251,14 +252,19 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
     const uint32_t d = tmem;
     const uint32_t st = smem_u32(base + s * kStageBytesTc);
 #define PL(x) sw32_desc(st + (uint32_t)((x) * kPlane))
-    umma(d, PL(kAhr), PL(kBhr), id_bf, opens ? 0u : 1u);   // Ar [Br; Bi]
-    umma(d, PL(kAhi), PL(kBhn), id_bf, 1u);                // Ai [-Bi; Br]
-    umma(d, PL(kAhr), PL(kBlr), id_bf, 1u);
-    umma(d, PL(kAhi), PL(kBln), id_bf, 1u);
-    umma(d, PL(kAlr), PL(kBhr), id_bf, 1u);
-    umma(d, PL(kAli), PL(kBhn), id_bf, 1u);
-    umma(d, PL(kA2r), PL(kB2r), id_h, 1u);
-    umma(d, PL(kA2i), PL(kB2n), id_h, 1u);
+    const uint32_t dre = d, dim = d + kRsTcTile, acc = opens ? 0u : 1u;
+    umma(d, PL(kAhr), PL(kBhr), id_bf256, acc);   // re += Ar Br, im += Ar Bi
+    umma(dre, PL(kAhi), PL(kBhi), id_bfn, 1u);    // re -= Ai Bi
+    umma(dim, PL(kAhi), PL(kBhr), id_bf, 1u);     // im += Ai Br
+    umma(d, PL(kAhr), PL(kBlr), id_bf256, 1u);
+    umma(dre, PL(kAhi), PL(kBli), id_bfn, 1u);
+    umma(dim, PL(kAhi), PL(kBlr), id_bf, 1u);
+    umma(d, PL(kAlr), PL(kBhr), id_bf256, 1u);
+    umma(dre, PL(kAli), PL(kBhi), id_bfn, 1u);
+    umma(dim, PL(kAli), PL(kBhr), id_bf, 1u);
+    umma(d, PL(kA2r), PL(kB2r), id_h256, 1u);
+    umma(dre, PL(kA2i), PL(kB2i), id_hn, 1u);
+    umma(dim, PL(kA2i), PL(kB2r), id_h, 1u);
 #undef PL
     umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
     if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(acc_full);
