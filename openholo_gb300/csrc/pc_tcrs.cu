@@ -41,7 +41,10 @@
 // Pairs for which the expansion does not hold (window cuts the tile, the cone
 // test is not passed by the whole tile, |w| or the cross phase too large:
 // rs_tc_eligible) get zero factors here and are added afterwards by the
-// CUDA-core rs_kernel, which skips exactly the pairs this kernel took.
+// CUDA-core rs_kernel. The record warps mark them in a per-tile bitmask
+// (one ballot word per 32 points, each word written by one warp of one
+// CTA), which that kernel reads: it evaluates exactly the pairs left here
+// and loads no other point.
 //
 // Every mbarrier wait is bounded (%globaltimer); on a timeout the CTA raises
 // an error word, waits (bounded) for its issued MMAs, frees TMEM and returns.
