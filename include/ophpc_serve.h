@@ -55,16 +55,18 @@ typedef struct ophpc_server_options {
     double step_ms;            /* target GPU time of one scheduling step (<= 0: 2 ms) */
 } ophpc_server_options;
 
-/* One hologram job: generateHologram (RS or Fresnel; RS on the tensor cores
- * when mode has OPHPC_MODE_TENSOR_BF16X3) and, when h_codes is set,
- * encoding + normalize. */
+/* One hologram job: generateHologram (RS or Fresnel, on the FP32 cores or,
+ * by mode, on the tensor cores) and, when h_codes is set, encoding +
+ * normalize. */
 typedef struct ophpc_job {
     ophpc_config cfg;
     const ophpc_vertex* h_vertices;  /* host, n_points records */
     uint64_t n_points;
     uint32_t diff_flag;              /* OPHPC_DIFF_RS / OPHPC_DIFF_FRESNEL */
-    uint32_t mode;                   /* OPHPC_MODE_*: OPHPC_MODE_TENSOR_BF16X3 with RS runs on the
-                                        tensor cores; other tensor modes are rejected */
+    uint32_t mode;                   /* OPHPC_MODE_*: RS with OPHPC_MODE_TENSOR_BF16X3, and Fresnel
+                                        with OPHPC_MODE_TENSOR_BF16X3 or OPHPC_MODE_TENSOR_FP16, run
+                                        on the tensor cores; RS with OPHPC_MODE_TENSOR_FP16, or both
+                                        tensor bits at once, is rejected */
     double* h_field;                 /* optional host output [ch][pnY][pnX][re, im] */
     uint8_t* h_codes;                /* optional host output [ch][pnY][pnX] */
     uint32_t encode_flag;            /* OPHPC_ENCODE_* for h_codes */
