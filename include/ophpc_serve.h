@@ -87,7 +87,8 @@ ophpc_status ophpc_server_create(int32_t device, const ophpc_server_options* opt
 ophpc_status ophpc_server_submit(ophpc_server* server, const ophpc_job* job, uint64_t* ticket);
 
 /* Waits for a job (timeout_s < 0: no limit) and forgets its ticket. Returns
- * the job's status, or OPHPC_ERROR_TIMEOUT (the ticket stays valid). */
+ * the job's status, or OPHPC_ERROR_TIMEOUT (the ticket stays valid).
+ * timeout_s = 0 polls: it never blocks on the job. */
 ophpc_status ophpc_server_wait(ophpc_server* server, uint64_t ticket, double timeout_s, ophpc_job_stats* stats);
 
 /* Finishes every queued job, then stops the worker and frees the server. */

@@ -145,6 +145,16 @@ class Server:
             codes = c.numpy().copy() if pinned else c
         return Result(st, s.t_submit, s.t_admit, s.t_done, field, codes)
 
+    def poll(self, ticket: int) -> Optional[Result]:
+        """The job's result if it has finished (the ticket is then spent), else
+        None without blocking (ophpc_server_wait with timeout 0)."""
+        try:
+            return self.wait(ticket, 0.0)
+        except OphpcError as e:
+            if e.status == 8:
+                return None
+            raise
+
     def close(self) -> None:
         if self._h:
             self._L.ophpc_server_destroy(self._h)

@@ -154,3 +154,29 @@ def test_tensor_modes_rejected_where_not_served(gpu_ctx):
         for d, m in ((0, 0x100), (0, 0x300), (1, 0x300)):
             with pytest.raises(OphpcError):
                 srv.submit(g, v, d, mode=m)
+
+
+def test_poll_does_not_block(gpu_ctx):
+    """ophpc_server_wait with timeout 0 polls: None while the job runs, then
+    the job's result, the same as a blocking wait; the ticket is spent
+    after that."""
+    import time
+    from openholo_gb300.serving import Server
+    rng = np.random.default_rng(11)
+    n = 20000
+    v = np.zeros((n, 7))
+    v[:, 0:2] = rng.uniform(-5e-4, 5e-4, (n, 2))
+    v[:, 2] = rng.uniform(0.1, 0.3, n)
+    v[:, 3:6] = 1.0 - rng.uniform(0.0, 1.0, (n, 3))
+    g = dict(pnx=2048, pny=2048, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    with Server(0) as srv:
+        blocking = srv.wait(srv.submit(g, v, 0))
+        t = srv.submit(g, v, 0)
+        assert srv.poll(t) is None      # ~5e10 interactions, polled right after submission
+        r, t0 = None, time.monotonic()
+        while r is None and time.monotonic() - t0 < 60.0:
+            time.sleep(1e-3)
+            r = srv.poll(t)
+        assert r is not None and r.status == 0
+        assert np.array_equal(r.field, blocking.field)
+        assert srv.poll(t).status != 0  # spent ticket: OPHPC_ERROR_INVALID_ARGUMENT
