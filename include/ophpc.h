@@ -173,16 +173,24 @@ ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_
  * fixed budget, or a real-time loop that must never enter cudaMalloc /
  * cudaFree, which can synchronise the whole device. Same arguments and
  * result as ophpc_generate (plain RS and Fresnel kernels; tensor modes return
- * OPHPC_ERROR_UNSUPPORTED), but no context: it runs on the calling thread's
- * current device, and its scratch is one file-scope 32 MiB device array that
- * every GPU loading the library holds until the process exits. It allocates
- * nothing. The first call on a device does a one-time set-up on that device
- * (looks up the array's device address); make that first call before any
- * stream capture. n_points * n_channels above OPHPC_STATIC_SCRATCH_RECORDS is
- * rejected with OPHPC_ERROR_INVALID_ARGUMENT before any work is queued. All
- * calls on a device share the array and it keeps the last call's contents;
- * nothing in it needs to start at zero, but calls whose GPU work overlaps
- * (other streams, unsynchronised threads) race on it. Asynchronous on
+ * OPHPC_ERROR_UNSUPPORTED; a NULL cfg is OPHPC_ERROR_INVALID_ARGUMENT), but no
+ * context: it runs on the calling thread's current device, and its scratch is
+ * one file-scope 32 MiB device array that every GPU loading the library holds
+ * until the process exits. It allocates nothing. Every call looks up the
+ * array's device address on the current device and sets the kernels'
+ * shared-memory limits there (neither allocates), so a device reset between
+ * calls is harmless; the first call on a device also loads the library's
+ * device code there, so make that first call before any stream capture.
+ * n_points * n_channels above OPHPC_STATIC_SCRATCH_RECORDS is rejected with
+ * OPHPC_ERROR_INVALID_ARGUMENT before any work is queued, and so are field
+ * and vertex buffers in another device's memory. A CUDA error already
+ * pending on the calling thread is reported as OPHPC_ERROR_CUDA before any
+ * work is queued and is left pending. All calls on a device share the array
+ * and it keeps the last call's contents; nothing in it needs to start at
+ * zero, but calls whose GPU work overlaps (other streams, unsynchronised
+ * threads) race on it. Small fields run slower than through ophpc_generate:
+ * with no room for partial sums, the point range is never split across CTAs,
+ * so a field of few 64x32 tiles leaves most SMs idle. Asynchronous on
  * `stream`. */
 ophpc_status ophpc_generate_static_scratch(const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                                            uint64_t n_points, uint32_t diff_flag, uint32_t mode,

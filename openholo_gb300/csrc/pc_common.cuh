@@ -181,5 +181,9 @@ void launch_normalize(const double* d_encoded, int n_channels, int64_t n_pixels,
                       unsigned long long* d_minmax, cudaStream_t stream);
 int rs_blocks_per_sm();
 int fresnel_blocks_per_sm();
+// Raise the kernels' dynamic shared-memory limit on the current device (a
+// per-module attribute: it is lost when the context is reset).
+cudaError_t rs_set_smem_limit();
+cudaError_t fresnel_set_smem_limit();
 
 }  // namespace ophpc

@@ -337,8 +337,12 @@ __global__ void sum_partials_kernel(double2* __restrict__ field, const double2* 
 
 constexpr size_t kFresnelSmem = sizeof(FrSRec) * kChunk + sizeof(double2) * kPixH * kPixW * kThreads;
 
+cudaError_t fresnel_set_smem_limit() {
+    return cudaFuncSetAttribute(fresnel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFresnelSmem);
+}
+
 int fresnel_blocks_per_sm() {
-    cudaFuncSetAttribute(fresnel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFresnelSmem);
+    fresnel_set_smem_limit();
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fresnel_kernel, kThreads, kFresnelSmem) != cudaSuccess) nb = 1;
     return nb > 0 ? nb : 1;

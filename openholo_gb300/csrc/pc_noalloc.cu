@@ -15,6 +15,13 @@
 // never split, so there are no partial sums), so nothing has to start at
 // zero. Two calls whose GPU work overlaps (different streams, or different
 // host threads without ordering) race on the array.
+//
+// Nothing is cached between calls: every call looks up the array's device
+// address and sets the kernels' shared-memory limits on the current device
+// (neither allocates). A reset of the device (cudaDeviceReset, or a reset of
+// the primary context) unloads the module, and with it the array and those
+// attributes; the next call then loads the module again and finds the new
+// address, so no stale address is ever handed to a kernel.
 #include "ophpc.h"
 #include "pc_common.cuh"
 
@@ -22,7 +29,6 @@
 
 #include <cmath>
 #include <cstring>
-#include <mutex>
 
 namespace ophpc {
 namespace {
@@ -35,27 +41,17 @@ static_assert(kStaticScratchBytes == 32ull * 1024 * 1024, "32 MiB of point recor
 // cudaGetSymbolAddress (see scratch_on_current_device).
 __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// Per-device set-up, done once under a lock with that device current: the
-// symbol's device address, and the kernels' shared-memory attributes.
+// Per-call set-up with the calling thread's device current: the symbol's
+// device address (a host-side stand-in must never reach a kernel) and the
+// kernels' dynamic shared-memory limits. Both are looked up afresh on every
+// call; neither allocates device memory.
 cudaError_t scratch_on_current_device(void** out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess) return e;
-        rs_blocks_per_sm();        // sets the kernels' dynamic shared-memory limits
-        fresnel_blocks_per_sm();
-        g_scratch_addr[dev] = p;
-    }
-    *out = g_scratch_addr[dev];
+    if ((e = rs_set_smem_limit()) != cudaSuccess) return e;
+    if ((e = fresnel_set_smem_limit()) != cudaSuccess) return e;
+    *out = p;
     return cudaSuccess;
 }
 
@@ -109,13 +105,16 @@ JobGeom geometry(const ophpc_config* c, int64_t n_points) {
     return jg;
 }
 
-bool on_device(const void* p) {
+// Device (or managed) memory of the current device only: a buffer on another
+// GPU would be written through this device's kernels.
+bool on_device(const void* p, int dev) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
+        cudaGetLastError();   // our own query's error; nothing was pending on entry
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace
@@ -125,13 +124,19 @@ extern "C" ophpc_status ophpc_generate_static_scratch(const ophpc_config* cfg, c
                                                       uint64_t n_points, uint32_t diff_flag, uint32_t mode,
                                                       double* d_field, void* stream) {
     using namespace ophpc;
+    // an error already pending on this thread belongs to an earlier call:
+    // report it without queueing work, and leave it pending for its owner
+    if (cudaPeekAtLastError() != cudaSuccess) return OPHPC_ERROR_CUDA;
+    if (!cfg) return OPHPC_ERROR_INVALID_ARGUMENT;
     if (!config_ok(cfg)) return OPHPC_ERROR_CONFIG;
     if (diff_flag != OPHPC_DIFF_RS && diff_flag != OPHPC_DIFF_FRESNEL) return OPHPC_ERROR_INVALID_ARGUMENT;
     if (mode & (OPHPC_MODE_TENSOR_FP16 | OPHPC_MODE_TENSOR_BF16X3)) return OPHPC_ERROR_UNSUPPORTED;
     // the size limit of the static scratch: one 64-byte record per (point, channel)
     if (n_points > (uint64_t)OPHPC_STATIC_SCRATCH_RECORDS / cfg->n_channels) return OPHPC_ERROR_INVALID_ARGUMENT;
-    if (!d_field || !on_device(d_field)) return OPHPC_ERROR_INVALID_ARGUMENT;
-    if (n_points > 0 && (!d_vertices || !on_device(d_vertices))) return OPHPC_ERROR_INVALID_ARGUMENT;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return OPHPC_ERROR_CUDA;
+    if (!d_field || !on_device(d_field, dev)) return OPHPC_ERROR_INVALID_ARGUMENT;
+    if (n_points > 0 && (!d_vertices || !on_device(d_vertices, dev))) return OPHPC_ERROR_INVALID_ARGUMENT;
     // the kernels move the field as 16-byte double2 words and read vertices as doubles
     if (((uintptr_t)d_field & 15) != 0 || ((uintptr_t)d_vertices & 7) != 0) return OPHPC_ERROR_INVALID_ARGUMENT;
     void* scratch = nullptr;

@@ -487,8 +487,12 @@ rs_kernel(const PointRec* __restrict__ recs, const JobGeom jg, double2* __restri
 
 constexpr size_t kRsSmem = sizeof(RsSRec) * kChunk + sizeof(double2) * kPixH * kPixW * kThreads;
 
+cudaError_t rs_set_smem_limit() {
+    return cudaFuncSetAttribute(rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRsSmem);
+}
+
 int rs_blocks_per_sm() {
-    cudaFuncSetAttribute(rs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRsSmem);
+    rs_set_smem_limit();
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, rs_kernel, kThreads, kRsSmem) != cudaSuccess) nb = 1;
     return nb > 0 ? nb : 1;

@@ -74,6 +74,39 @@ def test_static_scratch_matches_allocating_entry_point():
                 assert err <= FIELD_TOL, f"diff={diff}: relL2 {err:.3e}"
 
 
+def test_static_scratch_full_array_and_empty_call():
+    """The largest accepted call fills the array exactly (one channel,
+    OPHPC_STATIC_SCRATCH_RECORDS points); a call with no points writes a zero
+    field over whatever the buffer held."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.fail("GPU test selected but no CUDA device is visible")
+    import openholo_gb300 as oph
+
+    gen_static = _entry(oph.lib())
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    cfg = oph.make_config(64, 64, 8e-6, 8e-6, [532e-9])
+    v = _points(524288, 3, z=(0.2, 0.3))
+    dv = torch.from_numpy(v).cuda()
+    with oph.Context(0) as ctx:
+        for diff in (oph.DIFF_RS, oph.DIFF_FRESNEL):
+            want = torch.empty((1, 64, 64, 2), dtype=torch.float64, device="cuda")
+            got = torch.full_like(want, float("nan"))
+            ctx.generate(cfg, dv.data_ptr(), v.shape[0], diff, 0, want.data_ptr(), stream.cuda_stream)
+            st = gen_static(ctypes.byref(cfg), dv.data_ptr(), v.shape[0], diff, 0, got.data_ptr(),
+                            stream.cuda_stream)
+            assert st == 0, f"status {st}"
+            torch.cuda.synchronize()
+            err = _rel(got.cpu().numpy(), want.cpu().numpy())
+            assert err <= FIELD_TOL, f"diff={diff}, full array: relL2 {err:.3e}"
+    empty = torch.full((1, 64, 64, 2), float("nan"), dtype=torch.float64, device="cuda")
+    st = gen_static(ctypes.byref(cfg), dv.data_ptr(), 0, oph.DIFF_RS, 0, empty.data_ptr(), stream.cuda_stream)
+    assert st == 0, f"status {st}"
+    torch.cuda.synchronize()
+    assert bool((empty == 0).all())
+
+
 def test_static_scratch_rejects_sizes_beyond_its_array():
     torch = pytest.importorskip("torch")
     import openholo_gb300 as oph
@@ -87,3 +120,6 @@ def test_static_scratch_rejects_sizes_beyond_its_array():
     assert st == 1   # OPHPC_ERROR_INVALID_ARGUMENT, rejected before any work is queued
     torch.cuda.synchronize()
     assert not out.any()
+    # a NULL config is an invalid argument, as for ophpc_generate
+    st = gen_static(None, dv.data_ptr(), 4, 0, 0, out.data_ptr(), None)
+    assert st == 1
