@@ -58,13 +58,13 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-points", type=int, default=0, help="points in the CPU sample (0 = auto)")
-    ap.add_argument("--serving-jobs", type=int, default=128, help="jobs in the serving stream (512 = full)")
+    ap.add_argument("--serving-jobs", type=int, default=512, help="jobs in the serving stream")
     ap.add_argument("--profile-case", default=None,
                     help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
                          "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points), "
                          "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points), tcrs_fhd_full (all 100,000)")
-    ap.add_argument("--serving-max-points", type=int, default=100_000,
-                    help="largest point count of a serving job (500000 = full)")
+    ap.add_argument("--serving-max-points", type=int, default=500_000,
+                    help="largest point count of a serving job")
     return ap.parse_args()
 
 
@@ -227,6 +227,34 @@ def reference_arm(args, w):
 
 # ------------------------------------------------------------------ serving
 
+def single_server_p99(iso: np.ndarray, arrivals: np.ndarray, key) -> float:
+    """p99 latency (s) of an ideal preemptive single server that runs one job
+    at a time at its isolated speed, highest priority first (key(j, arrival)
+    -> sort key, smaller first). A queueing bound for the serving stream:
+    whatever the GPU overlaps beyond this is gained by running jobs side by
+    side."""
+    n = len(iso)
+    rem = iso.astype(np.float64).copy()
+    done = np.zeros(n)
+    active = []
+    t, i = 0.0, 0
+    while i < n or active:
+        if not active:
+            t = max(t, arrivals[i])
+        while i < n and arrivals[i] <= t + 1e-12:
+            active.append(i)
+            i += 1
+        j = min(active, key=lambda q: key(q, arrivals[q]))
+        nxt = arrivals[i] if i < n else np.inf
+        dt = min(rem[j], nxt - t)
+        rem[j] -= dt
+        t += dt
+        if rem[j] <= 1e-12:
+            done[j] = t
+            active.remove(j)
+    return float(np.percentile(done - arrivals, 99))
+
+
 def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int = 4):
     """Mixed hologram jobs with Poisson arrivals through the serving engine.
 
@@ -277,7 +305,13 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
         lat = np.array([r.t_done - r.t_submit for r in res])
         span = max(r.t_done for r in res) - min(r.t_submit for r in res)
         slow = lat / iso
+        arr_rel = arrivals - arrivals[0]
+        p99_iso = float(np.percentile(iso, 99))
+        model = {"fcfs_p99_over_isolated_p99": single_server_p99(iso, arr_rel, lambda q, a: a) / p99_iso,
+                 "edf_p99_over_isolated_p99": single_server_p99(iso, arr_rel, lambda q, a: a + 2 * iso[q] + 0.02)
+                 / p99_iso}
         return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "single_server_model": model,
                 "p99_over_isolated_p99": float(np.percentile(lat, 99) / np.percentile(iso, 99)),
                 "slowdown_p50": float(np.percentile(slow, 50)), "slowdown_p99": float(np.percentile(slow, 99)),
                 "throughput_interactions_per_s": float(sum(p[5] for p in prepared) / span),
@@ -341,6 +375,168 @@ def plan_leg(ctx, sp, reps: int = 50):
                     fn()
                 ms[key] = (time.perf_counter() - t0) / reps * 1e3
         out[name] = ms
+    return out
+
+
+def facade_e2e(w, mode: int, steps: int) -> dict:
+    """The reference caller's sequence through the ophPointCloud façade's C
+    ABI with host buffers: setPointCloudModel, generateHologram(RS),
+    encoding(PHASE), normalize. Wall clock around the synchronous calls
+    (after 3 untimed repetitions); bytes are those the façade copies."""
+    from openholo_gb300.pointcloud import PointCloud
+    with tempfile.TemporaryDirectory() as d:
+        xml = os.path.join(d, "cfg.xml")
+        with open(xml, "w") as f:
+            f.write(w.config_xml())
+        h = PointCloud()
+        try:
+            if not h.readConfig(xml):
+                raise RuntimeError(f"readConfig: {h.lastError()}")
+            h.SetMode(mode)
+            v = np.ascontiguousarray(w.vertices)
+            gen_s = []
+
+            def step():
+                h.setPointCloudModel(v)
+                secs = h.generateHologram(0)
+                if secs <= 0.0:
+                    raise RuntimeError(f"generateHologram: {h.lastError()}")
+                gen_s.append(secs)
+                h.encoding(0)
+                h.normalize()
+
+            for _ in range(3):
+                step()
+            gen_s.clear()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                step()
+            t = (time.perf_counter() - t0) / steps
+        finally:
+            h.release()
+    npx = w.pnx * w.pny * w.n_channels
+    return {"s_per_step": t, "generate_s": sum(gen_s) / len(gen_s),
+            "h2d": w.n_points * 56 + npx * 16 + npx * 8, "d2h": npx * 16 + npx * 8 + npx}
+
+
+def generate_host_e2e(ctx, w, cfg, mode: int, steps: int) -> dict:
+    """ophpc_generate_host: host vertices in, one host complex_H buffer per
+    channel out (page-locked here), synchronous; wall clock per call."""
+    import torch
+    hv = torch.from_numpy(np.ascontiguousarray(w.vertices)).pin_memory()
+    hf = [torch.empty((w.pny, w.pnx, 2), dtype=torch.float64).pin_memory() for _ in range(w.n_channels)]
+    ptrs = [t.data_ptr() for t in hf]
+    for _ in range(3):
+        ctx.generate_host(cfg, hv.data_ptr(), w.n_points, 0, mode, ptrs)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ctx.generate_host(cfg, hv.data_ptr(), w.n_points, 0, mode, ptrs)
+    t = (time.perf_counter() - t0) / steps
+    return {"value": w.interactions / t, "unit": UNIT, "ms_per_call": t * 1e3,
+            "h2d_bytes_per_step": w.n_points * 56, "d2h_bytes_per_step": w.pnx * w.pny * w.n_channels * 16,
+            "call": "ophpc_generate_host (RS, tensor cores): host Vertex[] in, host complex_H per channel out"}
+
+
+def relL2_at_pixels(ctx, w, diff: int, mode: int, n_pix: int = 256, seed: int = 17):
+    """relL2 of one generate against the FP64 oracle at seeded pixels of
+    every channel, all points (accuracy leg; outside any timed region)."""
+    import torch
+
+    import openholo_gb300 as oph
+    import oracle
+    cfg = oph.make_config(**w.geometry_kwargs())
+    npx = w.pnx * w.pny
+    dv = torch.from_numpy(w.vertices).cuda()
+    f = torch.empty((w.n_channels, npx, 2), dtype=torch.float64, device="cuda")
+    ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    pix = np.sort(np.random.default_rng(seed).choice(npx, n_pix, replace=False))
+    g = f[:, torch.from_numpy(pix).cuda()].cpu().numpy()
+    got = g[..., 0] + 1j * g[..., 1]
+    gw = oracle.Geometry(pnx=w.pnx, pny=w.pny, ppx=w.pp, ppy=w.pp, wavelengths=list(w.wavelengths),
+                         scale=w.scale, distance=w.distance)
+    want = np.stack([oracle.field_at(gw, w.vertices, diff, c, pix) for c in range(w.n_channels)])
+    del dv, f
+    return float(np.linalg.norm(got - want) / np.linalg.norm(want))
+
+
+def extra_workload_leg(ctx, w, variants, steps: int) -> dict:
+    """Device-timed generate calls of one more benchmark workload (L2 is
+    flushed by the inputs: every field here is larger than the 129 MB L2,
+    except rs_1k's, whose steps flush it with a 256 MB write), each with its
+    relL2 against the FP64 oracle at 256 seeded pixels per channel."""
+    import torch
+
+    import openholo_gb300 as oph
+    cfg = oph.make_config(**w.geometry_kwargs())
+    s = torch.cuda.current_stream()
+    dv = torch.from_numpy(w.vertices).cuda()
+    f = torch.empty((w.n_channels, w.pny, w.pnx, 2), dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    out = {"pnx": w.pnx, "pny": w.pny, "channels": w.n_channels, "n_points": w.n_points,
+           "interactions_per_call": w.interactions}
+    for name, diff, mode in variants:
+        ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), s.cuda_stream)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), s.cuda_stream)
+            b.record(s)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        t = sum(ts) / len(ts)
+        out[name] = {"value": w.interactions / t, "unit": UNIT, "ms_per_generate": t * 1e3}
+    del dv, f, flush
+    torch.cuda.empty_cache()
+    if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
+        for name, diff, mode in variants:
+            out[name]["relL2_vs_fp64"] = relL2_at_pixels(ctx, w, diff, mode)
+        out["relL2_samples"] = f"all {w.n_points} points at 256 seeded pixels per channel (FP64 oracle)"
+    return out
+
+
+def full_field_codes(ctx, w, mode: int) -> dict:
+    """8-bit codes of the headline step (generate + encode + normalise over
+    all channels) against the codes of the reference's own FP64 GPU kernel's
+    field over every pixel (accuracy leg, outside any timed region; the
+    reference kernel takes ~3 minutes at sphere_fhd)."""
+    import torch
+
+    import oracle
+    from oracle import ref_gpu
+    if not ref_gpu.available():
+        return {"unavailable": "reference GPU kernels not built"}
+    import openholo_gb300 as oph
+    k = ref_gpu.RefGpuKernels()
+    try:
+        ref = k.generate(w.geometry_kwargs(), w.vertices, 0, chunk_points=5000)
+    finally:
+        k.close()
+    cfg = oph.make_config(**w.geometry_kwargs())
+    npx = w.pnx * w.pny
+    dv = torch.from_numpy(w.vertices).cuda()
+    f = torch.empty((w.n_channels, npx, 2), dtype=torch.float64, device="cuda")
+    codes = torch.empty((w.n_channels, npx), dtype=torch.uint8, device="cuda")
+    sp = torch.cuda.current_stream().cuda_stream
+    ctx.generate(cfg, dv.data_ptr(), w.n_points, 0, mode, f.data_ptr(), sp)
+    torch.cuda.synchronize()
+    h = f.cpu().numpy()
+    got_field = (h[..., 0] + 1j * h[..., 1]).reshape(ref.shape)
+    out = {"checker": "reference FP64 GPU kernel (ophgen/src/ophPCKernel.cu, compiled for sm_103a), every pixel",
+           "field_relL2": float(np.linalg.norm(got_field - ref) / np.linalg.norm(ref))}
+    for flag, name in ((0, "phase"), (1, "amplitude")):
+        ctx.encode(f.data_ptr(), w.n_channels, npx, flag, None, codes.data_ptr(), sp)
+        torch.cuda.synchronize()
+        got = codes.cpu().numpy().astype(np.int32)
+        want, _, _ = oracle.normalize(oracle.encode(ref, flag))
+        dlt = got - want.reshape(got.shape).astype(np.int32)
+        if flag == 0:
+            dlt = (dlt + 128) % 256 - 128
+        out[name] = {"codes_exact_frac": float(np.mean(dlt == 0)), "codes_max_lsb": int(np.abs(dlt).max())}
+    del dv, f, codes
     return out
 
 
@@ -456,40 +652,43 @@ def gpu_arm(args, w):
         f4 = torch.empty((1, w4.pny, w4.pnx, 2), dtype=torch.float64, device="cuda")
         tensor["box_4k"] = tensor_leg(w4, dv4, cfg4, f4, 2)
         del dv4, f4
+        if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
+            for name, mode in (("fp16", oph.MODE_TENSOR_FP16), ("bf16x3", oph.MODE_TENSOR_BF16X3)):
+                tensor["box_4k"][name]["relL2_vs_fp64"] = relL2_at_pixels(ctx, w4, 1, mode)
+            tensor["box_4k"]["relL2_vs_fp64_samples"] = "all 1,000,000 points at 256 seeded pixels (FP64 oracle)"
+
+    # the other benchmark workloads: rs_1k (1024x1024, 5,000 points) and
+    # box_8k (7680x4320, 2,000,000 points; tensor-core RS only: the FP32-core
+    # kernel would take ~30 s a call)
+    from openholo_gb300 import workloads as W
+    more = {}
+    if os.environ.get("OPHPC_BENCH_SKIP_MORE") != "1":
+        more["rs_1k"] = extra_workload_leg(ctx, W.rs_1k(), [("rs_plain", 0, 0), ("rs_tc_bf16x3", 0, rs_mode),
+                                                             ("fresnel_plain", 1, 0),
+                                                             ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3)],
+                                           max(3, args.steps // 2))
+        more["box_8k"] = extra_workload_leg(ctx, W.box_8k(), [("rs_tc_bf16x3", 0, rs_mode)], 2)
+    codes_full = None
+    if os.environ.get("OPHPC_BENCH_SKIP_FULLCODES") != "1" and rank == 0:
+        codes_full = full_field_codes(ctx, w, rs_mode)
 
     serving = None
     if os.environ.get("OPHPC_BENCH_SKIP_SERVING") != "1" and world == 1:
         serving = serving_leg(args.serving_jobs, args.serving_max_points)
     plan_replay = plan_leg(ctx, sp)
 
-    # --- end to end through the host-facing ABI ------------------------------
-    hv = torch.from_numpy(w.vertices).pin_memory()
-    hfield = torch.empty((nch, pny, pnx, 2), dtype=torch.float64).pin_memory()
-    hcodes = torch.empty((nch, npx), dtype=torch.uint8).pin_memory()
-    dv2 = torch.empty_like(dv)
-
-    # the field download runs on a second stream once the generate is done,
-    # overlapping the encode
-    side = torch.cuda.Stream()
-
-    def e2e_step():
-        dv2.copy_(hv, non_blocking=True)
-        ctx.generate(cfg, dv2.data_ptr(), w.n_points, oph.DIFF_RS, rs_mode, field.data_ptr(), sp)
-        side.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(side):
-            hfield.copy_(field, non_blocking=True)
-        ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
-        hcodes.copy_(codes, non_blocking=True)
-        torch.cuda.current_stream().wait_stream(side)
-
-    e2e_step()
-    torch.cuda.synchronize()
-    e2e_times = timed(e2e_step, max(3, args.steps // 2))
-    t_e2e = sum(e2e_times) / len(e2e_times)
-    t_e2e = max_over_ranks(t_e2e, dist, "cuda")
-    e2e_value = job_value(inter, world, t_e2e)
-    h2d = hv.numel() * 8
-    d2h = hfield.numel() * 8 + hcodes.numel()
+    # --- end to end through the reference-facing API, host buffers ---------
+    # What a reference caller runs (Example/examPointCloud/examPointCloud.cpp:
+    # setPointCloudModel, generateHologram, encoding, normalize): the
+    # ophPointCloud façade's C ABI, every buffer on the host. Each step copies
+    # the vertices into the object and uploads them, downloads complex_H,
+    # uploads it again for encoding (the caller may have edited it), downloads
+    # m_lpEncoded, uploads it for normalize and downloads m_lpNormalized.
+    e2e = facade_e2e(w, rs_mode | oph.MODE_GPU, max(3, args.steps // 2))
+    e2e_value = job_value(inter, world, max_over_ranks(e2e["s_per_step"], dist, "cuda"))
+    # ophpc_generate_host alone (host vertices in, host complex_H out): the
+    # genCghPointCloudGPU equivalent, without encoding
+    gh = generate_host_e2e(ctx, w, cfg, rs_mode, max(3, args.steps // 2))
 
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 1995.0
@@ -572,7 +771,9 @@ def gpu_arm(args, w):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "vs_baseline": None,
+            "dtype": "bf16x3+fp16 (tcgen05 split-BF16 hi*hi+hi*lo+lo*hi and an FP16 cross pair, FP32 "
+                     "accumulation; FP64 phase reduction and FP64 field)", "data": "synthetic",
             "config": {"workload": w.name, "pnx": pnx, "pny": pny, "pixel_pitch_m": w.pp,
                        "wavelengths_m": list(w.wavelengths), "n_points": w.n_points, "diff": "RS",
                        "step": "generateHologram(RS, 3 channels; tensor-core RS, split-BF16) + phase encode + "
@@ -601,10 +802,20 @@ def gpu_arm(args, w):
             "fresnel": {"value": job_value(inter, world, t_fr), "unit": UNIT, "ms_per_generate": t_fr * 1e3,
                         "kernel": "fresnel_kernel (FP32 cores, separable)"},
             "tensor_fresnel": tensor,
+            "rs_1k": more.get("rs_1k"),
+            "box_8k": more.get("box_8k"),
+            "codes_vs_reference": codes_full,
+            "codes_exact_frac": (codes_full or {}).get("phase", {}).get("codes_exact_frac"),
+            "codes_max_lsb": (codes_full or {}).get("phase", {}).get("codes_max_lsb"),
             "serving": serving,
             "plan_replay": plan_replay,
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": t_e2e * 1e3},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": e2e["h2d"],
+                    "d2h_bytes_per_step": e2e["d2h"], "ms_per_step": e2e["s_per_step"] * 1e3,
+                    "call": "ophPointCloud facade C ABI (ophpc_pc_set_point_cloud, ophpc_pc_generate_hologram, "
+                            "ophpc_pc_encoding(PHASE), ophpc_pc_normalize): host Vertex[] in, host complex_H, "
+                            "m_lpEncoded and m_lpNormalized out; wall clock around the synchronous calls",
+                    "generate_s_reported": e2e["generate_s"]},
+            "e2e_generate_host": gh,
             "gpu_launches": int(launches),
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"],
                        "reasons": clocks["reasons"], "samples": clocks["samples"]},

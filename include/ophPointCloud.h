@@ -193,6 +193,7 @@ private:
     void* d_codes_ = nullptr;
     size_t cap_v_ = 0, cap_f_ = 0, cap_e_ = 0, cap_c_ = 0;
     bool encoded_valid_ = false;
+    bool host_pinned_ = false;  /* per-channel buffers are page-locked (cudaHostAlloc) */
 };
 
 #endif /* OPHPC_OPHPOINTCLOUD_H */

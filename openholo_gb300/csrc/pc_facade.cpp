@@ -18,13 +18,41 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
+
+static_assert(sizeof(Complex<Real>) == 2 * sizeof(Real) && std::is_trivially_copyable<Complex<Real>>::value,
+              "complex_H elements are plain {re, im} pairs");
 
 #define OPH_LOG(...) std::printf(__VA_ARGS__)
 
 namespace {
 constexpr double kPi = 3.14159265358979323846;
+
+// The per-channel host buffers are page-locked when the CUDA runtime can
+// provide it, so that the uploads and downloads around every call run at
+// the link's speed; without a device (readConfig works without one) they are
+// ordinary heap memory. Either way they start zeroed.
+void* host_alloc(size_t bytes, bool pinned) {
+    void* p = nullptr;
+    if (pinned) {
+        if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    } else {
+        p = ::operator new(bytes);
+    }
+    std::memset(p, 0, bytes);
+    return p;
 }
+
+void host_free(void* p, bool pinned) {
+    if (!p) return;
+    if (pinned) cudaFreeHost(p);
+    else ::operator delete(p);
+}
+}  // namespace
 
 ophPointCloud::ophPointCloud(void) { context_.wave_length = wave_length_; }
 
@@ -48,9 +76,9 @@ void ophPointCloud::release(void) { delete this; }
 
 void ophPointCloud::freeBuffers() {
     for (uint c = 0; c < n_old_channels_; ++c) {
-        if (complex_H_) delete[] complex_H_[c];
-        if (encoded_) delete[] encoded_[c];
-        if (normalized_) delete[] normalized_[c];
+        if (complex_H_) host_free(complex_H_[c], host_pinned_);
+        if (encoded_) host_free(encoded_[c], host_pinned_);
+        if (normalized_) host_free(normalized_[c], host_pinned_);
     }
     delete[] complex_H_;
     delete[] encoded_;
@@ -67,15 +95,32 @@ bool ophPointCloud::initialize() {
     const uint nch = context_.waveNum;
     const long long n = (long long)context_.pixel_number[_X] * context_.pixel_number[_Y];
     if (nch < 1 || nch > OPHPC_MAX_CHANNELS || n <= 0) return false;
-    complex_H_ = new Complex<Real>*[nch];
-    encoded_ = new Real*[nch];
-    normalized_ = new uchar*[nch];
-    for (uint c = 0; c < nch; ++c) {
-        complex_H_[c] = new Complex<Real>[n];
-        encoded_[c] = new Real[n]();
-        normalized_[c] = new uchar[n]();
-    }
+    complex_H_ = new Complex<Real>*[nch]();
+    encoded_ = new Real*[nch]();
+    normalized_ = new uchar*[nch]();
     n_old_channels_ = nch;
+    // page-locked if every buffer can be, else all on the heap
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        host_pinned_ = attempt == 0;
+        bool ok = true;
+        for (uint c = 0; c < nch && ok; ++c) {
+            // Complex<Real> is a pair of doubles with no state beyond it: a
+            // zeroed buffer holds value-initialised elements
+            complex_H_[c] = static_cast<Complex<Real>*>(host_alloc(sizeof(Complex<Real>) * (size_t)n, host_pinned_));
+            encoded_[c] = static_cast<Real*>(host_alloc(sizeof(Real) * (size_t)n, host_pinned_));
+            normalized_[c] = static_cast<uchar*>(host_alloc((size_t)n, host_pinned_));
+            ok = complex_H_[c] && encoded_[c] && normalized_[c];
+        }
+        if (ok) break;
+        for (uint c = 0; c < nch; ++c) {
+            host_free(complex_H_[c], host_pinned_);
+            host_free(encoded_[c], host_pinned_);
+            host_free(normalized_[c], host_pinned_);
+            complex_H_[c] = nullptr;
+            encoded_[c] = nullptr;
+            normalized_[c] = nullptr;
+        }
+    }
     buffer_pixels_ = n;
     return true;
 }

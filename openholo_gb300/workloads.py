@@ -57,6 +57,17 @@ class Workload:
         return dict(pnx=self.pnx, pny=self.pny, ppx=self.pp, ppy=self.pp, wavelengths=list(self.wavelengths),
                     scale=self.scale, distance=self.distance)
 
+    def config_xml(self) -> str:
+        """The workload's geometry as the flat <PointCloud> config file that
+        readConfig parses (ophgen/src/ophGen.cpp:221-358,
+        ophgen/src/ophPointCloud.cpp:83-149)."""
+        keys = [("ScaleX", self.scale[0]), ("ScaleY", self.scale[1]), ("ScaleZ", self.scale[2]),
+                ("Distance", self.distance), ("FieldLength", 0.0), ("SLM_PixelPitchX", self.pp),
+                ("SLM_PixelPitchY", self.pp), ("SLM_PixelNumX", self.pnx), ("SLM_PixelNumY", self.pny),
+                ("SLM_WaveNum", self.n_channels)]
+        keys += [(f"SLM_WaveLength_{i + 1}", float(w)) for i, w in enumerate(self.wavelengths)]
+        return "<PointCloud>\n" + "".join(f"  <{k}>{v!r}</{k}>\n" for k, v in keys) + "</PointCloud>\n"
+
     def subset(self, n: int, name_suffix: str = "") -> "Workload":
         return Workload(self.name + name_suffix, self.pnx, self.pny, self.pp, self.wavelengths,
                         np.ascontiguousarray(self.vertices[:n]), self.distance, self.scale)

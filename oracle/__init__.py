@@ -26,7 +26,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "lib", "libophpc_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libophref.so")
-REFERENCE_TREE = os.environ.get("OPHPC_REFERENCE_TREE", "/root/reference")
+# The reference's source tree: $OPHPC_REFERENCE_TREE, else a directory named
+# "reference" beside this repository's checkout (where it is absent, e.g. on
+# a machine that only runs the tests, the reference build is skipped).
+REFERENCE_TREE = os.environ.get("OPHPC_REFERENCE_TREE") or \
+    os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 _lock = threading.Lock()
 _ora = None

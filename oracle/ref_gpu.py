@@ -114,20 +114,32 @@ class RefGpuKernels:
         self._check(self.cu.cuLaunchKernel(self.fn[(diff_flag, single)], grid, 1, 1, BLOCK, 1, 1, 0,
                                            ctypes.c_void_p(stream), args, None), "cuLaunchKernel")
 
-    def generate(self, geom: dict, vertices: np.ndarray, diff_flag: int, single: bool = False):
+    def generate(self, geom: dict, vertices: np.ndarray, diff_flag: int, single: bool = False,
+                 chunk_points: int = 0):
         """The reference driver's single-GPU loop on one device buffer per
-        channel; returns complex128 [n_channels, pnY, pnX]."""
+        channel; returns complex128 [n_channels, pnY, pnX]. With
+        chunk_points > 0 each channel runs as launches over consecutive
+        ranges of that many points accumulating into the same buffer (what
+        the reference's multi-GPU driver does per device,
+        ophgen/src/ophPointCloud_GPU.cpp:287-410), so that no launch runs
+        for more than a few seconds."""
         import torch
         pnx, pny = geom["pnx"], geom["pny"]
+        n = vertices.shape[0]
+        step = chunk_points if chunk_points > 0 else max(n, 1)
         d_v = torch.from_numpy(np.ascontiguousarray(vertices, dtype=np.float64)).cuda()
         d_dst = torch.zeros((pny * pnx, 2), dtype=torch.float64, device="cuda")
         out = []
+        stream = torch.cuda.current_stream().cuda_stream
         for ch, lam in enumerate(geom["wavelengths"]):
-            cfg = make_config(pnx, pny, geom["ppx"], geom["ppy"], lam, vertices.shape[0], diff_flag,
-                              geom.get("scale", (1.0, 1.0, 1.0)), geom.get("distance", 0.0))
-            d_cfg = torch.frombuffer(bytearray(bytes(cfg)), dtype=torch.uint8).cuda()
-            self.launch(diff_flag, single, ch, d_v.data_ptr(), d_cfg.data_ptr(), d_dst.data_ptr(), pnx * pny,
-                        torch.cuda.current_stream().cuda_stream)
+            for p0 in range(0, n, step):
+                m = min(step, n - p0)
+                cfg = make_config(pnx, pny, geom["ppx"], geom["ppy"], lam, m, diff_flag,
+                                  geom.get("scale", (1.0, 1.0, 1.0)), geom.get("distance", 0.0))
+                d_cfg = torch.frombuffer(bytearray(bytes(cfg)), dtype=torch.uint8).cuda()
+                self.launch(diff_flag, single, ch, d_v.data_ptr() + p0 * 56, d_cfg.data_ptr(), d_dst.data_ptr(),
+                            pnx * pny, stream)
+                torch.cuda.synchronize()
             h = d_dst.cpu().numpy()
             out.append((h[:, 0] + 1j * h[:, 1]).reshape(pny, pnx))
             d_dst.zero_()
