@@ -62,7 +62,9 @@ def parse():
     ap.add_argument("--profile-case", default=None,
                     help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
                          "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points), "
-                         "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points), tcrs_fhd_full (all 100,000)")
+                         "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points), tcrs_fhd_full (all 100,000), "
+                         "tcf_fhd_full (tensor-core Fresnel, sphere_fhd), tcf_4k (tensor-core Fresnel, box_4k "
+                         "geometry, 131,072 points)")
     ap.add_argument("--serving-max-points", type=int, default=500_000,
                     help="largest point count of a serving job")
     return ap.parse_args()
@@ -498,6 +500,81 @@ def extra_workload_leg(ctx, w, variants, steps: int) -> dict:
     return out
 
 
+def wrp_leg(ctx, steps: int) -> dict:
+    """WRP generator (ophWRP::generateHologram): the reference's own example
+    (Example/dataset/Dice/WRP/Dice_WRP.xml geometry: 1920x1080, 4.3 um, 532
+    nm, scale 0.0015/0.0015/0.0003, WRP at 300 um, propagation 0.1 m, the
+    Dice point cloud's shape as seeded points: 7,493 points on a cube's
+    faces) and the sphere_fhd point cloud (100,000 points, three colours)
+    with its WRP 1 mm in front of the sphere and 0.5 m of propagation.
+    Device-timed per hologram (L2 flushed), relL2 against the FP64 oracle
+    (splat restated, propagation by numpy FFT)."""
+    import torch
+
+    import openholo_gb300 as oph
+    import oracle
+    from openholo_gb300 import workloads as W
+    s = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    rng = np.random.default_rng(7)
+    n = 7493
+    face = rng.integers(0, 6, n)
+    uv = rng.uniform(-1, 1, (n, 2))
+    cube = np.zeros((n, 3))
+    for f in range(6):
+        m = face == f
+        ax, sg = f // 2, 1.0 if f % 2 else -1.0
+        others = [a for a in range(3) if a != ax]
+        cube[m, ax] = sg * 0.37
+        cube[m, others[0]] = 0.37 * uv[m, 0]
+        cube[m, others[1]] = 0.37 * uv[m, 1]
+    dice = np.zeros((n, 7))
+    dice[:, 0:3] = cube * np.array([1.0, 1.45, 1.2])
+    dice[:, 3:6] = 1.0 - rng.uniform(0.0, 1.0, (n, 3))
+    sph = W.sphere_fhd()
+    cases = {
+        "dice_example": (dict(pnx=1920, pny=1080, ppx=4.3e-6, ppy=4.3e-6, wavelengths=[532e-9],
+                              scale=(0.0015, 0.0015, 0.0003), wrp_location=300e-6, distance=0.1), dice),
+        "sphere_fhd": (dict(pnx=1920, pny=1080, ppx=8e-6, ppy=8e-6, wavelengths=list(sph.wavelengths),
+                            scale=(1.0, 1.0, 1.0), wrp_location=float(sph.vertices[:, 2].max()) + 1e-3,
+                            distance=0.5), sph.vertices),
+    }
+    out = {}
+    for name, (kw, v) in cases.items():
+        cfg = oph.make_wrp_config(**kw)
+        dv = torch.from_numpy(np.ascontiguousarray(v)).cuda()
+        f = torch.empty((cfg.n_channels, kw["pny"], kw["pnx"], 2), dtype=torch.float64, device="cuda")
+        run = lambda: ctx.wrp_generate(cfg, dv.data_ptr(), v.shape[0], f.data_ptr(), s.cuda_stream)  # noqa: E731
+        run()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            run()
+            b.record(s)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        t = sum(ts) / len(ts)
+        g = oracle.WrpGeometry(**kw)
+        zmax = oracle.wrp_zmax(g, v)
+        wsq = [int(abs(lam * (kw["wrp_location"] - zmax) / (kw["ppx"] ** 2 * 2)) * 2) for lam in kw["wavelengths"]]
+        res = {"pnx": kw["pnx"], "pny": kw["pny"], "channels": cfg.n_channels, "n_points": int(v.shape[0]),
+               "splat_half_width_px": wsq, "ms_per_hologram": t * 1e3, "holograms_per_s": 1.0 / t,
+               "note": "synchronises once per call to read the depth range"}
+        if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
+            t0 = time.perf_counter()
+            want = oracle.wrp_generate(g, v)
+            res["oracle_cpu_s"] = time.perf_counter() - t0
+            h = f.cpu().numpy()
+            got = h[..., 0] + 1j * h[..., 1]
+            res["relL2_vs_fp64"] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+        out[name] = res
+        del dv, f
+    return out
+
+
 def full_field_codes(ctx, w, mode: int) -> dict:
     """8-bit codes of the headline step (generate + encode + normalise over
     all channels) against the codes of the reference's own FP64 GPU kernel's
@@ -668,6 +745,9 @@ def gpu_arm(args, w):
                                                              ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3)],
                                            max(3, args.steps // 2))
         more["box_8k"] = extra_workload_leg(ctx, W.box_8k(), [("rs_tc_bf16x3", 0, rs_mode)], 2)
+    wrp = None
+    if os.environ.get("OPHPC_BENCH_SKIP_MORE") != "1" and rank == 0:
+        wrp = wrp_leg(ctx, max(3, args.steps // 2))
     codes_full = None
     if os.environ.get("OPHPC_BENCH_SKIP_FULLCODES") != "1" and rank == 0:
         codes_full = full_field_codes(ctx, w, rs_mode)
@@ -804,6 +884,7 @@ def gpu_arm(args, w):
             "tensor_fresnel": tensor,
             "rs_1k": more.get("rs_1k"),
             "box_8k": more.get("box_8k"),
+            "wrp": wrp,
             "codes_vs_reference": codes_full,
             "codes_exact_frac": (codes_full or {}).get("phase", {}).get("codes_exact_frac"),
             "codes_max_lsb": (codes_full or {}).get("phase", {}).get("codes_max_lsb"),
@@ -842,8 +923,8 @@ def measured_peaks() -> dict:
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one tc_rs_kernel launch of
 # the workload's tensor-core RS generate, from a 1-pass ncu capture of
-# `bench.py --profile-case tcrs_fhd_full` (profiles/tc_rs_kernel_sphere_fhd.md).
-TCRS_TRAFFIC_BYTES = {"sphere_fhd": 21441280 + 255688192}
+# `bench.py --profile-case tcrs_fhd_full` (profiles/tc_tile_kernels_sphere_fhd_dram.md).
+TCRS_TRAFFIC_BYTES = {"sphere_fhd": 21014784 + 83691008}
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one rs_kernel launch of the
@@ -871,6 +952,10 @@ def profile_case(name: str) -> None:
         w, diff, mode = workloads.sphere_fhd().subset(20_000), 0, oph.MODE_TENSOR_BF16X3
     elif name == "tcrs_fhd_full":   # the headline step's tensor-core RS generate (~110 MB on the device)
         w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
+    elif name == "tcf_fhd_full":    # tensor-core Fresnel (on-chip factors), sphere_fhd, all points
+        w, diff, mode = workloads.sphere_fhd(), 1, oph.MODE_TENSOR_BF16X3
+    elif name == "tcf_4k":          # tensor-core Fresnel (on-chip factors), box_4k geometry, 131,072 points
+        w, diff, mode = workloads.box_4k(n_points=131_072), 1, oph.MODE_TENSOR_BF16X3
     else:
         raise SystemExit(f"unknown profile case {name}")
     ctx = oph.Context(0)

@@ -16,11 +16,11 @@ from ._abi import (  # noqa: F401
     DIFF_FRESNEL, DIFF_RS, ENCODE_AMPLITUDE, ENCODE_BURCKHARDT, ENCODE_IMAGINARY, ENCODE_PHASE, ENCODE_REAL,
     ENCODE_SIMPLENI, ENCODE_TWOPHASE, MODE_CPU,
     MODE_DOUBLE, MODE_FASTMATH, MODE_FLOAT, MODE_GPU, MODE_TENSOR_BF16X3, MODE_TENSOR_FP16, OphpcConfig,
-    OphpcError, STATUS, lib, lib_path, make_config,
+    OphpcError, OphpcWrpConfig, STATUS, lib, lib_path, make_config, make_wrp_config,
 )
 
 __all__ = [
-    "Context", "OphpcConfig", "OphpcError", "make_config", "lib", "lib_path",
+    "Context", "OphpcConfig", "OphpcError", "make_config", "lib", "lib_path", "OphpcWrpConfig", "make_wrp_config",
     "DIFF_RS", "DIFF_FRESNEL", "MODE_CPU", "MODE_GPU", "MODE_DOUBLE", "MODE_FLOAT", "MODE_FASTMATH",
     "MODE_TENSOR_FP16", "MODE_TENSOR_BF16X3", "ENCODE_PHASE", "ENCODE_AMPLITUDE", "ENCODE_REAL",
     "ENCODE_IMAGINARY", "ENCODE_SIMPLENI", "ENCODE_BURCKHARDT", "ENCODE_TWOPHASE", "Plan", "PLAN_NO_ENCODE",
@@ -81,6 +81,35 @@ class Context:
                                            ctypes.c_uint64(n_points), diff_flag, mode, arr, ctypes.byref(secs))
         self._check(st, "ophpc_generate_host")
         return secs.value
+
+    # WRP generator (include/ophpc_wrp.h)
+    def wrp_generate(self, cfg: OphpcWrpConfig, d_vertices: int, n_points: int, d_field: int,
+                     stream: int = 0) -> None:
+        st = self._lib.ophpc_wrp_generate(self._h, ctypes.byref(cfg), ctypes.c_void_p(d_vertices),
+                                          ctypes.c_uint64(n_points), ctypes.c_void_p(d_field), ctypes.c_void_p(stream))
+        self._check(st, "ophpc_wrp_generate")
+
+    def wrp_plane(self, cfg: OphpcWrpConfig, d_vertices: int, n_points: int, channel: int, d_plane: int,
+                  stream: int = 0) -> None:
+        st = self._lib.ophpc_wrp_plane(self._h, ctypes.byref(cfg), ctypes.c_void_p(d_vertices),
+                                       ctypes.c_uint64(n_points), channel, ctypes.c_void_p(d_plane),
+                                       ctypes.c_void_p(stream))
+        self._check(st, "ophpc_wrp_plane")
+
+    def wrp_generate_host(self, cfg: OphpcWrpConfig, h_vertices: int, n_points: int,
+                          h_fields: Sequence[int]) -> float:
+        arr = (ctypes.c_void_p * len(h_fields))(*h_fields)
+        secs = ctypes.c_double()
+        st = self._lib.ophpc_wrp_generate_host(self._h, ctypes.byref(cfg), ctypes.c_void_p(h_vertices),
+                                               ctypes.c_uint64(n_points), arr, ctypes.byref(secs))
+        self._check(st, "ophpc_wrp_generate_host")
+        return secs.value
+
+    def fresnel_fft(self, pnx: int, pny: int, ppx: float, ppy: float, wavelength: float, distance: float,
+                    d_src: int, d_dst: int, stream: int = 0) -> None:
+        st = self._lib.ophpc_fresnel_fft(self._h, pnx, pny, ppx, ppy, wavelength, distance, ctypes.c_void_p(d_src),
+                                         ctypes.c_void_p(d_dst), ctypes.c_void_p(stream))
+        self._check(st, "ophpc_fresnel_fft")
 
     def encode(self, d_field: int, n_channels: int, n_pixels: int, encode_flag: int,
                d_encoded: Optional[int], d_normalized: Optional[int], stream: int = 0) -> None:

@@ -71,6 +71,37 @@ def make_config(pnx: int, pny: int, ppx: float, ppy: float, wavelengths: Sequenc
     return c
 
 
+class OphpcWrpConfig(ctypes.Structure):
+    """struct ophpc_wrp_config (include/ophpc_wrp.h)."""
+    _fields_ = [
+        ("pixel_number", ctypes.c_int32 * 2),
+        ("pixel_pitch", ctypes.c_double * 2),
+        ("scale", ctypes.c_double * 3),
+        ("wrp_location", ctypes.c_double),
+        ("propagation_distance", ctypes.c_double),
+        ("n_channels", ctypes.c_uint32),
+        ("wave_length", ctypes.c_double * 3),
+        ("random_phase", ctypes.c_int32),
+    ]
+
+
+def make_wrp_config(pnx: int, pny: int, ppx: float, ppy: float, wavelengths: Sequence[float],
+                    scale=(1.0, 1.0, 1.0), wrp_location: float = 0.0, distance: float = 0.0,
+                    random_phase: bool = False) -> OphpcWrpConfig:
+    c = OphpcWrpConfig()
+    c.pixel_number[0], c.pixel_number[1] = int(pnx), int(pny)
+    c.pixel_pitch[0], c.pixel_pitch[1] = float(ppx), float(ppy)
+    for i in range(3):
+        c.scale[i] = float(scale[i])
+    c.wrp_location = float(wrp_location)
+    c.propagation_distance = float(distance)
+    c.n_channels = len(wavelengths)
+    for i, w in enumerate(wavelengths):
+        c.wave_length[i] = float(w)
+    c.random_phase = 1 if random_phase else 0
+    return c
+
+
 _lock = threading.Lock()
 _lib = None
 
@@ -106,6 +137,16 @@ def _declare(L: ctypes.CDLL) -> None:
         getattr(L, fn).restype = ctypes.c_int
     L.ophpc_plan_destroy.argtypes = [vp]
     L.ophpc_plan_destroy.restype = ctypes.c_int
+    W = ctypes.POINTER(OphpcWrpConfig)
+    L.ophpc_wrp_generate.argtypes = [vp, W, vp, u64, vp, vp]
+    L.ophpc_wrp_generate.restype = ctypes.c_int
+    L.ophpc_wrp_plane.argtypes = [vp, W, vp, u64, u32, vp, vp]
+    L.ophpc_wrp_plane.restype = ctypes.c_int
+    L.ophpc_wrp_generate_host.argtypes = [vp, W, vp, u64, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_double)]
+    L.ophpc_wrp_generate_host.restype = ctypes.c_int
+    d = ctypes.c_double
+    L.ophpc_fresnel_fft.argtypes = [vp, i32, i32, d, d, d, d, vp, vp, vp]
+    L.ophpc_fresnel_fft.restype = ctypes.c_int
 
 
 def lib() -> ctypes.CDLL:

@@ -12,6 +12,7 @@
 #include "pc_common.cuh"
 #include "pc_tc.cuh"
 #include "pc_tcrs.cuh"
+#include "ophpc_wrp.h"
 
 #include <atomic>
 #include <chrono>
@@ -29,6 +30,16 @@ namespace ophpc {
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 uint64_t launches_so_far() { return g_launches.load(std::memory_order_relaxed); }
+}  // namespace ophpc
+
+namespace ophpc {
+bool wrp_sizes_supported(int pnx, int pny);
+ophpc_status wrp_generate_device(cudaMemPool_t pool, const ophpc_wrp_config* cfg, const ophpc_vertex* d_vertices,
+                                 uint64_t n_points, double* d_out, int plane_channel, cudaStream_t s,
+                                 std::string* err);
+ophpc_status fresnel_fft_device(cudaMemPool_t pool, int pnx, int pny, double ppx, double ppy, double lambda,
+                                double distance, const double2* src, double2* dst, cudaStream_t s,
+                                std::string* err);
 }  // namespace ophpc
 
 struct ophpc_context {
@@ -97,6 +108,34 @@ ophpc_status check_config(ophpc_context* ctx, const ophpc_config* cfg) {
         return fail(ctx, OPHPC_ERROR_CONFIG, "field_length must be finite");
     if (std::abs(cfg->offset[0]) > (1 << 24) || std::abs(cfg->offset[1]) > (1 << 24))
         return fail(ctx, OPHPC_ERROR_CONFIG, "offset out of range");
+    return OPHPC_SUCCESS;
+}
+
+// The WRP generator's configuration (ophgen/src/ophWRP.cpp:137-213 reads
+// it; its splat and propagation need no more than finite values, and the
+// padded transform sizes factor into 2, 3, 5, 7).
+ophpc_status check_wrp_config(ophpc_context* ctx, const ophpc_wrp_config* cfg, bool propagates = true) {
+    if (!cfg) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "config is NULL");
+    if (cfg->pixel_number[0] <= 0 || cfg->pixel_number[1] <= 0)
+        return fail(ctx, OPHPC_ERROR_CONFIG, "pixel_number must be positive");
+    // the padded transform of 2 pnX x 2 pnY: up to 32768 lines each way
+    if (cfg->pixel_number[0] > 16384 || cfg->pixel_number[1] > 16384)
+        return fail(ctx, OPHPC_ERROR_CONFIG, "pixel_number above 16384");
+    if (!finite_pos(cfg->pixel_pitch[0]) || !finite_pos(cfg->pixel_pitch[1]))
+        return fail(ctx, OPHPC_ERROR_CONFIG, "pixel_pitch must be positive and finite");
+    if (cfg->n_channels < 1 || cfg->n_channels > OPHPC_MAX_CHANNELS)
+        return fail(ctx, OPHPC_ERROR_CONFIG, "n_channels must be 1..3 (Vertex carries 3 colours)");
+    for (uint32_t c = 0; c < cfg->n_channels; ++c)
+        if (!finite_pos(cfg->wave_length[c]))
+            return fail(ctx, OPHPC_ERROR_CONFIG, "wave_length must be positive and finite");
+    for (int i = 0; i < 3; ++i)
+        if (!std::isfinite(cfg->scale[i])) return fail(ctx, OPHPC_ERROR_CONFIG, "scale must be finite");
+    if (!std::isfinite(cfg->wrp_location) || !std::isfinite(cfg->propagation_distance))
+        return fail(ctx, OPHPC_ERROR_CONFIG, "wrp_location and propagation_distance must be finite");
+    if (cfg->random_phase)
+        return fail(ctx, OPHPC_ERROR_UNSUPPORTED, "random phase is not supported (the reference's is unseeded)");
+    if (propagates && !wrp_sizes_supported(cfg->pixel_number[0], cfg->pixel_number[1]))
+        return fail(ctx, OPHPC_ERROR_UNSUPPORTED, "2*pnX and 2*pnY must factor into 2, 3, 5 and 7");
     return OPHPC_SUCCESS;
 }
 
@@ -197,6 +236,11 @@ ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const 
         return e == cudaSuccess ? OPHPC_SUCCESS : cuda_fail(ctx, e, "cudaMemsetAsync(field)");
     }
     if (tensor && !accumulate) {
+        // split-BF16: factors generated on chip per 128x128 tile; FP16:
+        // factor tables in HBM and a tcgen05 GEMM over them
+        if (mode & OPHPC_MODE_TENSOR_BF16X3)
+            return tc_generate_fresnel_tiles(ctx->pool, jg, cfg, d_vertices, n_points, d_field, ctx->sm_count, s,
+                                             &ctx->last_error, d_err_out);
         return tc_generate_fresnel(ctx->pool, cfg, d_vertices, n_points, mode, d_field, s, &ctx->last_error,
                                    d_err_out);
     }
@@ -452,6 +496,110 @@ ophpc_status ophpc_generate_host(ophpc_context* ctx, const ophpc_config* cfg, co
     if (seconds_out)
         *seconds_out = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return st;
+}
+
+ophpc_status ophpc_wrp_generate(ophpc_context* ctx, const ophpc_wrp_config* cfg, const ophpc_vertex* d_vertices,
+                                uint64_t n_points, double* d_field, void* stream) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    ophpc_status st = check_wrp_config(ctx, cfg);
+    if (st != OPHPC_SUCCESS) return st;
+    if (n_points > (uint64_t)INT32_MAX) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "n_points above 2^31-1");
+    DeviceGuard guard(ctx->device);
+    if (!d_field || !is_device_ptr(d_field))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be device memory");
+    if (n_points > 0 && (!d_vertices || !is_device_ptr(d_vertices)))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_vertices must be device memory");
+    if (!aligned(d_field, 16) || !aligned(d_vertices, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_vertices 8-byte aligned");
+    return wrp_generate_device(ctx->pool, cfg, d_vertices, n_points, d_field, -1, (cudaStream_t)stream,
+                               &ctx->last_error);
+}
+
+ophpc_status ophpc_wrp_plane(ophpc_context* ctx, const ophpc_wrp_config* cfg, const ophpc_vertex* d_vertices,
+                             uint64_t n_points, uint32_t channel, double* d_plane, void* stream) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    ophpc_status st = check_wrp_config(ctx, cfg, false);
+    if (st != OPHPC_SUCCESS) return st;
+    if (channel >= cfg->n_channels) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "channel out of range");
+    if (n_points > (uint64_t)INT32_MAX) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "n_points above 2^31-1");
+    DeviceGuard guard(ctx->device);
+    if (!d_plane || !is_device_ptr(d_plane))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_plane must be device memory");
+    if (n_points > 0 && (!d_vertices || !is_device_ptr(d_vertices)))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_vertices must be device memory");
+    if (!aligned(d_plane, 16) || !aligned(d_vertices, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_plane must be 16-byte and d_vertices 8-byte aligned");
+    return wrp_generate_device(ctx->pool, cfg, d_vertices, n_points, d_plane, (int)channel, (cudaStream_t)stream,
+                               &ctx->last_error);
+}
+
+ophpc_status ophpc_wrp_generate_host(ophpc_context* ctx, const ophpc_wrp_config* cfg,
+                                     const ophpc_vertex* h_vertices, uint64_t n_points,
+                                     double* const* h_field_per_channel, double* seconds_out) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    auto t0 = std::chrono::steady_clock::now();
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    ophpc_status st = check_wrp_config(ctx, cfg);
+    if (st != OPHPC_SUCCESS) return st;
+    if (n_points > (uint64_t)INT32_MAX) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "n_points above 2^31-1");
+    if (!h_field_per_channel) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "field buffers are NULL");
+    for (uint32_t c = 0; c < cfg->n_channels; ++c)
+        if (!h_field_per_channel[c]) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "field buffer is NULL");
+    if (n_points > 0 && !h_vertices) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "vertices are NULL");
+    DeviceGuard guard(ctx->device);
+    cudaStream_t s = ctx->host_stream;
+    const int64_t plane = (int64_t)cfg->pixel_number[0] * cfg->pixel_number[1];
+    ophpc_vertex* d_v = nullptr;
+    double* d_f = nullptr;
+    cudaError_t e = pool_alloc(ctx, &d_v, sizeof(ophpc_vertex) * n_points, s);
+    if (e == cudaSuccess) e = pool_alloc(ctx, &d_f, sizeof(double2) * plane * cfg->n_channels, s);
+    if (e != cudaSuccess) {
+        if (d_v) cudaFreeAsync(d_v, s);
+        cudaStreamSynchronize(s);
+        return cuda_fail(ctx, e, "scratch allocation (WRP host path)");
+    }
+    if (n_points) e = cudaMemcpyAsync(d_v, h_vertices, sizeof(ophpc_vertex) * n_points, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+        st = wrp_generate_device(ctx->pool, cfg, d_v, n_points, d_f, -1, s, &ctx->last_error);
+    else
+        st = cuda_fail(ctx, e, "cudaMemcpyAsync(vertices)");
+    if (st == OPHPC_SUCCESS) {
+        for (uint32_t c = 0; c < cfg->n_channels && e == cudaSuccess; ++c)
+            e = cudaMemcpyAsync(h_field_per_channel[c], d_f + 2 * plane * c, sizeof(double2) * plane,
+                                cudaMemcpyDeviceToHost, s);
+        if (e != cudaSuccess) st = cuda_fail(ctx, e, "cudaMemcpyAsync(field)");
+    }
+    cudaFreeAsync(d_v, s);
+    cudaFreeAsync(d_f, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess && st == OPHPC_SUCCESS) st = cuda_fail(ctx, e, "WRP generate (host path)");
+    if (seconds_out) *seconds_out = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return st;
+}
+
+ophpc_status ophpc_fresnel_fft(ophpc_context* ctx, int32_t pnx, int32_t pny, double ppx, double ppy, double lambda,
+                               double distance, const double* d_src, double* d_dst, void* stream) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    if (pnx <= 0 || pny <= 0 || pnx > 16384 || pny > 16384)
+        return fail(ctx, OPHPC_ERROR_CONFIG, "pixel numbers must be 1..16384");
+    if (!finite_pos(ppx) || !finite_pos(ppy) || !finite_pos(lambda) || !std::isfinite(distance))
+        return fail(ctx, OPHPC_ERROR_CONFIG, "pitch, wavelength and distance must be finite (positive)");
+    if (!wrp_sizes_supported(pnx, pny))
+        return fail(ctx, OPHPC_ERROR_UNSUPPORTED, "2*pnX and 2*pnY must factor into 2, 3, 5 and 7");
+    DeviceGuard guard(ctx->device);
+    if (!d_src || !d_dst || !is_device_ptr(d_src) || !is_device_ptr(d_dst))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_src and d_dst must be device memory");
+    if (!aligned(d_src, 16) || !aligned(d_dst, 16))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_src and d_dst must be 16-byte aligned");
+    return fresnel_fft_device(ctx->pool, pnx, pny, ppx, ppy, lambda, distance, (const double2*)d_src, (double2*)d_dst,
+                              (cudaStream_t)stream, &ctx->last_error);
 }
 
 ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_channels, uint64_t n_pixels,

@@ -50,6 +50,12 @@ __device__ __forceinline__ unsigned long long ordered_bits(double d) {
     return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
 }
 
+__device__ __forceinline__ uint64_t global_ns_enc() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+
 __global__ void __launch_bounds__(256) encode_minmax_kernel(const double2* __restrict__ field, int64_t n,
                                                             int flag, double* __restrict__ encoded,
                                                             unsigned long long* __restrict__ minmax) {
@@ -302,6 +308,8 @@ __global__ void init_est_minmax_kernel(unsigned long long* minmax) {
     unsigned* w = reinterpret_cast<unsigned*>(minmax + 2);
     w[0] = ordered32(__int_as_float(0x7f800000));    // +inf
     w[1] = ordered32(__int_as_float((int)0xff800000u));   // -inf
+    minmax[3] = 0;   // single-pass codes: grid barrier count
+    minmax[4] = 0;   //                    barrier timeout
 }
 
 // block reduction of a min and a max pair of doubles into the exact words
@@ -418,6 +426,116 @@ __global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restric
     }
 }
 
+// Single pass of the codes, for fields whose FP32 estimates fit in the
+// shared memory of the CTAs the GPU holds at once (cooperative launch):
+// every CTA owns `per` consecutive pixels and
+//   1. reads them once, keeps their estimates in shared memory (NaN where
+//      there is none) and reduces its estimated min/max;
+//   2. computes in FP64 the pixels within the band of its own estimated
+//      extremes (the pixel holding the CTA's exact extreme is among them, so
+//      the grid's exact extremes are found) and those without an estimate,
+//      and folds them into the exact words;
+//   3. waits at a grid barrier (all CTAs are resident; the wait is bounded by
+//      %globaltimer and records a timeout in word [4]);
+//   4. writes every code from its cached estimate, in FP64 where the
+//      estimate is within its error margin of a code boundary (as
+//      est_codes_kernel, so the codes are the same bit for bit).
+// The field is read once (plus the few FP64 pixels); words [3] and [4]
+// (barrier count, timeout) are zeroed by init_est_minmax_kernel.
+template <int FLAG>
+__global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restrict__ field, int64_t n, int64_t per,
+                                                          unsigned long long* __restrict__ minmax,
+                                                          uint8_t* __restrict__ out) {
+    extern __shared__ float s_est[];
+    __shared__ float s_red[2][8];
+    const int64_t base = (int64_t)blockIdx.x * per;
+    const int64_t cnt = base < n ? min(per, n - base) : 0;
+    const float qnan = __int_as_float(0x7fc00000);
+    float mn = __int_as_float(0x7f800000), mx = -mn;
+    double emn = kMaxDouble, emx = kMinDouble;
+    for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+        const double2 h = field[base + j];
+        bool ok;
+        const float e = estimate<FLAG>(h, ok);
+        if (ok) {
+            s_est[j] = e;
+            mn = fminf(mn, e);
+            mx = fmaxf(mx, e);
+        } else {
+            s_est[j] = qnan;
+            const double x = encode_value(h, FLAG);
+            if (x < emn) emn = x;
+            if (x > emx) emx = x;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        s_red[0][threadIdx.x >> 5] = mn;
+        s_red[1][threadIdx.x >> 5] = mx;
+    }
+    __syncthreads();
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+        mn = fminf(mn, s_red[0][k]);
+        mx = fmaxf(mx, s_red[1][k]);
+    }
+    const float band = est_band<FLAG>(mx);
+    for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+        const float e = s_est[j];
+        if (e == e && (e <= mn + band || e >= mx - band)) {
+            const double x = encode_value(field[base + j], FLAG);
+            if (x < emn) emn = x;
+            if (x > emx) emx = x;
+        }
+    }
+    fold_exact(emn, emx, minmax);
+    // grid barrier
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(&minmax[3], 1ull);
+        const uint64_t t0 = global_ns_enc();
+        bool ok = true;
+        while (*(volatile unsigned long long*)&minmax[3] < (unsigned long long)gridDim.x) {
+            if (global_ns_enc() - t0 > 2000000000ull) {
+                ok = false;
+                atomicExch(&minmax[4], 1ull);
+                break;
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    const double gmn = from_ordered(__ldcg(&minmax[0]));
+    const double gmx = from_ordered(__ldcg(&minmax[1]));
+    const double gap = __dsub_rn(gmx, gmn);
+    const bool usable = gap > 0.0 && gap < 1e30 && gmn > -1e30 && gmn < 1e30;
+    const float mn_f = (float)gmn, sc_f = usable ? (float)(255.0 / gap) : 0.f;
+    const float err = FLAG == 0 ? kPhaseErr : kAmpErrRel * (float)fmax(fabs(gmx), fabs(gmn));
+    const float margin = 2.f * err * sc_f + 1e-4f;
+    for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
+        const float e = s_est[j];
+        uint8_t code = 0;
+        if (s_ok) {
+            const float v = (e - mn_f) * sc_f + 0.5f;
+            const float fl = floorf(v);
+            if (usable && e == e && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f) {
+                code = (uint8_t)(int)fl;
+            } else {
+                const double x = encode_value(field[base + j], FLAG);
+                const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(x, gmn), gap), 255.0), 0.5);
+                code = (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
+            }
+        }
+        out[base + j] = code;
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -428,6 +546,47 @@ int grid_for(int64_t n, int threads) {
     const int64_t want = (n + threads - 1) / threads;
     return (int)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
 }
+// Cooperative single-pass codes when the grid of resident CTAs can cache
+// every estimate (4 bytes a pixel). False when it cannot (the three-pass
+// kernels run instead).
+bool launch_fused_codes(const double2* d_field, int64_t n, int flag, unsigned long long* d_minmax,
+                        uint8_t* d_codes, cudaStream_t stream) {
+    // not inside a stream capture (a plan): there the three-pass kernels run
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return false;
+    }
+    int dev = 0, sms = 0, coop = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop || sms <= 0) return false;
+    const void* fn = flag == 0 ? (const void*)fused_codes_kernel<0> : (const void*)fused_codes_kernel<1>;
+    for (int bps = 8; bps >= 1; bps >>= 1) {
+        const int64_t grid = (int64_t)sms * bps;
+        const int64_t per = ((n + grid - 1) / grid + 31) / 32 * 32;
+        const size_t smem = (size_t)per * sizeof(float);
+        if (smem > 200 * 1024) continue;
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        int fit = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, 256, smem) != cudaSuccess || fit < bps) continue;
+        count_launches(2);
+        init_est_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
+        void* args[] = {(void*)&d_field, (void*)&n, (void*)&per, (void*)&d_minmax, (void*)&d_codes};
+        const cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3((unsigned)grid), dim3(256), args, smem, stream);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return false;   // the three-pass kernels run instead (init is repeated there)
+        }
+        return true;
+    }
+    return false;
+}
+
 }  // namespace
 
 void launch_normalize(const double* d_encoded, int n_channels, int64_t n_pixels, uint8_t* d_normalized,
@@ -463,7 +622,9 @@ void launch_encode(const double2* d_field, int n_channels, int64_t n_pixels, int
         return;
     }
     if (!d_encoded && d_normalized && (encode_flag == 0 || encode_flag == 1)) {
-        // codes only: FP32 estimates, FP64 where they cannot decide
+        // codes only: FP32 estimates, FP64 where they cannot decide; one
+        // pass when the estimates fit in the resident CTAs' shared memory
+        if (launch_fused_codes(d_field, n, encode_flag, d_minmax, d_normalized, stream)) return;
         count_launches(4);
         init_est_minmax_kernel<<<1, 1, 0, stream>>>(d_minmax);
         if (encode_flag == 0) {

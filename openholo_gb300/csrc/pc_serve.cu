@@ -17,10 +17,12 @@
 //
 // RS jobs submitted with OPHPC_MODE_TENSOR_BF16X3 run their point-range
 // steps on the tensor-core RS kernel (plus its CUDA-core complement for the
-// same range); Fresnel jobs with either tensor mode run one channel's chunk
-// of points per step on the tensor-core Fresnel (factor tables + GEMM into
-// FP64 sums, the channel's field written after its last chunk). Steps are
-// sized by each path's rate.
+// same range); Fresnel jobs with OPHPC_MODE_TENSOR_BF16X3 run point-range
+// steps of the tensor-core Fresnel tile kernel (factors generated on chip,
+// adding into the job's FP64 field); Fresnel jobs with OPHPC_MODE_TENSOR_FP16
+// run one channel's chunk of points per step on the table path (factor
+// tables + GEMM into FP64 sums, the channel's field written after its last
+// chunk). Steps are sized by each path's rate.
 //
 // A job's result does not depend on what else runs: its chunking is fixed
 // by the job alone and every chunk adds into the FP64 field in order.
@@ -74,7 +76,8 @@ struct ServeJob {
     uint8_t* d_codes = nullptr;
     unsigned long long* d_mm = nullptr;
     bool tc = false;            // RS on the tensor cores (OPHPC_MODE_TENSOR_BF16X3)
-    bool tcf = false;           // Fresnel on the tensor cores (either tensor mode)
+    bool tcf = false;           // Fresnel on the tensor cores, factor tables (OPHPC_MODE_TENSOR_FP16)
+    bool tcft = false;          // Fresnel on the tensor cores, on-chip factors (OPHPC_MODE_TENSOR_BF16X3)
     float* d_amax = nullptr;    // tensor cores: per-channel amplitude bound
     int32_t* d_left = nullptr;  // tensor-core RS: per-tile pair counts for the complement
     uint32_t* d_mask = nullptr; // tensor-core RS: per-tile bits of the pairs left to the complement
@@ -130,7 +133,8 @@ struct ophpc_server {
     bool stop = false;
     double rate_rs = 2.0e12, rate_fresnel = 2.6e12;   // interactions/s used to size steps
     double rate_tc_rs = 2.2e13;                        // tensor-core RS
-    double rate_tcf_bf16x3 = 4e13, rate_tcf_fp16 = 9e13;   // tensor-core Fresnel
+    double rate_tcf_fp16 = 9e13;                       // tensor-core Fresnel, tables
+    double rate_tcf_tile = 4.5e13;                     // tensor-core Fresnel, on-chip factors
     int* h_err = nullptr;                              // [slot]: page-locked copies of the jobs' error words
 };
 
@@ -189,8 +193,9 @@ JobGeom make_job_geom(const ophpc_config* cfg, int64_t n) {
 }
 
 bool uses_tc(const ophpc_job* j) { return j->diff_flag == OPHPC_DIFF_RS && (j->mode & OPHPC_MODE_TENSOR_BF16X3); }
-bool uses_tcf(const ophpc_job* j) {
-    return j->diff_flag == OPHPC_DIFF_FRESNEL && (j->mode & (OPHPC_MODE_TENSOR_BF16X3 | OPHPC_MODE_TENSOR_FP16));
+bool uses_tcf(const ophpc_job* j) { return j->diff_flag == OPHPC_DIFF_FRESNEL && (j->mode & OPHPC_MODE_TENSOR_FP16); }
+bool uses_tcft(const ophpc_job* j) {
+    return j->diff_flag == OPHPC_DIFF_FRESNEL && (j->mode & OPHPC_MODE_TENSOR_BF16X3);
 }
 
 // Points per tensor-core Fresnel step: ~step_ms of GPU time for one
@@ -223,7 +228,7 @@ size_t tcf_bytes(const ophpc_job* j, int64_t kc) {
 size_t job_bytes(const ophpc_job* j, int64_t tcf_kc) {
     const size_t px = (size_t)j->cfg.pixel_number[0] * j->cfg.pixel_number[1] * j->cfg.n_channels;
     return align256(sizeof(ophpc_vertex) * j->n_points) + align256(sizeof(PointRec) * j->n_points * j->cfg.n_channels) +
-           align256(sizeof(double2) * px) + align256(px) + 256 + (uses_tc(j) || uses_tcf(j) ? 256 : 0) +
+           align256(sizeof(double2) * px) + align256(px) + 256 + (uses_tc(j) || uses_tcf(j) || uses_tcft(j) ? 256 : 0) +
            (uses_tc(j) ? tc_left_bytes(j) + tc_mask_bytes(j) : 0) + (uses_tcf(j) ? tcf_bytes(j, tcf_kc) : 0);
 }
 
@@ -236,13 +241,14 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
     const int64_t px = (int64_t)d.cfg.pixel_number[0] * d.cfg.pixel_number[1];
     cudaError_t e = cudaSuccess;
     if (j->stage == 0) {
-        if (j->tc || j->tcf) e = cudaMemsetAsync(j->d_amax, 0, 32, st);   // amax[0..3] and the error word
+        if (j->tc || j->tcf || j->tcft) e = cudaMemsetAsync(j->d_amax, 0, 32, st);   // amax[0..3], error word
         if (n > 0) {
             if (e == cudaSuccess)
                 e = cudaMemcpyAsync(j->d_v, d.h_vertices, sizeof(ophpc_vertex) * n, cudaMemcpyHostToDevice, st);
             launch_prep(j->d_v, n, d.cfg.scale, d.cfg.distance, d.cfg.field_length, d.cfg.viewing_window,
                         (int)d.diff_flag, j->jg, j->d_recs, st);
             if (j->tc) launch_rs_amax(j->d_recs, n, (int)d.cfg.n_channels, j->d_amax, st);
+            if (j->tcft) launch_fresnel_amax(j->d_recs, n, (int)d.cfg.n_channels, j->d_amax, st);
             if (j->tcf)
                 for (uint32_t c = 0; c < d.cfg.n_channels; ++c)
                     launch_tc_fresnel_cmax(j->d_recs + (int64_t)c * n, n, j->d_amax + c, st);
@@ -276,6 +282,9 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
             e = launch_tc_rs_range(j->jg, j->d_recs, g.p0, g.p1, g.accumulate != 0,
                                    reinterpret_cast<double2*>(j->d_field), j->d_amax, j->d_left, j->d_mask,
                                    tc_rs_mask_words((int64_t)d.n_points), j->d_err, st);
+        else if (j->tcft)
+            e = launch_tc_fresnel_range(j->jg, j->d_recs, g.p0, g.p1, g.accumulate != 0,
+                                        reinterpret_cast<double2*>(j->d_field), j->d_amax, j->d_err, st);
         else if (d.diff_flag == OPHPC_DIFF_RS)
             launch_rs(j->d_recs, g, reinterpret_cast<double2*>(j->d_field), nullptr, st);
         else
@@ -292,7 +301,7 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
         }
         if (d.h_field && e == cudaSuccess)
             e = cudaMemcpyAsync(d.h_field, j->d_field, sizeof(double2) * px * d.cfg.n_channels, cudaMemcpyDeviceToHost, st);
-        if ((j->tc || j->tcf) && e == cudaSuccess)
+        if ((j->tc || j->tcf || j->tcft) && e == cudaSuccess)
             e = cudaMemcpyAsync(&s->h_err[j->slot], j->d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
         j->stage = 3;
     }
@@ -330,7 +339,7 @@ bool admit(ophpc_server* s, ServeJob* j) {
     j->d_codes = q;
     q += align256(px);
     j->d_mm = (unsigned long long*)q;
-    if (j->tc || j->tcf) {
+    if (j->tc || j->tcf || j->tcft) {
         q += 256;
         j->d_amax = (float*)q;   // [4] floats, then the error word
         j->d_err = (int*)(q + 16);
@@ -397,7 +406,8 @@ void worker_main(ophpc_server* s) {
                 if (q != cudaSuccess) {
                     j->status = OPHPC_ERROR_CUDA;
                     j->stage = 3;
-                } else if (j->tc && j->stage == 3 && s->h_err[j->slot] != 0 && j->status == OPHPC_SUCCESS) {
+                } else if ((j->tc || j->tcf || j->tcft) && j->stage == 3 && s->h_err[j->slot] != 0 &&
+                           j->status == OPHPC_SUCCESS) {
                     j->status = OPHPC_ERROR_TIMEOUT;   // a tensor-core wait gave up
                 }
             }
@@ -507,14 +517,17 @@ ophpc_status ophpc_server_submit(ophpc_server* s, const ophpc_job* job, uint64_t
     j->desc = *job;
     j->tc = uses_tc(job);
     j->tcf = uses_tcf(job);
-    const double tcf_rate = (job->mode & OPHPC_MODE_TENSOR_BF16X3) ? s->rate_tcf_bf16x3 : s->rate_tcf_fp16;
+    j->tcft = uses_tcft(job);
+    const double tcf_rate = s->rate_tcf_fp16;
     const int64_t tcf_kc = j->tcf ? tcf_step_points(job, s->opt.step_ms, tcf_rate) : 0;
     j->bytes = job_bytes(job, tcf_kc);
     if (j->bytes > s->opt.memory_budget) return OPHPC_ERROR_OUT_OF_MEMORY;
     j->jg = make_job_geom(&job->cfg, (int64_t)job->n_points);
     const double px = (double)job->cfg.pixel_number[0] * job->cfg.pixel_number[1] * job->cfg.n_channels;
-    const double rate = j->tc ? s->rate_tc_rs
-                              : j->tcf ? tcf_rate : (job->diff_flag == OPHPC_DIFF_RS ? s->rate_rs : s->rate_fresnel);
+    const double rate = j->tc     ? s->rate_tc_rs
+                        : j->tcft ? s->rate_tcf_tile
+                        : j->tcf  ? tcf_rate
+                                  : (job->diff_flag == OPHPC_DIFF_RS ? s->rate_rs : s->rate_fresnel);
     int64_t cp = (int64_t)(s->opt.step_ms * 1e-3 * rate / px);
     cp = std::max<int64_t>(kChunk, cp / kChunk * kChunk);
     j->chunk_points = j->tcf ? tcf_kc : cp;

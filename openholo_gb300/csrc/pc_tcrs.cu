@@ -71,11 +71,23 @@ constexpr int kRecWarps = 3;                             // warps 9-11: point re
 constexpr int kRecThreads = 32 * kRecWarps;
 constexpr int kThreadsTc = kProducers + 32 + kRecThreads;   // 384: 12 warps, 168 registers each
 constexpr int kStagePts = 16;                            // points per stage: one K=16 MMA step
-constexpr int kStagesTc = 3;
 constexpr int kPlane = kRsTcTile * kStagePts * 2;        // 4096 B: 128 rows x 32 B
-// planes of one stage ([Br; Bi] of each B part contiguous: one N=256 operand)
-enum : int { kAhr = 0, kAhi, kAlr, kAli, kA2r, kA2i, kBhr, kBhi, kBlr, kBli, kB2r, kB2i, kPlanes };
-constexpr int kStageBytesTc = kPlanes * kPlane;          // 61,440
+// Planes of one stage ([Br; Bi] of each B part contiguous: one N=256
+// operand). RS (FR false): split-BF16 hi/lo of A and B plus the FP16 cross
+// pair A2/B2, 12 planes, 3 stages. Fresnel (FR true): no cross pair, 8
+// planes, and the shared memory this frees goes to a fourth stage.
+template <bool FR>
+struct Lay {
+    enum : int {
+        Ahr = 0, Ahi = 1, Alr = 2, Ali = 3,
+        A2r = FR ? -1 : 4, A2i = FR ? -1 : 5,
+        Bhr = FR ? 4 : 6, Bhi = FR ? 5 : 7, Blr = FR ? 6 : 8, Bli = FR ? 7 : 9,
+        B2r = FR ? -1 : 10, B2i = FR ? -1 : 11,
+        Planes = FR ? 8 : 12,
+        Stages = FR ? 4 : 3
+    };
+    static constexpr int kStageBytes = Planes * kPlane;   // RS 49,152; Fresnel 32,768
+};
 constexpr int kChunkTc = kProducers;                     // points per record round (one per producer)
 constexpr int kStagesPerChunk = kChunkTc / kStagePts;    // 16
 constexpr int kPeriod = 64;                              // stages per TMEM accumulation run (1024 points)
@@ -95,8 +107,13 @@ struct __align__(16) TcRsPair {
 };
 static_assert(sizeof(TcRsPair) == 64, "TcRsPair size");
 
-constexpr size_t kSmemTc = 1024 + (size_t)kStagesTc * kStageBytesTc + sizeof(TcRsPair) * kChunkTc + 512;
-static_assert(kSmemTc <= 232448, "shared memory per CTA");
+template <bool FR>
+constexpr size_t smem_tc() {
+    return 1024 + (size_t)Lay<FR>::Stages * Lay<FR>::kStageBytes + sizeof(TcRsPair) * kChunkTc + 512;
+}
+constexpr size_t kSmemTc = smem_tc<false>();
+constexpr size_t kSmemTcFr = smem_tc<true>();
+static_assert(kSmemTc <= 232448 && kSmemTcFr <= 232448, "shared memory per CTA");
 
 struct TcRsArgs {
     JobGeom jg;
@@ -107,14 +124,19 @@ struct TcRsArgs {
     int* error;
     int32_t tiles_x, tiles_y;
     // Points [p_base, p_base + p_count) of the records. The range of every
-    // tile is split into ksplit parts of pps points (blockIdx.z = channel *
-    // ksplit + part) so that the CTA count fills whole waves; part 0 writes
-    // (or, with jg.accumulate, adds into) the field, part k > 0 writes
-    // partials[k - 1] (same layout), summed afterwards.
+    // tile is split into ksplit parts of pps points (blockIdx.x = tile
+    // column * ksplit + part: the parts of a tile are launched side by side
+    // and run at the same time) so that the CTA count fills whole waves;
+    // part 0 writes (or, with jg.accumulate, adds into) the field, part k > 0
+    // writes partials[k - 1] (same layout). The last part of a tile to finish
+    // (tickets[tile], zeroed by the caller) adds the partial tiles into the
+    // field in part order and discards their lines from L2, so that the
+    // partials, read while still in L2, are never written back to DRAM.
     int64_t p_base, p_count;
     int32_t ksplit;
     int64_t pps;            // a multiple of kChunkTc
     double2* partials;
+    int32_t* tickets;       // [n_channels][tiles_y][tiles_x], when ksplit > 1
     // per tile, one bit per point of [p_base, p_base + p_count) for the
     // pairs left to the CUDA cores (word (i - p_base) / 32); mask_words words a tile
     uint32_t* mask;
@@ -213,20 +235,135 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
         const uint32_t ro = h ? ro1 : ro0;
         const int o = 4 * h;
 #define ST(plane, w) st_v4(ro + (plane) * kPlane, w[o], w[o + 1], w[o + 2], w[o + 3])
+        using L = Lay<false>;
         if (SIDE_A) {
-            ST(kAhr, w_hr);
-            ST(kAhi, w_hi);
-            ST(kAlr, w_lr);
-            ST(kAli, w_li);
-            ST(kA2r, w_xr);
-            ST(kA2i, w_xi);
+            ST(L::Ahr, w_hr);
+            ST(L::Ahi, w_hi);
+            ST(L::Alr, w_lr);
+            ST(L::Ali, w_li);
+            ST(L::A2r, w_xr);
+            ST(L::A2i, w_xi);
         } else {
-            ST(kBhr, w_hr);
-            ST(kBhi, w_hi);
-            ST(kBlr, w_lr);
-            ST(kBli, w_li);
-            ST(kB2r, w_xr);
-            ST(kB2i, w_xi);
+            ST(L::Bhr, w_hr);
+            ST(L::Bhi, w_hi);
+            ST(L::Blr, w_lr);
+            ST(L::Bli, w_li);
+            ST(L::B2r, w_xr);
+            ST(L::B2i, w_xi);
+        }
+#undef ST
+    }
+}
+
+// 1.0 where tile-relative index i lies in the window [lo, hi) held in
+// bytes `sh` (lo) and `sh + 8` (hi) of the packed window word, else 0.
+__device__ __forceinline__ float in_window(float packed, int sh, int i) {
+    const uint32_t w = __float_as_uint(packed);
+    const int lo = (int)((w >> sh) & 0xffu), hi = (int)((w >> (sh + 8)) & 0xffu);
+    return (i >= lo && i < hi) ? 1.f : 0.f;
+}
+
+// Fresnel factors of 8 points of a stage for two rows (SIDE_A) or columns,
+// the Fresnel counterpart of produce_stage: the phase splits exactly into
+// a row part and a column part, so there is no series and no cross pair.
+// CUT: some point of the stage has a window that cuts the tile; then the
+// window rectangle becomes 0/1 factor masks (ia, ib: tile-relative indices
+// of the thread's two rows/columns) and each point's expansion centre
+// (u0, v0: offset from the tile centre) lies inside its window, so that the
+// factor phases stay within the window's chirp (<= 64 turns) however far the
+// point lies from the tile centre. Otherwise u0 = v0 = 0 and every mask is 1.
+template <bool SIDE_A, bool CUT>
+__device__ __forceinline__ void produce_stage_fr(const TcRsPair* prs, float offa, float offb, int ia, int ib,
+                                                 uint32_t ro0, uint32_t ro1) {
+    using f2::v2;
+    const v2 offpa = f2::splat(offa), off2pa = f2::splat(offa * offa);
+    const v2 offpb = f2::splat(offb), off2pb = f2::splat(offb * offb);
+    const v2 two_pi = f2::splat(kTwoPiF);
+    uint32_t w_hr[8], w_hi[8], w_lr[8], w_li[8];
+#pragma unroll
+    for (int qq = 0; qq < 8; ++qq) {
+        const int q = (qq & 1) * 4 + (qq >> 1);   // output slot: row (qq & 1), pair qq >> 1
+        const v2 offp = (qq & 1) ? offpb : offpa;
+        const ulonglong2* R = reinterpret_cast<const ulonglong2*>(&prs[qq >> 1]);
+        const ulonglong2 r0 = R[0];   // h, P
+        v2 d, d2;
+        ulonglong2 r1;
+        if (CUT) {
+            r1 = R[1];   // u0, window
+        }
+        if (SIDE_A) {
+            const ulonglong2 r2 = R[2];   // Q, v0
+            const ulonglong2 r3 = R[3];   // fc, ac
+            if (CUT) {
+                d = f2::sub(offp, r2.y);
+                d2 = f2::mul(d, d);
+            } else {
+                d = offp;
+                d2 = (qq & 1) ? off2pb : off2pa;
+            }
+            v2 ph = f2::fma(r2.x, d, f2::fma(r0.x, d2, r3.x));   // turns
+            v2 amp = r3.y;
+            if (CUT) {
+                float wa, wb;
+                f2::unpack(r1.y, wa, wb);
+                const int idx = (qq & 1) ? ib : ia;
+                amp = f2::mul(amp, f2::pack(in_window(wa, 16, idx), in_window(wb, 16, idx)));
+            }
+            ph = f2::mul(ph, two_pi);
+            float p0, p1, s0, c0, s1, c1;
+            f2::unpack(ph, p0, p1);
+            __sincosf(p0, &s0, &c0);
+            __sincosf(p1, &s1, &c1);
+            const v2 vr = f2::mul(amp, f2::pack(c0, c1)), vi = f2::mul(amp, f2::pack(s0, s1));
+            w_hr[q] = bf2v(vr);
+            w_hi[q] = bf2v(vi);
+            w_lr[q] = bf2v(f2::sub(vr, bf2_to_v2(w_hr[q])));
+            w_li[q] = bf2v(f2::sub(vi, bf2_to_v2(w_hi[q])));
+        } else {
+            if (CUT) {
+                d = f2::sub(offp, r1.x);
+                d2 = f2::mul(d, d);
+            } else {
+                d = offp;
+                d2 = (qq & 1) ? off2pb : off2pa;
+            }
+            v2 ph = f2::fma(r0.y, d, f2::mul(r0.x, d2));
+            ph = f2::mul(ph, two_pi);
+            float p0, p1, s0, c0, s1, c1;
+            f2::unpack(ph, p0, p1);
+            __sincosf(p0, &s0, &c0);
+            __sincosf(p1, &s1, &c1);
+            v2 vr = f2::pack(c0, c1), vi = f2::pack(s0, s1);
+            if (CUT) {
+                float wa, wb;
+                f2::unpack(r1.y, wa, wb);
+                const int idx = (qq & 1) ? ib : ia;
+                const v2 m = f2::pack(in_window(wa, 0, idx), in_window(wb, 0, idx));
+                vr = f2::mul(vr, m);
+                vi = f2::mul(vi, m);
+            }
+            w_hr[q] = bf2v(vr);
+            w_hi[q] = bf2v(vi);
+            w_lr[q] = bf2v(f2::sub(vr, bf2_to_v2(w_hr[q])));
+            w_li[q] = bf2v(f2::sub(vi, bf2_to_v2(w_hi[q])));
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const uint32_t ro = h ? ro1 : ro0;
+        const int o = 4 * h;
+        using L = Lay<true>;
+#define ST(plane, w) st_v4(ro + (plane) * kPlane, w[o], w[o + 1], w[o + 2], w[o + 3])
+        if (SIDE_A) {
+            ST(L::Ahr, w_hr);
+            ST(L::Ahi, w_hi);
+            ST(L::Alr, w_lr);
+            ST(L::Ali, w_li);
+        } else {
+            ST(L::Bhr, w_hr);
+            ST(L::Bhi, w_hi);
+            ST(L::Blr, w_lr);
+            ST(L::Bli, w_li);
         }
 #undef ST
     }
@@ -237,9 +374,11 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
 // every producer warp drained the previous run out of D. Issuing blocks
 // while the tensor core's queue is full (about as long as a stage's MMAs
 // take), which is why a warp of its own does it. False on abort.
+template <bool FR>
 __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* base, uint64_t* full, uint64_t* empty,
                                             uint64_t* acc_full, uint64_t* acc_empty, volatile int* abort,
                                             uint32_t tmem) {
+    using L = Lay<FR>;
     constexpr uint32_t id_bf256 = idesc_f16(1u, false, kRsTcTile, 2 * kRsTcTile);   // BF16, N=256
     constexpr uint32_t id_bf = idesc_f16(1u, false, kRsTcTile, kRsTcTile);          // BF16, N=128
     constexpr uint32_t id_bfn = idesc_f16(1u, true, kRsTcTile, kRsTcTile);          // BF16, N=128, -A
@@ -249,25 +388,27 @@ __device__ __forceinline__ bool issue_stage(int k, int total, unsigned char* bas
     const int p = k / kPeriod;
     const bool opens = (k % kPeriod) == 0;
     if (opens && p >= 1 && !mbar_wait_for(acc_empty, (uint32_t)(p - 1) & 1u, abort, kWaitNs)) return false;
-    const int s = k % kStagesTc;
-    if (!mbar_wait_for(&full[s], (uint32_t)(k / kStagesTc) & 1u, abort, kWaitNs)) return false;
+    const int s = k % L::Stages;
+    if (!mbar_wait_for(&full[s], (uint32_t)(k / L::Stages) & 1u, abort, kWaitNs)) return false;
     tc_fence_after();
     const uint32_t d = tmem;
-    const uint32_t st = smem_u32(base + s * kStageBytesTc);
+    const uint32_t st = smem_u32(base + s * L::kStageBytes);
 #define PL(x) sw32_desc(st + (uint32_t)((x) * kPlane))
     const uint32_t dre = d, dim = d + kRsTcTile, acc = opens ? 0u : 1u;
-    umma(d, PL(kAhr), PL(kBhr), id_bf256, acc);   // re += Ar Br, im += Ar Bi
-    umma(dre, PL(kAhi), PL(kBhi), id_bfn, 1u);    // re -= Ai Bi
-    umma(dim, PL(kAhi), PL(kBhr), id_bf, 1u);     // im += Ai Br
-    umma(d, PL(kAhr), PL(kBlr), id_bf256, 1u);
-    umma(dre, PL(kAhi), PL(kBli), id_bfn, 1u);
-    umma(dim, PL(kAhi), PL(kBlr), id_bf, 1u);
-    umma(d, PL(kAlr), PL(kBhr), id_bf256, 1u);
-    umma(dre, PL(kAli), PL(kBhi), id_bfn, 1u);
-    umma(dim, PL(kAli), PL(kBhr), id_bf, 1u);
-    umma(d, PL(kA2r), PL(kB2r), id_h256, 1u);
-    umma(dre, PL(kA2i), PL(kB2i), id_hn, 1u);
-    umma(dim, PL(kA2i), PL(kB2r), id_h, 1u);
+    umma(d, PL(L::Ahr), PL(L::Bhr), id_bf256, acc);   // re += Ar Br, im += Ar Bi
+    umma(dre, PL(L::Ahi), PL(L::Bhi), id_bfn, 1u);    // re -= Ai Bi
+    umma(dim, PL(L::Ahi), PL(L::Bhr), id_bf, 1u);     // im += Ai Br
+    umma(d, PL(L::Ahr), PL(L::Blr), id_bf256, 1u);
+    umma(dre, PL(L::Ahi), PL(L::Bli), id_bfn, 1u);
+    umma(dim, PL(L::Ahi), PL(L::Blr), id_bf, 1u);
+    umma(d, PL(L::Alr), PL(L::Bhr), id_bf256, 1u);
+    umma(dre, PL(L::Ali), PL(L::Bhi), id_bfn, 1u);
+    umma(dim, PL(L::Ali), PL(L::Bhr), id_bf, 1u);
+    if constexpr (!FR) {
+        umma(d, PL(L::A2r), PL(L::B2r), id_h256, 1u);
+        umma(dre, PL(L::A2i), PL(L::B2i), id_hn, 1u);
+        umma(dim, PL(L::A2i), PL(L::B2r), id_h, 1u);
+    }
 #undef PL
     umma_commit(&empty[s]);   // frees the stage once these MMAs have read it
     if ((k % kPeriod) == kPeriod - 1 || k == total - 1) umma_commit(acc_full);
@@ -398,18 +539,120 @@ __device__ __forceinline__ bool make_record(TcRsPair* buf, int t, bool valid, co
     return is_left;
 }
 
+// Fresnel values of point idx on the tile into record pair slot t of buf
+// (ophgen/src/ophGen.cpp:447-514): with s = 1/(2 z lambda) and an expansion
+// centre (Xe, Ye) = tile centre + (u0, v0), dx0 = Xe - x, dy0 = Ye - y,
+//   phase (turns) = frac(s (dx0^2 + dy0^2) + z / lambda)      [FP64, ~1e6 turns]
+//                 + s (2 dy0 e + e^2) + s (2 dx0 d + d^2),     e = v - v0, d = u - u0
+// exactly. h = s, P = 2 dx0 s, Q = 2 dy0 s and the amplitude coef / amax
+// (0 when the window misses the tile). The window rectangle, relative to the
+// tile's first column and row, is packed in bytes (xlo, xhi, ylo, yhi). When
+// the window holds the whole tile the centre is the tile centre (u0 = v0 =
+// 0); otherwise it is the tile centre clamped into the window. Returns true
+// for a point whose window cuts the tile (masks needed).
+__device__ __forceinline__ bool make_record_fr(TcRsPair* buf, int t, bool valid, const PointRec& p,
+                                               const RsTcTile& tile, double inv_lambda, float inv_amax,
+                                               const ChannelGeom& g, int X0, int Y0) {
+    float h = 0.f, P = 0.f, u0 = 0.f, win = 0.f, Q = 0.f, v0 = 0.f, fc = 0.f, ac = 0.f;
+    bool cut = false;
+    if (valid) {
+        const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
+        const int iy0 = max(Y0, p.y_lo), iy1 = min(tile.vy1, p.y_hi);
+        if (ix0 < ix1 && iy0 < iy1) {
+            const int xlo = ix0 - X0, xhi = ix1 - X0, ylo = iy0 - Y0, yhi = iy1 - Y0;
+            const bool cut_x = !(ix0 == X0 && ix1 == tile.vx1), cut_y = !(iy0 == Y0 && iy1 == tile.vy1);
+            cut = cut_x || cut_y;
+            const int c0 = cut_x ? min(max(kRsTcHalf, xlo), xhi - 1) : kRsTcHalf;
+            const int r0 = cut_y ? min(max(kRsTcHalf, ylo), yhi - 1) : kRsTcHalf;
+            const double du0 = (double)(c0 - kRsTcHalf) * g.ppX, dv0 = (double)(kRsTcHalf - r0) * g.ppY;
+            const double dxc = (tile.Xc - p.x) + du0, dyc = (tile.Yc - p.y) + dv0;
+            const double sq = p.aux;   // 1 / (2 z lambda)
+            const double tc = sq * (dxc * dxc + dyc * dyc) + p.z * inv_lambda;
+            h = (float)sq;
+            P = (float)(2.0 * dxc * sq);
+            Q = (float)(2.0 * dyc * sq);
+            u0 = (float)du0;
+            v0 = (float)dv0;
+            fc = (float)(tc - rint(tc));
+            ac = (float)p.coef * inv_amax;
+            win = __uint_as_float((uint32_t)xlo | ((uint32_t)xhi << 8) | ((uint32_t)ylo << 16) |
+                                  ((uint32_t)yhi << 24));
+        }
+    }
+    float* f = reinterpret_cast<float*>(&buf[t >> 1]) + (t & 1);
+    f[0] = h;
+    f[2] = P;
+    f[4] = u0;
+    f[6] = win;
+    f[8] = Q;
+    f[10] = v0;
+    f[12] = fc;
+    f[14] = ac;
+    return cut;
+}
+
 // One CTA per 128x128 tile of one channel. Warps 0-7 produce the factors
 // (threads 0-127 the rows, 128-255 the columns: two rows or columns and 8
 // points of a stage each) and drain the accumulator; warp 8 allocates TMEM and its lane 0
 // issues the MMAs; warps 9-11 form the point records of the chunks, one
 // chunk ahead of the producers (double-buffered, an mbarrier pair per buffer).
-__global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
+// Called by every part of a tile once its own writes are done: the last
+// part to arrive adds the partial tiles into the field (field + partials[0]
+// + ... in that order, whoever arrives last, so the result is
+// deterministic) and discards the partials' 128-byte lines that lie wholly
+// inside the tile from L2 (nothing reads them again). s_flag: one word of
+// shared memory.
+__device__ __noinline__ void sum_parts(const TcRsArgs& a, int ch, int tx, int X0, int Y0, int* s_flag) {
+    const ChannelGeom& g = a.jg.ch[0];
+    const int64_t plane = (int64_t)g.pnX * g.pnY;
+    const int64_t field_elems = plane * a.jg.n_channels;
+    __syncthreads();   // every thread of this part has written its share
+    if (threadIdx.x == 0) {
+        __threadfence();   // release this part's writes before taking a ticket
+        const int t = atomicAdd(&a.tickets[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + tx], 1);
+        *s_flag = (t == a.ksplit - 1);
+        if (*s_flag) __threadfence();   // acquire the other parts' writes
+    }
+    __syncthreads();
+    if (!*s_flag) return;
+    const int cols = min(kRsTcTile, g.pnX - X0), rows = min(kRsTcTile, g.pnY - Y0);
+    double2* field = a.field + (int64_t)ch * plane;
+    for (int i = threadIdx.x; i < rows * cols; i += blockDim.x) {
+        const int r = i / cols, c = i - r * cols;
+        const int64_t o = (int64_t)(Y0 + r) * g.pnX + X0 + c;
+        double2 v = __ldcg(&field[o]);   // written by part 0, possibly on another SM
+        for (int k = 1; k < a.ksplit; ++k) {
+            const double2 p = __ldcg(&a.partials[(int64_t)(k - 1) * field_elems + (int64_t)ch * plane + o]);
+            v.x += p.x;
+            v.y += p.y;
+        }
+        field[o] = v;
+    }
+    __syncthreads();
+    // 128-byte lines of the partial rows that lie wholly inside the tile
+    const int lines_per_row = kRsTcTile * (int)sizeof(double2) / 128 + 1;
+    for (int k = 1; k < a.ksplit; ++k) {
+        const char* base =
+            reinterpret_cast<const char*>(a.partials + (int64_t)(k - 1) * field_elems + (int64_t)ch * plane);
+        for (int i = threadIdx.x; i < rows * lines_per_row; i += blockDim.x) {
+            const int r = i / lines_per_row, l = i - r * lines_per_row;
+            const uintptr_t b0 = (uintptr_t)(base + ((int64_t)(Y0 + r) * g.pnX + X0) * (int64_t)sizeof(double2));
+            const uintptr_t b1 = b0 + (uintptr_t)cols * sizeof(double2);
+            const uintptr_t line = ((b0 + 127) & ~(uintptr_t)127) + (uintptr_t)l * 128;
+            if (line + 128 <= b1) asm volatile("discard.global.L2 [%0], 128;" ::"l"(line) : "memory");
+        }
+    }
+}
+
+template <bool FR>
+__device__ __forceinline__ void tile_body(const TcRsArgs& a) {
+    using L = Lay<FR>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    TcRsPair* s_rec = reinterpret_cast<TcRsPair*>(base + kStagesTc * kStageBytesTc);   // [2][kChunkTc / 2]
+    TcRsPair* s_rec = reinterpret_cast<TcRsPair*>(base + L::Stages * L::kStageBytes);   // [2][kChunkTc / 2]
     uint64_t* full = reinterpret_cast<uint64_t*>(s_rec + kChunkTc);
-    uint64_t* empty = full + kStagesTc;
-    uint64_t* acc_full = empty + kStagesTc;   // MMA -> drains: D holds a finished run
+    uint64_t* empty = full + L::Stages;
+    uint64_t* acc_full = empty + L::Stages;   // MMA -> drains: D holds a finished run
     uint64_t* acc_empty = acc_full + 1;       // drains -> MMA: D was read
     uint64_t* drain_bar = acc_empty + 1;      // abort path: issued MMAs complete
     uint64_t* rec_full = drain_bar + 1;       // [2] record warps -> producers: a chunk's records are formed
@@ -417,11 +660,14 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(rec_empty + 2);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
+    // Fresnel: per record buffer, one word per stage: nonzero when a point
+    // of the stage has a window that cuts the tile
+    uint32_t* s_cut = tmem_slot + 4;   // [2][kStagesPerChunk]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ch = blockIdx.z / a.ksplit, part = blockIdx.z % a.ksplit;
+    const int ch = blockIdx.z, part = blockIdx.x % a.ksplit, tx = blockIdx.x / a.ksplit;
     const ChannelGeom& g = a.jg.ch[ch];
-    const int X0 = blockIdx.x * kRsTcTile, Y0 = blockIdx.y * kRsTcTile;
+    const int X0 = tx * kRsTcTile, Y0 = blockIdx.y * kRsTcTile;
     const int64_t p_beg = a.p_base + (int64_t)part * a.pps;
     const int64_t n = min(a.p_base + a.p_count, p_beg + a.pps) - p_beg;   // this CTA's points: [p_beg, p_beg + n)
     double2* out = part == 0 ? a.field
@@ -431,7 +677,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     const int periods = (total + kPeriod - 1) / kPeriod;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStagesTc; ++s) {
+        for (int s = 0; s < L::Stages; ++s) {
             mbar_init(&full[s], kProdWarps);
             mbar_init(&empty[s], 1);
         }
@@ -475,7 +721,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     if (warp == kMmaWarp) {
         if (lane == 0) {
             for (; issued < total; ++issued)
-                if (!issue_stage(issued, total, base, full, empty, acc_full, acc_empty, abort, tmem)) break;
+                if (!issue_stage<FR>(issued, total, base, full, empty, acc_full, acc_empty, abort, tmem)) break;
             if (issued < total && issued > 0) {
                 // aborted: wait (bounded) for the MMAs already issued before TMEM is released
                 umma_commit(drain_bar);
@@ -488,7 +734,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
         // records of chunk c into buffer c & 1, once the producers released
         // the chunk that used it before (c - 2)
         const int rt = t - (kProducers + 32);
-        const int64_t mask_base = (((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x) * a.mask_words;
+        const int64_t mask_base = (((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + tx) * a.mask_words;
         for (int c = 0; c < nchunks && !dead; ++c) {
             const int b = c & 1;
             if (c >= 2) {
@@ -500,13 +746,24 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
             for (int j = rt; j < kChunkTc; j += kRecThreads) {
                 const int64_t idx = (int64_t)c * kChunkTc + j;
                 const bool valid = idx < n;
-                const bool l = make_record(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda, inv_amax, X0,
-                                           Y0, left);
-                // the warp's 32 consecutive points -> one word of the left-pair
-                // mask (this CTA alone writes it: pps is a multiple of kChunkTc)
-                const uint32_t bits = __ballot_sync(0xffffffffu, l);
-                if (lane == 0 && a.mask)
-                    a.mask[mask_base + (((int64_t)part * a.pps + idx) >> 5)] = bits;
+                if constexpr (FR) {
+                    const bool cut = make_record_fr(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda,
+                                                    inv_amax, g, X0, Y0);
+                    // the warp's 32 consecutive points are two whole stages
+                    const uint32_t bits = __ballot_sync(0xffffffffu, cut);
+                    if (lane == 0) {
+                        s_cut[b * kStagesPerChunk + (j >> 4)] = bits & 0xffffu;
+                        s_cut[b * kStagesPerChunk + (j >> 4) + 1] = bits >> 16;
+                    }
+                } else {
+                    const bool l = make_record(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda, inv_amax,
+                                               X0, Y0, left);
+                    // the warp's 32 consecutive points -> one word of the left-pair
+                    // mask (this CTA alone writes it: pps is a multiple of kChunkTc)
+                    const uint32_t bits = __ballot_sync(0xffffffffu, l);
+                    if (lane == 0 && a.mask)
+                        a.mask[mask_base + (((int64_t)part * a.pps + idx) >> 5)] = bits;
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&rec_full[b]);
@@ -523,15 +780,31 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
             const TcRsPair* rb = s_rec + b * (kChunkTc / 2);
             const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
             for (int it = it0; it < it1; ++it) {
-                const int s = it % kStagesTc;
+                const int s = it % L::Stages;
                 bool ok = true;
-                if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / kStagesTc) & 1u) ^ 1u, abort, kWaitNs);
+                if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / L::Stages) & 1u) ^ 1u, abort, kWaitNs);
                 dead = !__shfl_sync(0xffffffffu, ok, 0);
                 if (dead) break;
-                const uint32_t sb = smem_u32(base + s * kStageBytesTc);
+                const uint32_t sb = smem_u32(base + s * L::kStageBytes);
                 const TcRsPair* recs8 = rb + ((it - it0) * kStagePts) / 2 + 4 * kc;
-                if (side_a) produce_stage<true>(recs8, off, offb, sb + row_off0, sb + row_off1);
-                else produce_stage<false>(recs8, off, offb, sb + row_off0, sb + row_off1);
+                if constexpr (FR) {
+                    // warp-uniform: every thread reads the same stage flag
+                    const bool cut = s_cut[b * kStagesPerChunk + (it - it0)] != 0;
+                    if (cut) {
+                        if (side_a) produce_stage_fr<true, true>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                                 sb + row_off1);
+                        else produce_stage_fr<false, true>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                           sb + row_off1);
+                    } else {
+                        if (side_a) produce_stage_fr<true, false>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                                  sb + row_off1);
+                        else produce_stage_fr<false, false>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                            sb + row_off1);
+                    }
+                } else {
+                    if (side_a) produce_stage<true>(recs8, off, offb, sb + row_off0, sb + row_off1);
+                    else produce_stage<false>(recs8, off, offb, sb + row_off0, sb + row_off1);
+                }
                 fence_async_smem();   // generic-proxy writes -> visible to the tensor core
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[s]);
@@ -558,23 +831,65 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_const
     tc_fence_after();
     if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemColsTc);
     if (threadIdx.x == 0) {
-        if (*s_left) atomicAdd(&a.left[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + blockIdx.x], *s_left);
+        if (*s_left) atomicAdd(&a.left[((int64_t)ch * a.tiles_y + blockIdx.y) * a.tiles_x + tx], *s_left);
         if (*abort) atomicExch(a.error, 1);
     }
+    if (a.ksplit > 1) sum_parts(a, ch, tx, X0, Y0, s_left);
+}
+
+__global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
+    tile_body<false>(a);
+}
+
+// Fresnel on the tensor cores, factors generated on chip: the same tile
+// pipeline with no cross pair and no CUDA-core complement.
+__global__ void __launch_bounds__(kThreadsTc, 1) tc_fresnel_kernel(const __grid_constant__ TcRsArgs a) {
+    tile_body<true>(a);
 }
 
 // Largest coef / z^2 of a channel: bounds every coef / r_c^2, so the
 // factors stay within [-1, 1] (FP16 range for the cross pair).
-__global__ void rs_amax_kernel(const PointRec* __restrict__ recs, int64_t n, float* out) {
+// (RS: coef / z^2; Fresnel, with per_z2 false: coef, the factor amplitude
+// before any window.)
+__global__ void rs_amax_kernel(const PointRec* __restrict__ recs, int64_t n, float* out, bool per_z2 = true) {
     float m = 0.f;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        m = fmaxf(m, fabsf((float)(recs[i].coef / recs[i].aux)));
+        m = fmaxf(m, fabsf((float)(per_z2 ? recs[i].coef / recs[i].aux : recs[i].coef)));
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));   // m >= 0
 }
 
 size_t align_up(size_t v, size_t al) { return (v + al - 1) / al * al; }
+
+// One CTA per SM: split every tile's points into k parts so that the CTA
+// count fills whole waves (each extra part costs a field-sized partial and a
+// summing pass: demand a 3% gain, at least 1,024 points a part, at most
+// 2 GiB of partials). Parts are whole chunks of kChunkTc points (the
+// left-pair mask words of a part are its own), and none is empty.
+void choose_tile_split(int64_t tiles, int64_t n_points, size_t field_bytes, int sm_count, int* ksplit_out,
+                       int64_t* pps_out) {
+    const int slots = sm_count > 0 ? sm_count : 1;
+    auto part_points = [&](int k) {
+        const int64_t p = (n_points + k - 1) / k;
+        return (p + kChunkTc - 1) / kChunkTc * kChunkTc;
+    };
+    int ksplit = 1;
+    double best = 0.0;
+    for (int k = 1; k <= 8; ++k) {
+        if (k > 1 && (n_points / k < 1024 || (size_t)(k - 1) * field_bytes > ((size_t)2 << 30) ||
+                      n_points - (k - 1) * part_points(k) < 1))
+            break;
+        const double waves = (double)(tiles * k) / slots;
+        const double eff = waves / std::ceil(waves);
+        if (eff > best + 0.03) {
+            best = eff;
+            ksplit = k;
+        }
+    }
+    *ksplit_out = ksplit;
+    *pps_out = part_points(ksplit);
+}
 
 }  // namespace
 
@@ -593,34 +908,13 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
     const size_t rec_bytes = align_up(sizeof(PointRec) * n_points * nch, 256);
     const size_t left_bytes = align_up(sizeof(int32_t) * (size_t)nch * tiles_x * tiles_y, 256);
-    // One CTA per SM: split every tile's points into k parts so that the
-    // CTA count fills whole waves (each extra part costs a field-sized
-    // partial and a summing pass: demand a 3% gain, at least 1,024 points
-    // a part, at most 2 GiB of partials). Parts are whole chunks of
-    // kChunkTc points (the left-pair mask words of a part are its own), and
-    // none is empty.
     const int64_t tiles = (int64_t)tiles_x * tiles_y * nch;
     const size_t field_bytes = sizeof(double2) * (size_t)nch * pnX * pnY;
-    const int slots = sm_count > 0 ? sm_count : 1;
-    auto part_points = [&](int k) {
-        const int64_t p = ((int64_t)n_points + k - 1) / k;
-        return (p + kChunkTc - 1) / kChunkTc * kChunkTc;
-    };
     int ksplit = 1;
-    double best = 0.0;
-    for (int k = 1; k <= 8; ++k) {
-        if (k > 1 && ((int64_t)n_points / k < 1024 || (size_t)(k - 1) * field_bytes > ((size_t)2 << 30) ||
-                      (int64_t)n_points - (k - 1) * part_points(k) < 1))
-            break;
-        const double waves = (double)(tiles * k) / slots;
-        const double eff = waves / std::ceil(waves);
-        if (eff > best + 0.03) {
-            best = eff;
-            ksplit = k;
-        }
-    }
-    const int64_t pps = part_points(ksplit);
+    int64_t pps = 0;
+    choose_tile_split(tiles, (int64_t)n_points, field_bytes, sm_count, &ksplit, &pps);
     const size_t part_bytes = align_up(field_bytes * (size_t)(ksplit - 1), 256);
+    const size_t ticket_bytes = align_up(sizeof(int32_t) * (size_t)tiles, 256);
     // left-pair mask: one bit per (tile, point); without room for it the
     // complement re-tests eligibility instead
     static_assert(kChunkTc == 256, "tc_rs_mask_words assumes chunks of 256 points");
@@ -628,17 +922,18 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     size_t mask_bytes = align_up(sizeof(uint32_t) * (size_t)tiles * (size_t)mask_words, 256);
     if (mask_bytes > ((size_t)4 << 30)) mask_bytes = 0;
     unsigned char* buf = nullptr;
-    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + part_bytes + mask_bytes + 256, pool, s) !=
-        cudaSuccess)
+    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + left_bytes + ticket_bytes + part_bytes + mask_bytes + 256,
+                                pool, s) != cudaSuccess)
         return fail(OPHPC_ERROR_OUT_OF_MEMORY, "tensor-core RS scratch allocation failed");
     PointRec* recs = (PointRec*)buf;
     int32_t* left = (int32_t*)(buf + rec_bytes);
-    double2* partials = ksplit > 1 ? (double2*)(buf + rec_bytes + left_bytes) : nullptr;
-    uint32_t* mask = mask_bytes ? (uint32_t*)(buf + rec_bytes + left_bytes + part_bytes) : nullptr;
-    float* amax = (float*)(buf + rec_bytes + left_bytes + part_bytes + mask_bytes);   // [3]
+    int32_t* tickets = (int32_t*)(buf + rec_bytes + left_bytes);
+    double2* partials = ksplit > 1 ? (double2*)(buf + rec_bytes + left_bytes + ticket_bytes) : nullptr;
+    uint32_t* mask = mask_bytes ? (uint32_t*)(buf + rec_bytes + left_bytes + ticket_bytes + part_bytes) : nullptr;
+    float* amax = (float*)(buf + rec_bytes + left_bytes + ticket_bytes + part_bytes + mask_bytes);   // [3]
     int* errw = (int*)(amax + 4);
     cudaMemsetAsync(amax, 0, 32, s);   // amax[0..3] and the error word
-    cudaMemsetAsync(left, 0, left_bytes, s);
+    cudaMemsetAsync(left, 0, left_bytes + ticket_bytes, s);
 
     launch_prep(d_vertices, (int64_t)n_points, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window,
                 (int)OPHPC_DIFF_RS, jg, recs, s);
@@ -662,13 +957,11 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     ta.ksplit = ksplit;
     ta.pps = pps;
     ta.partials = partials;
+    ta.tickets = tickets;
     ta.mask = mask;
     ta.mask_words = mask_words;
     count_launches(1);
-    tc_rs_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)(nch * ksplit)), kThreadsTc, kSmemTc, s>>>(ta);
-    JobGeom js = jg;
-    js.ksplit = ksplit;
-    launch_sum_partials(js, (double2*)d_field, partials, s);
+    tc_rs_kernel<<<dim3((unsigned)(tiles_x * ksplit), (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTc, s>>>(ta);
 
     // the CUDA-core complement: the pairs the tensor-core kernel left
     JobGeom jc = jg;
@@ -751,6 +1044,111 @@ cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_
     jc.tc_mask = d_mask;
     jc.tc_mask_words = mask_words;
     launch_rs(d_recs, jc, d_field, nullptr, s);
+    return cudaGetLastError();
+}
+
+ophpc_status tc_generate_fresnel_tiles(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
+                                       const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field,
+                                       int sm_count, cudaStream_t s, std::string* err, int* d_err_out) {
+    auto fail = [&](ophpc_status st, const char* msg) {
+        if (err) *err = msg;
+        return st;
+    };
+    if (cudaFuncSetAttribute(tc_fresnel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemTcFr) !=
+        cudaSuccess)
+        return fail(OPHPC_ERROR_CUDA, "cudaFuncSetAttribute(tc_fresnel_kernel) failed");
+    const int nch = jg.n_channels;
+    const int pnX = cfg->pixel_number[0], pnY = cfg->pixel_number[1];
+    const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
+    const int64_t tiles = (int64_t)tiles_x * tiles_y * nch;
+    const size_t field_bytes = sizeof(double2) * (size_t)nch * pnX * pnY;
+    int ksplit = 1;
+    int64_t pps = 0;
+    choose_tile_split(tiles, (int64_t)n_points, field_bytes, sm_count, &ksplit, &pps);
+    const size_t rec_bytes = align_up(sizeof(PointRec) * n_points * nch, 256);
+    const size_t part_bytes = align_up(field_bytes * (size_t)(ksplit - 1), 256);
+    const size_t ticket_bytes = align_up(sizeof(int32_t) * (size_t)tiles, 256);
+    unsigned char* buf = nullptr;
+    if (cudaMallocFromPoolAsync((void**)&buf, rec_bytes + ticket_bytes + part_bytes + 256, pool, s) != cudaSuccess)
+        return fail(OPHPC_ERROR_OUT_OF_MEMORY, "tensor-core Fresnel scratch allocation failed");
+    PointRec* recs = (PointRec*)buf;
+    int32_t* tickets = (int32_t*)(buf + rec_bytes);
+    double2* partials = ksplit > 1 ? (double2*)(buf + rec_bytes + ticket_bytes) : nullptr;
+    float* amax = (float*)(buf + rec_bytes + ticket_bytes + part_bytes);   // [3]
+    int* errw = (int*)(amax + 4);
+    cudaMemsetAsync(amax, 0, 32, s);   // amax[0..3] and the error word
+    cudaMemsetAsync(tickets, 0, ticket_bytes, s);
+    launch_prep(d_vertices, (int64_t)n_points, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window,
+                (int)OPHPC_DIFF_FRESNEL, jg, recs, s);
+    for (int c = 0; c < nch; ++c) {
+        count_launches(1);
+        rs_amax_kernel<<<256, 256, 0, s>>>(recs + (int64_t)c * n_points, (int64_t)n_points, amax + c, false);
+    }
+    TcRsArgs ta;
+    std::memset(&ta, 0, sizeof(ta));
+    ta.jg = jg;
+    ta.jg.accumulate = 0;
+    ta.recs = recs;
+    ta.field = (double2*)d_field;
+    ta.amax = amax;
+    ta.error = errw;
+    ta.tiles_x = tiles_x;
+    ta.tiles_y = tiles_y;
+    ta.p_base = 0;
+    ta.p_count = (int64_t)n_points;
+    ta.ksplit = ksplit;
+    ta.pps = pps;
+    ta.partials = partials;
+    ta.tickets = tickets;
+    count_launches(1);
+    tc_fresnel_kernel<<<dim3((unsigned)(tiles_x * ksplit), (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTcFr,
+                        s>>>(ta);
+    cudaError_t e = cudaGetLastError();
+    int herr = 0;
+    if (d_err_out) {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d_err_out, errw, sizeof(int), cudaMemcpyDeviceToDevice, s);
+    } else {
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    cudaFreeAsync(buf, s);
+    if (e != cudaSuccess) return fail(OPHPC_ERROR_CUDA, cudaGetErrorString(e));
+    if (herr) return fail(OPHPC_ERROR_TIMEOUT, "tensor-core Fresnel kernel wait timed out");
+    return OPHPC_SUCCESS;
+}
+
+void launch_fresnel_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t s) {
+    for (int c = 0; c < n_channels; ++c) {
+        count_launches(1);
+        rs_amax_kernel<<<256, 256, 0, s>>>(d_recs + (int64_t)c * n_points, n_points, d_amax + c, false);
+    }
+}
+
+cudaError_t launch_tc_fresnel_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1,
+                                    bool accumulate, double2* d_field, const float* d_amax, int* d_err,
+                                    cudaStream_t s) {
+    cudaError_t e = cudaFuncSetAttribute(tc_fresnel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSmemTcFr);
+    if (e != cudaSuccess || p1 <= p0) return e;
+    const int nch = jg.n_channels;
+    const int pnX = jg.ch[0].pnX, pnY = jg.ch[0].pnY;
+    const int tiles_x = (pnX + kRsTcTile - 1) / kRsTcTile, tiles_y = (pnY + kRsTcTile - 1) / kRsTcTile;
+    TcRsArgs ta;
+    std::memset(&ta, 0, sizeof(ta));
+    ta.jg = jg;
+    ta.jg.accumulate = accumulate ? 1 : 0;
+    ta.recs = d_recs;
+    ta.field = d_field;
+    ta.amax = d_amax;
+    ta.error = d_err;
+    ta.tiles_x = tiles_x;
+    ta.tiles_y = tiles_y;
+    ta.p_base = p0;
+    ta.p_count = p1 - p0;
+    ta.ksplit = 1;
+    ta.pps = p1 - p0;
+    count_launches(1);
+    tc_fresnel_kernel<<<dim3((unsigned)tiles_x, (unsigned)tiles_y, (unsigned)nch), kThreadsTc, kSmemTcFr, s>>>(ta);
     return cudaGetLastError();
 }
 

@@ -146,4 +146,19 @@ cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_
                                double2* d_field, const float* d_amax, int32_t* d_left, uint32_t* d_mask,
                                int64_t mask_words, int* d_err, cudaStream_t stream);
 
+// Fresnel on the tensor cores with the factors generated on chip
+// (tc_fresnel_kernel, split-BF16, FP32 accumulation, FP64 field): the same
+// 128x128 tile pipeline as the RS kernel; the phase splits exactly and the
+// window is a rectangle, so every pair runs on the tensor cores. Whole call
+// (same conventions as tc_generate_rs), and the point-range building blocks
+// for the serving engine: launch_fresnel_amax (per channel the largest coef
+// into d_amax, zeroed by the caller) and launch_tc_fresnel_range.
+ophpc_status tc_generate_fresnel_tiles(cudaMemPool_t pool, const JobGeom& jg, const ophpc_config* cfg,
+                                       const ophpc_vertex* d_vertices, uint64_t n_points, double* d_field,
+                                       int sm_count, cudaStream_t stream, std::string* err, int* d_err_out = nullptr);
+void launch_fresnel_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t stream);
+cudaError_t launch_tc_fresnel_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1,
+                                    bool accumulate, double2* d_field, const float* d_amax, int* d_err,
+                                    cudaStream_t stream);
+
 }  // namespace ophpc

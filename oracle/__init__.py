@@ -148,6 +148,11 @@ def _load_oracle():
                                              ctypes.POINTER(ctypes.c_uint8), ctypes.POINTER(ctypes.c_double),
                                              ctypes.POINTER(ctypes.c_double)]
             lib.oracle_normalize.restype = None
+            lib.oracle_wrp_zmax.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int64]
+            lib.oracle_wrp_zmax.restype = ctypes.c_double
+            lib.oracle_wrp_plane.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int64,
+                                             ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+            lib.oracle_wrp_plane.restype = ctypes.c_int
             _ora = lib
     return _ora
 
@@ -214,6 +219,132 @@ def normalize(encoded: np.ndarray):
     mn, mx = ctypes.c_double(), ctypes.c_double()
     lib.oracle_normalize(_p(e), nch, per, _p(out, ctypes.c_uint8), ctypes.byref(mn), ctypes.byref(mx))
     return out, mn.value, mx.value
+
+
+# ---------------------------------------------------------------- WRP
+
+class OracleWrpConfig(ctypes.Structure):
+    _fields_ = [
+        ("pixel_number", ctypes.c_int32 * 2),
+        ("pixel_pitch", ctypes.c_double * 2),
+        ("scale", ctypes.c_double * 3),
+        ("wrp_location", ctypes.c_double),
+        ("propagation_distance", ctypes.c_double),
+        ("n_channels", ctypes.c_int32),
+        ("wave_length", ctypes.c_double * 3),
+    ]
+
+
+@dataclass
+class WrpGeometry:
+    """ophWRP's configuration (ophgen/src/ophGen.h:643-660 + the SLM keys of
+    OphConfig): the <WRP> config file's fields the generator reads."""
+    pnx: int
+    pny: int
+    ppx: float
+    ppy: float
+    wavelengths: Sequence[float]
+    scale: Sequence[float] = (1.0, 1.0, 1.0)
+    wrp_location: float = 0.0
+    distance: float = 0.0
+
+    def to_c(self) -> OracleWrpConfig:
+        c = OracleWrpConfig()
+        c.pixel_number[0], c.pixel_number[1] = self.pnx, self.pny
+        c.pixel_pitch[0], c.pixel_pitch[1] = self.ppx, self.ppy
+        for i in range(3):
+            c.scale[i] = float(self.scale[i])
+        c.wrp_location = float(self.wrp_location)
+        c.propagation_distance = float(self.distance)
+        c.n_channels = len(self.wavelengths)
+        for i, w in enumerate(self.wavelengths):
+            c.wave_length[i] = float(w)
+        return c
+
+    def xml(self) -> str:
+        """The <WRP> config file ophWRP::readConfig parses
+        (ophgen/src/ophWRP.cpp:137-213 and ophGen::readConfig)."""
+        keys = [("FieldLength", 1.0), ("ScaleX", self.scale[0]), ("ScaleY", self.scale[1]),
+                ("ScaleZ", self.scale[2]), ("Distance", self.distance), ("LocationOfWRP", self.wrp_location),
+                ("NumOfWRP", 1), ("SLM_PixelPitchX", self.ppx), ("SLM_PixelPitchY", self.ppy),
+                ("SLM_PixelNumX", self.pnx), ("SLM_PixelNumY", self.pny), ("SLM_WaveNum", len(self.wavelengths))]
+        keys += [(f"SLM_WaveLength_{i + 1}", float(w)) for i, w in enumerate(self.wavelengths)]
+        return "<WRP>\n" + "".join(f"  <{k}>{v!r}</{k}>\n" for k, v in keys) + "</WRP>\n"
+
+
+def wrp_zmax(geom: WrpGeometry, vertices: np.ndarray) -> float:
+    lib = _load_oracle()
+    v = _vertices(vertices)
+    c = geom.to_c()
+    return float(lib.oracle_wrp_zmax(ctypes.byref(c), _p(v), v.shape[0]))
+
+
+def wrp_plane(geom: WrpGeometry, vertices: np.ndarray, channel: int) -> np.ndarray:
+    """One channel's WRP plane (calculateWRPCPU's splat, RandomPhase off),
+    complex128 [pnY, pnX] (oracle/ophpc_oracle_wrp.c)."""
+    lib = _load_oracle()
+    v = _vertices(vertices)
+    out = np.empty((geom.pny, geom.pnx, 2), dtype=np.float64)
+    c = geom.to_c()
+    if lib.oracle_wrp_plane(ctypes.byref(c), _p(v), v.shape[0], channel, _p(out)) != 0:
+        raise ValueError("oracle_wrp_plane rejected its arguments")
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def wrp_propagate(plane: np.ndarray, geom: WrpGeometry, wavelength: float) -> np.ndarray:
+    """Angular-spectrum propagation of a WRP plane by geom.distance, the
+    transform ophGen::Fresnel_FFT (ophgen/src/ophGen.cpp:516-580) intends:
+    the plane at the centre (pnY/2, pnX/2) of a zero (2 pnY) x (2 pnX)
+    buffer; F = fftshift(FFT2(fftshift(buffer))) (Openholo::fft2 with its
+    fftShift, Openholo/src/Openholo.cpp:698-774; fftShift equals numpy's
+    fftshift for even sizes); F *= exp(i 2 pi d sqrt(1/lambda^2 - fx^2 -
+    fy^2)) with fx = (j - pnX) / (2 ssX), fy = (i - pnY) / (2 ssY);
+    buffer = fftshift(IFFT2(fftshift(F))) unnormalised (FFTW's backward
+    transform: numpy's ifft2 times the size); the centre block is the
+    hologram. The reference runs the shifts in place on an aliased buffer,
+    which scrambles its result; this restatement computes what its code
+    describes, in FP64 (numpy.fft, pocketfft)."""
+    pny, pnx = plane.shape
+    hy, hx = pny >> 1, pnx >> 1
+    buf = np.zeros((2 * pny, 2 * pnx), dtype=np.complex128)
+    buf[hy:hy + pny, hx:hx + pnx] = plane
+    f = np.fft.fftshift(np.fft.fft2(np.fft.fftshift(buf)))
+    ssx, ssy = pnx * geom.ppx, pny * geom.ppy
+    fx = ((np.arange(2 * pnx) - pnx) / (2 * ssx)) ** 2
+    fy = ((np.arange(2 * pny) - pny) / (2 * ssy)) ** 2
+    sq = np.sqrt(1.0 / (wavelength * wavelength) - fx[None, :] - fy[:, None])
+    f *= np.exp(1j * (2 * np.pi * geom.distance) * sq)
+    out = np.fft.fftshift(np.fft.ifft2(np.fft.fftshift(f))) * (4 * pnx * pny)
+    return out[hy:hy + pny, hx:hx + pnx]
+
+
+def wrp_generate(geom: WrpGeometry, vertices: np.ndarray) -> np.ndarray:
+    """ophWRP::generateHologram restated: per channel the splat, then the
+    propagation; complex128 [n_channels, pnY, pnX]."""
+    return np.stack([wrp_propagate(wrp_plane(geom, vertices, c), geom, w) for c, w in enumerate(geom.wavelengths)])
+
+
+REF_WRP_LIB = os.path.join(HERE, "_ref", "libophref_wrp.so")
+
+
+def ref_wrp_available() -> bool:
+    return os.path.exists(REF_WRP_LIB)
+
+
+def ref_wrp_planes(xml_path: str, vertices: np.ndarray, n_channels: int, pnx: int, pny: int) -> np.ndarray:
+    """The reference's own WRP splat planes (oracle/ref_wrp_driver.cpp),
+    complex128 [n_channels, pnY, pnX]."""
+    lib = ctypes.CDLL(REF_WRP_LIB)
+    lib.ophref_wrp_planes.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_ulonglong, ctypes.c_void_p,
+                                      ctypes.c_int]
+    lib.ophref_wrp_planes.restype = ctypes.c_int
+    v = _vertices(vertices)
+    out = np.zeros((n_channels, pny, pnx, 2), dtype=np.float64)
+    with _QuietStdout():
+        rc = lib.ophref_wrp_planes(xml_path.encode(), v.ctypes.data, v.shape[0], out.ctypes.data, n_channels)
+    if rc != n_channels:
+        raise RuntimeError(f"ophref_wrp_planes failed ({rc})")
+    return out[..., 0] + 1j * out[..., 1]
 
 
 # ---------------------------------------------------------------- reference

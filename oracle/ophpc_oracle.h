@@ -66,6 +66,27 @@ int oracle_encode(const double* field, int64_t n, int32_t encode_flag, double* e
 void oracle_normalize(const double* encoded, int32_t n_channels, int64_t n_per_channel,
                       uint8_t* out, double* min_out, double* max_out);
 
+/* WRP generator (ophgen/src/ophWRP.cpp, ophWRPConfig ophgen/src/ophGen.h:643-660):
+ * the geometry and the two WRP depths the splat reads. */
+typedef struct oracle_wrp_config {
+    int32_t pixel_number[2];
+    double pixel_pitch[2];
+    double scale[3];
+    double wrp_location;          /* LocationOfWRP */
+    double propagation_distance;  /* Distance */
+    int32_t n_channels;
+    double wave_length[3];
+} oracle_wrp_config;
+
+/* autoScaling's zmax: the largest scaled z, starting from MIN_DOUBLE. */
+double oracle_wrp_zmax(const oracle_wrp_config* cfg, const double* vertices, int64_t n_points);
+
+/* One channel's WRP plane (calculateWRPCPU's splat, RandomPhase off):
+ * plane_out [pnY][pnX][re, im], zeroed first. Returns 0, or -1 on bad
+ * arguments. (oracle/ophpc_oracle_wrp.c) */
+int oracle_wrp_plane(const oracle_wrp_config* cfg, const double* vertices, int64_t n_points, int32_t channel,
+                     double* plane_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -279,6 +279,51 @@ def make_encoders(xml):
     return out
 
 
+WRP_CASES = {
+    # three colours, positive depth difference: w = 16 (32 x 32 splats)
+    "wrp_3ch": (oracle.WrpGeometry(pnx=96, pny=72, ppx=8e-6, ppy=8e-6, wavelengths=[638e-9, 532e-9, 473e-9],
+                                   scale=(1.0, 1.0, 1.0), wrp_location=2e-3, distance=0.05),
+                box(120, (3.5e-4, 2.6e-4), (-1e-3, 0.0), 201)),
+    # negative depth difference (the WRP in front of the points), odd size,
+    # points reaching past the plane's edges
+    "wrp_negdz_edges": (oracle.WrpGeometry(pnx=67, pny=45, ppx=6.4e-6, ppy=7.1e-6, wavelengths=[532e-9],
+                                           scale=(2.0, 2.0, 0.5), wrp_location=-1.5e-3, distance=0.02),
+                        box(80, (2.4e-4, 1.8e-4), (-1e-3, 1e-3), 202)),
+}
+
+
+def make_wrp(xml):
+    """The reference's own WRP splat planes (ophWRP::calculateWRPCPU,
+    ophgen/src/ophWRP.cpp:321-420; captured by oracle/ref_wrp_driver.cpp):
+    two small synthetic cases in full, and the reference's WRP example
+    (Example/dataset/Dice/WRP/Dice_WRP.xml with the Dice point cloud,
+    1920x1080) at 16,384 seeded pixels among those the splat reaches, with
+    the plane's count of nonzero pixels, sum and L2 norm."""
+    out = {}
+    for name, (g, v) in WRP_CASES.items():
+        with open(xml, "w") as f:
+            f.write(g.xml())
+        planes = oracle.ref_wrp_planes(xml, v, len(g.wavelengths), g.pnx, g.pny)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), vertices=v, planes=planes, xml=g.xml(),
+                            pnx=g.pnx, pny=g.pny, ppx=g.ppx, ppy=g.ppy, wavelengths=np.array(g.wavelengths),
+                            scale=np.array(g.scale), wrp_location=g.wrp_location, distance=g.distance)
+        out[name] = planes.shape
+    wrp_dir = os.path.join(os.path.dirname(DICE_DIR), "WRP")
+    dice_xml = open(os.path.join(wrp_dir, "Dice_WRP.xml")).read()
+    verts = oracle.ref_load_ply(os.path.join(wrp_dir, "dice_100000.ply"))
+    with open(xml, "w") as f:
+        f.write(dice_xml)
+    plane = oracle.ref_wrp_planes(xml, verts, 1, 1920, 1080)[0]
+    nz = np.flatnonzero(plane)
+    rng = np.random.default_rng(41)
+    idx = np.sort(rng.choice(nz, min(16384, nz.size), replace=False))
+    np.savez_compressed(os.path.join(HERE, "wrp_dice.npz"), vertices=verts, xml=dice_xml, pixel_index=idx,
+                        plane_at=plane.reshape(-1)[idx], nonzero=nz.size, plane_sum=plane.sum(),
+                        plane_norm=np.linalg.norm(plane))
+    out["wrp_dice"] = nz.size
+    return out
+
+
 def main():
     if not oracle.ref_available():
         oracle.build(with_reference=True)
@@ -359,15 +404,16 @@ def main():
         out.update(make_encoders(xml))
         out.update(make_ply_faces())
         out.update(make_dice(xml))
+        out.update(make_wrp(xml))
     for k, v in out.items():
         print(k, v)
 
 
 if __name__ == "__main__":
     only = {"ohc": make_ohc, "encoders": make_encoders, "ply_faces": lambda xml: make_ply_faces(),
-            "dice": make_dice}
+            "dice": make_dice, "wrp": make_wrp}
     if len(sys.argv) == 2 and sys.argv[1] in only:   # one group of fixtures
-        if not oracle.ref_available():
+        if not oracle.ref_available() or not oracle.ref_wrp_available():
             oracle.build(with_reference=True)
         with tempfile.TemporaryDirectory() as d:
             print(only[sys.argv[1]](os.path.join(d, "cfg.xml")))
