@@ -63,6 +63,7 @@ def parse():
                     help="run one fixed case for a profiler and exit: rs_1k, fresnel_1k, rs_fhd (sphere_fhd "
                          "RS generate), tc_fp16_4k, tc_bf16x3_4k (box_4k distribution, 131,072 points), "
                          "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points), tcrs_fhd_full (all 100,000), "
+                         "step_fhd (the headline step: tensor-core RS + phase codes), "
                          "tcf_fhd_full (tensor-core Fresnel, sphere_fhd), tcf_4k (tensor-core Fresnel, box_4k "
                          "geometry, 131,072 points)")
     ap.add_argument("--serving-max-points", type=int, default=500_000,
@@ -952,6 +953,8 @@ def profile_case(name: str) -> None:
         w, diff, mode = workloads.sphere_fhd().subset(20_000), 0, oph.MODE_TENSOR_BF16X3
     elif name == "tcrs_fhd_full":   # the headline step's tensor-core RS generate (~110 MB on the device)
         w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
+    elif name == "step_fhd":        # the headline step: tensor-core RS generate + phase codes, sphere_fhd
+        w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
     elif name == "tcf_fhd_full":    # tensor-core Fresnel (on-chip factors), sphere_fhd, all points
         w, diff, mode = workloads.sphere_fhd(), 1, oph.MODE_TENSOR_BF16X3
     elif name == "tcf_4k":          # tensor-core Fresnel (on-chip factors), box_4k geometry, 131,072 points
@@ -962,8 +965,12 @@ def profile_case(name: str) -> None:
     cfg = oph.make_config(**w.geometry_kwargs())
     dv = torch.from_numpy(w.vertices).cuda()
     f = torch.empty((w.n_channels, w.pny, w.pnx, 2), dtype=torch.float64, device="cuda")
+    codes = torch.empty((w.n_channels, w.pny * w.pnx), dtype=torch.uint8, device="cuda")
     for _ in range(2):
         ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        if name == "step_fhd":
+            ctx.encode(f.data_ptr(), w.n_channels, w.pny * w.pnx, oph.ENCODE_PHASE, None, codes.data_ptr(),
+                       torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     print(f"profile case {name}: done")
 

@@ -18,10 +18,16 @@
  *
  * Differences: nBlocks and nThreads are ignored (launch shapes are chosen
  * for sm_103a), `mode` selects nothing (one kernel per method, FP32 with an
- * FP64 phase reduction and FP64 output), k is taken as 2*pi/lambda, and the
- * config is read back with a synchronous copy before the launch. These
- * functions return nothing, as the reference's do; a failure is printed to
- * stderr and reported by ophpc_refabi_last_status() on the calling thread.
+ * FP64 phase reduction and FP64 output), and k is taken as 2*pi/lambda.
+ * The launch sizes and the scratch depend on the config, which lives in
+ * device memory, so each call first reads the 120-byte config back with a
+ * copy on the legacy stream: the call waits for the work queued on that
+ * stream before it (in the reference driver's sequence, only the config
+ * upload that its own blocking cudaMemcpy has just made,
+ * ophgen/src/ophPointCloud_GPU.cpp:249-258) and returns while its own
+ * kernels run. These functions return nothing, as the reference's do; a
+ * failure is printed to stderr and reported by ophpc_refabi_last_status()
+ * on the calling thread.
  */
 #ifndef OPHPC_REFABI_H
 #define OPHPC_REFABI_H

@@ -3,12 +3,13 @@
 // (ophgen/src/ophPointCloud_GPU.h:220-234, ophgen/src/ophPCKernel.cu:874-933),
 // running this library's kernels.
 //
-// Each call reads the device-resident config back (one synchronous 120-byte
-// copy, ordered after the caller's cudaMemcpy of it on the legacy stream),
-// turns it into a one-channel ophpc_config and queues prep + RS/Fresnel on
-// the legacy default stream with the amplitude taken from color[iColor] and
-// the result added into d_dst. One context per device is created on first
-// use and kept for the life of the process.
+// Each call reads the device-resident config back (one 120-byte copy on the
+// legacy stream, ordered after the caller's upload of it: the call waits for
+// the work queued on that stream before it, and no longer), turns it into a
+// one-channel ophpc_config and queues prep + RS/Fresnel on the legacy
+// default stream with the amplitude taken from color[iColor] and the result
+// added into d_dst; it returns while those kernels run. One context per
+// device is created on first use and kept for the life of the process.
 #include "ophpc_refabi.h"
 #include "pc_common.cuh"
 

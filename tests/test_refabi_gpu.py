@@ -147,3 +147,41 @@ def test_launchers_reject_bad_arguments(gpu_ctx):
     assert _launch(L, 1, d_v.data_ptr(), d_dst.data_ptr(), d_cfg.data_ptr(), 0) == 1
     torch.cuda.synchronize()
     assert not torch.any(d_dst)
+
+
+def test_launcher_returns_before_its_kernel_completes(gpu_ctx):
+    """The reference's launchers only enqueue (ophgen/src/ophPCKernel.cu:
+    893-933); so do these: with the config uploaded the way the reference's
+    driver uploads it (a blocking cudaMemcpy right before the call,
+    ophgen/src/ophPointCloud_GPU.cpp:249-251), the call returns while its
+    kernel is still running, and the field is complete after a synchronise."""
+    import time
+
+    import torch
+    L = _lib()
+    rng = np.random.default_rng(12)
+    n = 40_000
+    v = np.zeros((n, 7))
+    v[:, 0:2] = rng.uniform(-1e-3, 1e-3, (n, 2))
+    v[:, 2] = rng.uniform(0.4, 0.5, n)
+    v[:, 3:6] = 1.0 - rng.uniform(0.0, 1.0, (n, 3))
+    g = dict(pnx=2048, pny=2048, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9])
+    d_v = torch.from_numpy(v).cuda()
+    d_dst = torch.zeros((g["pnx"] * g["pny"], 2), dtype=torch.float64, device="cuda")
+    # warm-up: the first call on a device creates the launchers' context
+    d_cfg = torch.frombuffer(bytearray(bytes(_config(g, 1, 0, 0))), dtype=torch.uint8).cuda()
+    assert _launch(L, 0, d_v.data_ptr(), d_dst.data_ptr(), d_cfg.data_ptr(), 0) == 0
+    d_dst.zero_()
+    d_cfg = torch.frombuffer(bytearray(bytes(_config(g, n, 0, 0))), dtype=torch.uint8).cuda()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    assert _launch(L, 0, d_v.data_ptr(), d_dst.data_ptr(), d_cfg.data_ptr(), 0) == 0
+    t_call = time.perf_counter() - t0
+    pending = not torch.cuda.default_stream().query()   # the launcher's work is on the legacy stream
+    torch.cuda.synchronize()
+    t_total = time.perf_counter() - t0
+    assert pending, "the launcher waited for its own kernel"
+    assert t_call < 0.5 * t_total, (t_call, t_total)
+    h = d_dst.cpu().numpy()
+    mine = run_generate(gpu_ctx, g, v, 0)
+    assert rel_l2((h[:, 0] + 1j * h[:, 1]).reshape(1, g["pny"], g["pnx"]), mine) <= 1e-12
