@@ -426,9 +426,26 @@ __global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restric
     }
 }
 
+// The code of one pixel from its cached estimate e (NaN: none), in FP64
+// where the estimate is within its error margin of a code boundary: the
+// rule of est_codes_kernel, so the codes are the same bit for bit.
+template <int FLAG>
+__device__ __forceinline__ uint32_t code_of(float e, const double2* __restrict__ px, bool usable, float mn_f,
+                                            float sc_f, float margin, double gmn, double gap) {
+    const float v = (e - mn_f) * sc_f + 0.5f;
+    const float fl = floorf(v);
+    if (usable && e == e && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f)
+        return (uint32_t)(int)fl;
+    const double x = encode_value(*px, FLAG);
+    const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(x, gmn), gap), 255.0), 0.5);
+    return (val >= 0.0 && val < 256.0) ? (uint32_t)(int)val : 0u;
+}
+
 // Single pass of the codes, for fields whose FP32 estimates fit in the
 // shared memory of the CTAs the GPU holds at once (cooperative launch):
-// every CTA owns `per` consecutive pixels and
+// every CTA owns `per` consecutive pixels (a multiple of 32) and every
+// thread four consecutive ones at a time (four 16-byte loads in flight, one
+// 4-byte store of codes):
 //   1. reads them once, keeps their estimates in shared memory (NaN where
 //      there is none) and reduces its estimated min/max;
 //   2. computes in FP64 the pixels within the band of its own estimated
@@ -436,37 +453,47 @@ __global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restric
 //      the grid's exact extremes are found) and those without an estimate,
 //      and folds them into the exact words;
 //   3. waits at a grid barrier (all CTAs are resident; the wait is bounded by
-//      %globaltimer and records a timeout in word [4]);
-//   4. writes every code from its cached estimate, in FP64 where the
-//      estimate is within its error margin of a code boundary (as
-//      est_codes_kernel, so the codes are the same bit for bit).
+//      %globaltimer and records a timeout in word [4], after which the CTA
+//      writes zero codes);
+//   4. writes every code from its cached estimate (code_of).
 // The field is read once (plus the few FP64 pixels); words [3] and [4]
-// (barrier count, timeout) are zeroed by init_est_minmax_kernel.
+// (barrier count, timeout) are zeroed by init_est_minmax_kernel. `out` is
+// 4-byte aligned.
 template <int FLAG>
 __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restrict__ field, int64_t n, int64_t per,
                                                           unsigned long long* __restrict__ minmax,
                                                           uint8_t* __restrict__ out) {
-    extern __shared__ float s_est[];
+    extern __shared__ float4 s_est4[];
+    float* s_est = reinterpret_cast<float*>(s_est4);
     __shared__ float s_red[2][8];
     const int64_t base = (int64_t)blockIdx.x * per;
-    const int64_t cnt = base < n ? min(per, n - base) : 0;
+    const int cnt = base < n ? (int)min(per, n - base) : 0;
+    const double2* fb = field + base;
     const float qnan = __int_as_float(0x7fc00000);
     float mn = __int_as_float(0x7f800000), mx = -mn;
     double emn = kMaxDouble, emx = kMinDouble;
-    for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
-        const double2 h = field[base + j];
-        bool ok;
-        const float e = estimate<FLAG>(h, ok);
-        if (ok) {
-            s_est[j] = e;
-            mn = fminf(mn, e);
-            mx = fmaxf(mx, e);
-        } else {
-            s_est[j] = qnan;
-            const double x = encode_value(h, FLAG);
-            if (x < emn) emn = x;
-            if (x > emx) emx = x;
+    for (int j = 4 * threadIdx.x; j < cnt; j += 4 * blockDim.x) {
+        double2 h[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) h[k] = (j + k < cnt) ? fb[j + k] : make_double2(0.0, 0.0);
+        float e[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            bool ok;
+            e[k] = estimate<FLAG>(h[k], ok);
+            if (j + k >= cnt) {
+                e[k] = qnan;
+            } else if (ok) {
+                mn = fminf(mn, e[k]);
+                mx = fmaxf(mx, e[k]);
+            } else {
+                e[k] = qnan;
+                const double x = encode_value(h[k], FLAG);
+                if (x < emn) emn = x;
+                if (x > emx) emx = x;
+            }
         }
+        s_est4[j >> 2] = make_float4(e[0], e[1], e[2], e[3]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -483,12 +510,16 @@ __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restr
         mx = fmaxf(mx, s_red[1][k]);
     }
     const float band = est_band<FLAG>(mx);
-    for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
-        const float e = s_est[j];
-        if (e == e && (e <= mn + band || e >= mx - band)) {
-            const double x = encode_value(field[base + j], FLAG);
-            if (x < emn) emn = x;
-            if (x > emx) emx = x;
+    for (int j = 4 * threadIdx.x; j < cnt; j += 4 * blockDim.x) {
+        const float4 e4 = s_est4[j >> 2];
+        const float e[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (e[k] == e[k] && (e[k] <= mn + band || e[k] >= mx - band)) {
+                const double x = encode_value(fb[j + k], FLAG);
+                if (x < emn) emn = x;
+                if (x > emx) emx = x;
+            }
         }
     }
     fold_exact(emn, emx, minmax);
@@ -506,6 +537,7 @@ __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restr
                 atomicExch(&minmax[4], 1ull);
                 break;
             }
+            __nanosleep(128);
         }
         __threadfence();
         s_ok = ok;
@@ -518,21 +550,21 @@ __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restr
     const float mn_f = (float)gmn, sc_f = usable ? (float)(255.0 / gap) : 0.f;
     const float err = FLAG == 0 ? kPhaseErr : kAmpErrRel * (float)fmax(fabs(gmx), fabs(gmn));
     const float margin = 2.f * err * sc_f + 1e-4f;
-    for (int64_t j = threadIdx.x; j < cnt; j += blockDim.x) {
-        const float e = s_est[j];
-        uint8_t code = 0;
+    uint8_t* ob = out + base;
+    for (int j = 4 * threadIdx.x; j < cnt; j += 4 * blockDim.x) {
+        const float4 e4 = s_est4[j >> 2];
+        const float e[4] = {e4.x, e4.y, e4.z, e4.w};
+        uint32_t c[4] = {0u, 0u, 0u, 0u};
         if (s_ok) {
-            const float v = (e - mn_f) * sc_f + 0.5f;
-            const float fl = floorf(v);
-            if (usable && e == e && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f) {
-                code = (uint8_t)(int)fl;
-            } else {
-                const double x = encode_value(field[base + j], FLAG);
-                const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(x, gmn), gap), 255.0), 0.5);
-                code = (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
-            }
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (j + k < cnt) c[k] = code_of<FLAG>(e[k], fb + j + k, usable, mn_f, sc_f, margin, gmn, gap);
         }
-        out[base + j] = code;
+        if (j + 4 <= cnt) {
+            *reinterpret_cast<uint32_t*>(ob + j) = c[0] | c[1] << 8 | c[2] << 16 | c[3] << 24;
+        } else {
+            for (int k = 0; j + k < cnt; ++k) ob[j + k] = (uint8_t)c[k];
+        }
     }
 }
 
@@ -547,8 +579,8 @@ int grid_for(int64_t n, int threads) {
     return (int)(want < (int64_t)sms * 8 ? want : (int64_t)sms * 8);
 }
 // Cooperative single-pass codes when the grid of resident CTAs can cache
-// every estimate (4 bytes a pixel). False when it cannot (the three-pass
-// kernels run instead).
+// every estimate (4 bytes a pixel) and the codes buffer is 4-byte aligned.
+// False otherwise (the three-pass kernels run instead).
 bool launch_fused_codes(const double2* d_field, int64_t n, int flag, unsigned long long* d_minmax,
                         uint8_t* d_codes, cudaStream_t stream) {
     // not inside a stream capture (a plan): there the three-pass kernels run
@@ -557,6 +589,7 @@ bool launch_fused_codes(const double2* d_field, int64_t n, int flag, unsigned lo
         cudaGetLastError();
         return false;
     }
+    if (((uintptr_t)d_codes & 3u) != 0) return false;   // the kernel stores four codes at a time
     int dev = 0, sms = 0, coop = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return false;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);

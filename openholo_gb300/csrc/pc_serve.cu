@@ -247,7 +247,9 @@ void enqueue_step(ophpc_server* s, ServeJob* j, int prio_index) {
                 e = cudaMemcpyAsync(j->d_v, d.h_vertices, sizeof(ophpc_vertex) * n, cudaMemcpyHostToDevice, st);
             launch_prep(j->d_v, n, d.cfg.scale, d.cfg.distance, d.cfg.field_length, d.cfg.viewing_window,
                         (int)d.diff_flag, j->jg, j->d_recs, st);
-            if (j->tc) launch_rs_amax(j->d_recs, n, (int)d.cfg.n_channels, j->d_amax, st);
+            if (j->tc)
+                launch_rs_amax(j->d_recs, n, (int)d.cfg.n_channels, d.cfg.pixel_number[0], d.cfg.pixel_number[1],
+                               j->d_amax, st);
             if (j->tcft) launch_fresnel_amax(j->d_recs, n, (int)d.cfg.n_channels, j->d_amax, st);
             if (j->tcf)
                 for (uint32_t c = 0; c < d.cfg.n_channels; ++c)

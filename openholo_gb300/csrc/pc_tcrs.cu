@@ -38,9 +38,12 @@
 //               the sum per point) into a running sum S in the other 256
 //               TMEM columns, and every 16 drains into the FP64 field.
 //
-// Pairs for which the expansion does not hold (window cuts the tile, the cone
-// test is not passed by the whole tile, |w| or the cross phase too large:
-// rs_tc_eligible) get zero factors here and are added afterwards by the
+// A pair whose window rectangle cuts the tile keeps the tile-centre
+// expansion and gets 0/1 factor masks from the rectangle (the window is
+// separable); the stages holding such a pair run a masked instance of the
+// producer loop. Pairs for which the expansion does not hold (the cone test
+// is not passed by the tile's pixels inside the rectangle, |w| or the cross
+// phase too large: rs_tc_eligible) get zero factors here and are added afterwards by the
 // CUDA-core rs_kernel. The record warps mark them in a per-tile bitmask
 // (one ballot word per 32 points, each word written by one warp of one
 // CTA), which that kernel reads: it evaluates exactly the pairs left here
@@ -58,6 +61,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 namespace ophpc {
 namespace {
@@ -107,19 +111,27 @@ struct __align__(16) TcRsPair {
 };
 static_assert(sizeof(TcRsPair) == 64, "TcRsPair size");
 
+// stages, the record ring, 512 bytes of barriers and flags, and the window
+// words of the two record buffers (RS: one uint32 per point)
 template <bool FR>
 constexpr size_t smem_tc() {
-    return 1024 + (size_t)Lay<FR>::Stages * Lay<FR>::kStageBytes + sizeof(TcRsPair) * kChunkTc + 512;
+    return 1024 + (size_t)Lay<FR>::Stages * Lay<FR>::kStageBytes + sizeof(TcRsPair) * kChunkTc + 512 +
+           sizeof(uint32_t) * 2 * kChunkTc;
 }
 constexpr size_t kSmemTc = smem_tc<false>();
 constexpr size_t kSmemTcFr = smem_tc<true>();
 static_assert(kSmemTc <= 232448 && kSmemTcFr <= 232448, "shared memory per CTA");
 
+// Word of the per-job amplitude buffer (after the OPHPC_MAX_CHANNELS
+// per-channel bounds) that holds the RS window flag.
+constexpr int kWindowWord = 3;
+static_assert(OPHPC_MAX_CHANNELS <= kWindowWord, "window flag after the channel bounds");
+
 struct TcRsArgs {
     JobGeom jg;
     const PointRec* recs;   // [n_channels][n_points]
     double2* field;         // [n_channels][pnY][pnX], overwritten
-    const float* amax;      // [n_channels]: max coef / z^2
+    const float* amax;      // [n_channels]: max coef / z^2; word kWindowWord (RS): window flag (rs_amax_kernel)
     int32_t* left;          // [n_channels][tiles_y][tiles_x]: pairs left to the CUDA cores
     int* error;
     int32_t tiles_x, tiles_y;
@@ -172,13 +184,22 @@ __device__ __forceinline__ uint32_t h2v(f2::v2 v) {
     return h2(a, b);
 }
 
+// 1.0 where tile-relative index i lies in [lo, hi) held in bytes `sh` (lo)
+// and `sh + 8` (hi) of a window word (xlo, xhi, ylo, yhi), else 0.
+__device__ __forceinline__ float in_window_u(uint32_t w, int sh, int i) {
+    const int lo = (int)((w >> sh) & 0xffu), hi = (int)((w >> (sh + 8)) & 0xffu);
+    return (i >= lo && i < hi) ? 1.f : 0.f;
+}
+
 // Factors of 8 points of a stage (4 record pairs: one 16-byte chunk of a
 // row of every plane) for two rows (SIDE_A) or columns of this thread, at
 // offsets offa and offb, written at ro0 and ro1. A lane pair covers the two
 // chunks of a row, so that one st.shared.v4 of a warp fills 16 whole rows.
-// Two points at a time in packed FP32 pairs.
-template <bool SIDE_A>
-__device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, float offb, uint32_t ro0, uint32_t ro1) {
+// Two points at a time in packed FP32 pairs. CUT: the 8 points' window words
+// (wins) turn into 0/1 masks of the thread's rows (columns) ia and ib.
+template <bool SIDE_A, bool CUT>
+__device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, float offb, uint32_t ro0, uint32_t ro1,
+                                              const uint32_t* wins, int ia, int ib) {
     using f2::v2;
     const v2 offpa = f2::splat(offa), off2pa = f2::splat(offa * offa);
     const v2 offpb = f2::splat(offb), off2pb = f2::splat(offb * offb);
@@ -215,6 +236,12 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
         __sincosf(p1, &s1, &c1);
         v2 amp = f2::fma(w, w, f2::sub(one, w));
         if (SIDE_A) amp = f2::mul(amp, r3.x);
+        if (CUT) {
+            // zero outside the window rectangle: rows by (ylo, yhi), columns by (xlo, xhi)
+            const int idx = (qq & 1) ? ib : ia, sh = SIDE_A ? 16 : 0;
+            const uint2 wp = reinterpret_cast<const uint2*>(wins)[qq >> 1];   // the pair's two window words
+            amp = f2::mul(amp, f2::pack(in_window_u(wp.x, sh, idx), in_window_u(wp.y, sh, idx)));
+        }
         const v2 vr = f2::mul(amp, f2::pack(c0, c1)), vi = f2::mul(amp, f2::pack(s0, s1));
         w_hr[q] = bf2v(vr);
         w_hi[q] = bf2v(vi);
@@ -258,9 +285,7 @@ __device__ __forceinline__ void produce_stage(const TcRsPair* prs, float offa, f
 // 1.0 where tile-relative index i lies in the window [lo, hi) held in
 // bytes `sh` (lo) and `sh + 8` (hi) of the packed window word, else 0.
 __device__ __forceinline__ float in_window(float packed, int sh, int i) {
-    const uint32_t w = __float_as_uint(packed);
-    const int lo = (int)((w >> sh) & 0xffu), hi = (int)((w >> (sh + 8)) & 0xffu);
-    return (i >= lo && i < hi) ? 1.f : 0.f;
+    return in_window_u(__float_as_uint(packed), sh, i);
 }
 
 // Fresnel factors of 8 points of a stage for two rows (SIDE_A) or columns,
@@ -490,11 +515,15 @@ __device__ __forceinline__ bool drain_run(int p, int periods, uint64_t* acc_full
 // Per (point, tile) values of point idx into record pair slot t of buf
 // (zeros when the pair is not taken). True (and counted in left) for a pair
 // left to the CUDA cores: the window overlaps the tile, the expansion does
-// not hold.
+// not hold. For a pair taken while its window rectangle cuts the tile, cut
+// is set and win holds the rectangle relative to the tile (bytes xlo, xhi,
+// ylo, yhi; the whole tile otherwise).
 __device__ __forceinline__ bool make_record(TcRsPair* buf, int t, bool valid, const PointRec& p,
                                             const RsTcTile& tile, double inv_lambda, float inv_amax, int X0, int Y0,
-                                            int& left) {
+                                            int& left, bool& cut, uint32_t& win) {
     bool is_left = false;
+    cut = false;
+    win = (uint32_t)kRsTcTile << 8 | (uint32_t)kRsTcTile << 24;
     float h = 0.f, tau = 0.f, P = 0.f, bx = 0.f, Q = 0.f, fc = 0.f, ac = 0.f, k2 = 0.f;
     if (valid) {
         const int ix0 = max(X0, p.x_lo), ix1 = min(tile.vx1, p.x_hi);
@@ -521,6 +550,9 @@ __device__ __forceinline__ bool make_record(TcRsPair* buf, int t, bool valid, co
                 fc = (float)(tc - rint(tc));
                 ac = (float)p.coef * hf * inv_amax;
                 k2 = -1.5707963267948966f * tau * wxm * kCrossScale;
+                cut = !(ix0 == X0 && ix1 == tile.vx1 && iy0 == Y0 && iy1 == tile.vy1);
+                win = (uint32_t)(ix0 - X0) | ((uint32_t)(ix1 - X0) << 8) | ((uint32_t)(iy0 - Y0) << 16) |
+                      ((uint32_t)(iy1 - Y0) << 24);
             } else {
                 ++left;
                 is_left = true;
@@ -644,7 +676,10 @@ __device__ __noinline__ void sum_parts(const TcRsArgs& a, int ch, int tx, int X0
     }
 }
 
-template <bool FR>
+// FR: Fresnel, else RS. MASKS (RS): some point's window rectangle may cut a
+// tile, so the producers run the masked loop instance for the chunks that
+// hold such a pair; without it the kernel carries no mask code at all.
+template <bool FR, bool MASKS>
 __device__ __forceinline__ void tile_body(const TcRsArgs& a) {
     using L = Lay<FR>;
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -660,9 +695,13 @@ __device__ __forceinline__ void tile_body(const TcRsArgs& a) {
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(rec_empty + 2);
     volatile int* abort = reinterpret_cast<volatile int*>(tmem_slot + 1);
     int* s_left = reinterpret_cast<int*>(tmem_slot + 2);
-    // Fresnel: per record buffer, one word per stage: nonzero when a point
-    // of the stage has a window that cuts the tile
-    uint32_t* s_cut = tmem_slot + 4;   // [2][kStagesPerChunk]
+    // per record buffer, one word per stage: nonzero when a point of the
+    // stage has a window that cuts the tile (factor masks needed), at byte
+    // 256 of the 512-byte tail (16-byte aligned for uint4 reads; the
+    // barriers and words above end before byte 136)
+    uint32_t* s_cut = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(full) + 256);   // [2][16]
+    // RS: the window words of the points of the two record buffers
+    uint32_t* s_win = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(full) + 512);   // [2][kChunkTc]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = blockIdx.z, part = blockIdx.x % a.ksplit, tx = blockIdx.x / a.ksplit;
@@ -756,13 +795,23 @@ __device__ __forceinline__ void tile_body(const TcRsArgs& a) {
                         s_cut[b * kStagesPerChunk + (j >> 4) + 1] = bits >> 16;
                     }
                 } else {
+                    bool cut;
+                    uint32_t win;
                     const bool l = make_record(buf, j, valid, chrec[valid ? idx : 0], tile, g.inv_lambda, inv_amax,
-                                               X0, Y0, left);
+                                               X0, Y0, left, cut, win);
+                    if (MASKS) s_win[b * kChunkTc + j] = win;
                     // the warp's 32 consecutive points -> one word of the left-pair
                     // mask (this CTA alone writes it: pps is a multiple of kChunkTc)
+                    // and the cut flags of two whole stages
                     const uint32_t bits = __ballot_sync(0xffffffffu, l);
-                    if (lane == 0 && a.mask)
-                        a.mask[mask_base + (((int64_t)part * a.pps + idx) >> 5)] = bits;
+                    const uint32_t cbits = MASKS ? __ballot_sync(0xffffffffu, cut) : 0u;
+                    if (lane == 0) {
+                        if (a.mask) a.mask[mask_base + (((int64_t)part * a.pps + idx) >> 5)] = bits;
+                        if (MASKS) {
+                            s_cut[b * kStagesPerChunk + (j >> 4)] = cbits & 0xffffu;
+                            s_cut[b * kStagesPerChunk + (j >> 4) + 1] = cbits >> 16;
+                        }
+                    }
                 }
             }
             __syncwarp();
@@ -779,44 +828,73 @@ __device__ __forceinline__ void tile_body(const TcRsArgs& a) {
             if (dead) break;
             const TcRsPair* rb = s_rec + b * (kChunkTc / 2);
             const int it0 = c * kStagesPerChunk, it1 = min(total, it0 + kStagesPerChunk);
-            for (int it = it0; it < it1; ++it) {
-                const int s = it % L::Stages;
-                bool ok = true;
-                if (lane == 0) ok = mbar_wait_for(&empty[s], ((uint32_t)(it / L::Stages) & 1u) ^ 1u, abort, kWaitNs);
-                dead = !__shfl_sync(0xffffffffu, ok, 0);
-                if (dead) break;
-                const uint32_t sb = smem_u32(base + s * L::kStageBytes);
-                const TcRsPair* recs8 = rb + ((it - it0) * kStagePts) / 2 + 4 * kc;
-                if constexpr (FR) {
-                    // warp-uniform: every thread reads the same stage flag
-                    const bool cut = s_cut[b * kStagesPerChunk + (it - it0)] != 0;
-                    if (cut) {
-                        if (side_a) produce_stage_fr<true, true>(recs8, off, offb, rc, rc + 64, sb + row_off0,
-                                                                 sb + row_off1);
-                        else produce_stage_fr<false, true>(recs8, off, offb, rc, rc + 64, sb + row_off0,
-                                                           sb + row_off1);
-                    } else {
-                        if (side_a) produce_stage_fr<true, false>(recs8, off, offb, rc, rc + 64, sb + row_off0,
-                                                                  sb + row_off1);
-                        else produce_stage_fr<false, false>(recs8, off, offb, rc, rc + 64, sb + row_off0,
-                                                            sb + row_off1);
-                    }
-                } else {
-                    if (side_a) produce_stage<true>(recs8, off, offb, sb + row_off0, sb + row_off1);
-                    else produce_stage<false>(recs8, off, offb, sb + row_off0, sb + row_off1);
-                }
-                fence_async_smem();   // generic-proxy writes -> visible to the tensor core
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&full[s]);
-                // the previous run is drained (by every producer warp) once
-                // the first stage of the next one is filled: the MMA warp
-                // needs D free only to issue that stage
-                if ((it % kPeriod) == 0 && it > 0) {
-                    dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out, X0,
-                                      Y0, amax, wrote);
-                    ++drained;
+            // the chunk's per-stage cut flags, read once: bit k for stage it0 + k
+            uint32_t cutmask = 0;
+#pragma unroll
+            for (int q = 0; q < (FR || MASKS ? kStagesPerChunk / 4 : 0); ++q) {
+                const uint4 f = reinterpret_cast<const uint4*>(s_cut + b * kStagesPerChunk)[q];
+                cutmask |= (uint32_t)(f.x != 0) << (4 * q) | (uint32_t)(f.y != 0) << (4 * q + 1) |
+                           (uint32_t)(f.z != 0) << (4 * q + 2) | (uint32_t)(f.w != 0) << (4 * q + 3);
+            }
+            // The chunk's stages. RS runs a separate instance of the loop
+            // (masks true) for a chunk that holds a window-cut pair.
+            auto stages = [&](auto masks) {
+                constexpr bool kMasks = decltype(masks)::value;
+                for (int it = it0; it < it1; ++it) {
+                    const int s = it % L::Stages;
+                    bool ok = true;
+                    if (lane == 0)
+                        ok = mbar_wait_for(&empty[s], ((uint32_t)(it / L::Stages) & 1u) ^ 1u, abort, kWaitNs);
+                    dead = !__shfl_sync(0xffffffffu, ok, 0);
                     if (dead) break;
+                    const uint32_t sb = smem_u32(base + s * L::kStageBytes);
+                    const TcRsPair* recs8 = rb + ((it - it0) * kStagePts) / 2 + 4 * kc;
+                    const bool cut = (cutmask >> (it - it0)) & 1u;   // warp-uniform
+                    if constexpr (FR) {
+                        if (cut) {
+                            if (side_a) produce_stage_fr<true, true>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                                     sb + row_off1);
+                            else produce_stage_fr<false, true>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                               sb + row_off1);
+                        } else {
+                            if (side_a) produce_stage_fr<true, false>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                                      sb + row_off1);
+                            else produce_stage_fr<false, false>(recs8, off, offb, rc, rc + 64, sb + row_off0,
+                                                                sb + row_off1);
+                        }
+                    } else {
+                        const uint32_t* wins = s_win + b * kChunkTc + (it - it0) * kStagePts + 8 * kc;
+                        if (kMasks && cut) {
+                            if (side_a) produce_stage<true, kMasks>(recs8, off, offb, sb + row_off0, sb + row_off1,
+                                                                    wins, rc, rc + 64);
+                            else produce_stage<false, kMasks>(recs8, off, offb, sb + row_off0, sb + row_off1, wins,
+                                                              rc, rc + 64);
+                        } else {
+                            if (side_a) produce_stage<true, false>(recs8, off, offb, sb + row_off0, sb + row_off1,
+                                                                   wins, rc, rc + 64);
+                            else produce_stage<false, false>(recs8, off, offb, sb + row_off0, sb + row_off1, wins,
+                                                             rc, rc + 64);
+                        }
+                    }
+                    fence_async_smem();   // generic-proxy writes -> visible to the tensor core
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&full[s]);
+                    // the previous run is drained (by every producer warp) once
+                    // the first stage of the next one is filled: the MMA warp
+                    // needs D free only to issue that stage
+                    if ((it % kPeriod) == 0 && it > 0) {
+                        dead = !drain_run(drained, periods, acc_full, acc_empty, abort, tmem, warp, lane, a, ch, out,
+                                          X0, Y0, amax, wrote);
+                        ++drained;
+                        if (dead) break;
+                    }
                 }
+            };
+            if constexpr (!FR && MASKS) {
+                if (cutmask != 0) stages(std::true_type{});
+                else stages(std::false_type{});
+            } else {
+                stages(std::false_type{});
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&rec_empty[b]);   // this chunk's records are no longer read
@@ -837,27 +915,43 @@ __device__ __forceinline__ void tile_body(const TcRsArgs& a) {
     if (a.ksplit > 1) sum_parts(a, ch, tx, X0, Y0, s_left);
 }
 
+// The RS tile with factor masks, out of line: its register allocation
+// stays apart from that of the full-window tile body in tc_rs_kernel.
+__device__ __noinline__ void tile_body_rs_masked(const TcRsArgs& a) { tile_body<false, true>(a); }
+
+// RS: the masked tile body when some point's window rectangle leaves part of
+// the field out (the flag word written by rs_amax_kernel), else the
+// full-window one: no pair can then cut a tile.
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_rs_kernel(const __grid_constant__ TcRsArgs a) {
-    tile_body<false>(a);
+    if (reinterpret_cast<const int*>(a.amax)[kWindowWord] != 0) tile_body_rs_masked(a);
+    else tile_body<false, false>(a);
 }
 
 // Fresnel on the tensor cores, factors generated on chip: the same tile
 // pipeline with no cross pair and no CUDA-core complement.
 __global__ void __launch_bounds__(kThreadsTc, 1) tc_fresnel_kernel(const __grid_constant__ TcRsArgs a) {
-    tile_body<true>(a);
+    tile_body<true, false>(a);
 }
 
 // Largest coef / z^2 of a channel: bounds every coef / r_c^2, so the
 // factors stay within [-1, 1] (FP16 range for the cross pair).
 // (RS: coef / z^2; Fresnel, with per_z2 false: coef, the factor amplitude
-// before any window.)
-__global__ void rs_amax_kernel(const PointRec* __restrict__ recs, int64_t n, float* out, bool per_z2 = true) {
+// before any window.) With window_flag (RS), also sets *window_flag to 1
+// when a point's non-empty window rectangle does not cover the whole
+// pnX x pnY field (its window can then cut a tile).
+__global__ void rs_amax_kernel(const PointRec* __restrict__ recs, int64_t n, float* out, bool per_z2 = true,
+                               int* window_flag = nullptr, int pnX = 0, int pnY = 0) {
     float m = 0.f;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        m = fmaxf(m, fabsf((float)(per_z2 ? recs[i].coef / recs[i].aux : recs[i].coef)));
+    bool part = false;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const PointRec& p = recs[i];
+        m = fmaxf(m, fabsf((float)(per_z2 ? p.coef / p.aux : p.coef)));
+        part |= p.x_lo < p.x_hi && p.y_lo < p.y_hi && !(p.x_lo <= 0 && p.x_hi >= pnX && p.y_lo <= 0 && p.y_hi >= pnY);
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));   // m >= 0
+    if (window_flag && __any_sync(0xffffffffu, part) && (threadIdx.x & 31) == 0) atomicExch(window_flag, 1);
 }
 
 size_t align_up(size_t v, size_t al) { return (v + al - 1) / al * al; }
@@ -939,7 +1033,8 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
                 (int)OPHPC_DIFF_RS, jg, recs, s);
     for (int c = 0; c < nch; ++c) {
         count_launches(1);
-        rs_amax_kernel<<<256, 256, 0, s>>>(recs + (int64_t)c * n_points, (int64_t)n_points, amax + c);
+        rs_amax_kernel<<<256, 256, 0, s>>>(recs + (int64_t)c * n_points, (int64_t)n_points, amax + c, true,
+                                           reinterpret_cast<int*>(amax) + kWindowWord, pnX, pnY);
     }
     TcRsArgs ta;
     std::memset(&ta, 0, sizeof(ta));
@@ -994,10 +1089,12 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
     return OPHPC_SUCCESS;
 }
 
-void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t s) {
+void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, int pnX, int pnY, float* d_amax,
+                    cudaStream_t s) {
     for (int c = 0; c < n_channels; ++c) {
         count_launches(1);
-        rs_amax_kernel<<<256, 256, 0, s>>>(d_recs + (int64_t)c * n_points, n_points, d_amax + c);
+        rs_amax_kernel<<<256, 256, 0, s>>>(d_recs + (int64_t)c * n_points, n_points, d_amax + c, true,
+                                           reinterpret_cast<int*>(d_amax) + kWindowWord, pnX, pnY);
     }
 }
 

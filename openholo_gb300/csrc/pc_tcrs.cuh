@@ -29,7 +29,9 @@ constexpr float kRsTcMaxDropped = 2e-7f;     // turns
 // uses; both kernels form them with rs_tc_tile.
 struct RsTcTile {
     int32_t X0, Y0, vx1, vy1;     // origin and end of the valid pixels
-    double Xc, Yc;                // centre pixel (X0 + 64, Y0 + 64)
+    int32_t xc, yc;               // centre pixel indices (X0 + 64, Y0 + 64)
+    double Xc, Yc;                // centre pixel coordinates
+    double ppx, ppy;              // pixel pitches
     float umin, umax, vmin, vmax; // offsets of the valid pixels from the centre (u with the column, v against the row)
     float uext, vext;             // 64 pitches
     float detx, dety, inv_lambda;
@@ -42,6 +44,10 @@ __device__ __forceinline__ RsTcTile rs_tc_tile(const ChannelGeom& g, int X0, int
     t.vx1 = min(X0 + kRsTcTile, g.pnX);
     t.vy1 = min(Y0 + kRsTcTile, g.pnY);
     const int xc = X0 + kRsTcHalf, yc = Y0 + kRsTcHalf;
+    t.xc = xc;
+    t.yc = yc;
+    t.ppx = g.ppX;
+    t.ppy = g.ppY;
     t.Xc = pixel_x(g, xc);
     t.Yc = pixel_y(g, yc);
     t.umin = __double2float_rn(__dmul_rn((double)(X0 - xc), g.ppX));
@@ -73,22 +79,36 @@ __device__ __forceinline__ float rcp_hw(float x) {
 
 // Decides whether the tensor-core RS kernel evaluates point p on tile t.
 // True only when
-//  - the point's window rectangle holds every valid pixel of the tile,
-//  - every valid pixel of the tile passes the reference's cone test
-//    (ophgen/src/ophGen.cpp:415-428) with a relative margin of 1e-5,
+//  - the point's window rectangle meets the tile (the pixels outside the
+//    rectangle get zero factors: the rectangle is separable),
+//  - every valid pixel of the tile inside the rectangle passes the
+//    reference's cone test (ophgen/src/ophGen.cpp:415-428) with a relative
+//    margin of 1e-5 (near a window edge this fails only on the rectangle's
+//    first column, where the reference's pixel grid puts |X - x| at or
+//    beyond the half-width),
 //  - |w| = |r_p^2 - r_c^2| / r_c^2 <= kRsTcMaxW over the tile, the phase
 //    terms the factors drop stay under kRsTcMaxDropped turns and the cross
 //    phase under kRsTcMaxCross radians.
-// wxm / wym receive the bounds of |w_x|, |w_y| over the tile.
+// wxm / wym receive the bounds of |w_x|, |w_y| over the tile. A pair whose
+// rectangle holds the tile is decided on the tile's own bounds.
 __device__ __forceinline__ bool rs_tc_eligible(const PointRec& p, const RsTcTile& t, float* wxm_out,
                                                float* wym_out) {
-    if (!(p.x_lo <= t.X0 && p.x_hi >= t.vx1 && p.y_lo <= t.Y0 && p.y_hi >= t.vy1)) return false;
+    const int ix0 = max(t.X0, p.x_lo), ix1 = min(t.vx1, p.x_hi);
+    const int iy0 = max(t.Y0, p.y_lo), iy1 = min(t.vy1, p.y_hi);
+    if (!(ix0 < ix1 && iy0 < iy1)) return false;
+    float umin = t.umin, umax = t.umax, vmin = t.vmin, vmax = t.vmax;
+    if (!(ix0 == t.X0 && ix1 == t.vx1 && iy0 == t.Y0 && iy1 == t.vy1)) {
+        umin = __double2float_rn(__dmul_rn((double)(ix0 - t.xc), t.ppx));
+        umax = __double2float_rn(__dmul_rn((double)(ix1 - 1 - t.xc), t.ppx));
+        vmax = __double2float_rn(__dmul_rn((double)(t.yc - iy0), t.ppy));
+        vmin = __double2float_rn(__dmul_rn((double)(t.yc - (iy1 - 1)), t.ppy));
+    }
     const float dxf = __double2float_rn(__dsub_rn(t.Xc, p.x));
     const float dyf = __double2float_rn(__dsub_rn(t.Yc, p.y));
     const float zzf = __double2float_rn(p.aux);
-    // cone test over the tile, conservative
-    const float xa = __fadd_rn(dxf, t.umin), xb = __fadd_rn(dxf, t.umax);
-    const float ya = __fadd_rn(dyf, t.vmin), yb = __fadd_rn(dyf, t.vmax);
+    // cone test over the tile's pixels inside the rectangle, conservative
+    const float xa = __fadd_rn(dxf, umin), xb = __fadd_rn(dxf, umax);
+    const float ya = __fadd_rn(dyf, vmin), yb = __fadd_rn(dyf, vmax);
     const float slack = __fmul_rn(1e-6f, __fadd_rn(__fadd_rn(fabsf(dxf), fabsf(dyf)), __fadd_rn(t.uext, t.vext)));
     const float maxdx = __fadd_rn(fmaxf(fabsf(xa), fabsf(xb)), slack);
     const float maxdy = __fadd_rn(fmaxf(fabsf(ya), fabsf(yb)), slack);
@@ -132,7 +152,9 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
 
 // Building blocks for callers that run a job as point-range steps (the
 // serving engine). launch_rs_amax: per channel the largest coef / z^2 of the
-// RS records into d_amax[0..n_channels) (zeroed by the caller).
+// RS records into d_amax[0..n_channels), and into word 3 a flag set when
+// some point's window rectangle leaves part of the pnX x pnY field out
+// (d_amax holds 4 words, zeroed by the caller).
 // launch_tc_rs_range: points [p0, p1) of the records on the tensor cores,
 // overwriting the field (accumulate false) or adding into it, then the
 // CUDA-core complement for the same range; d_left holds n_channels x tiles
@@ -140,7 +162,8 @@ ophpc_status tc_generate_rs(cudaMemPool_t pool, const JobGeom& jg, const ophpc_c
 // mask_words words, mask_words >= tc_rs_mask_words(p1 - p0), through which
 // the complement finds the pairs left to it; *d_err is set on a kernel
 // timeout.
-void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, float* d_amax, cudaStream_t stream);
+void launch_rs_amax(const PointRec* d_recs, int64_t n_points, int n_channels, int pnX, int pnY, float* d_amax,
+                    cudaStream_t stream);
 inline int64_t tc_rs_mask_words(int64_t n_points) { return (n_points + 255) / 256 * 8; }
 cudaError_t launch_tc_rs_range(const JobGeom& jg, const PointRec* d_recs, int64_t p0, int64_t p1, bool accumulate,
                                double2* d_field, const float* d_amax, int32_t* d_left, uint32_t* d_mask,

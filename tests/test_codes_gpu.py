@@ -41,6 +41,9 @@ def _fields():
     c = np.zeros((1, 64, 64, 2))
     c[..., 0] = 1.0
     out["constant"] = c
+    # a pixel count that is no multiple of 4: the single-pass kernel's last
+    # group of four pixels is partial
+    out["odd_size"] = rng.normal(size=(1, 123, 457, 2))
     return out
 
 
@@ -71,3 +74,20 @@ def test_codes_of_a_generated_hologram(gpu_ctx):
     field = f.cpu().numpy()
     for flag in (0, 1):
         assert np.array_equal(_codes(gpu_ctx, field, flag, False), _codes(gpu_ctx, field, flag, True)), flag
+
+
+def test_codes_into_unaligned_buffer(gpu_ctx):
+    """A codes buffer that is not 4-byte aligned takes the three-pass
+    kernels (the single-pass kernel stores four codes at a time): same
+    codes."""
+    import torch
+    field = _fields()["gaussian_3ch"]
+    want = _codes(gpu_ctx, field, 0, True)
+    f = torch.from_numpy(np.ascontiguousarray(field)).cuda()
+    nch, npx = field.shape[0], field.shape[1] * field.shape[2]
+    raw = torch.zeros(nch * npx + 16, dtype=torch.uint8, device="cuda")
+    for off in (1, 2, 3):
+        gpu_ctx.encode(f.data_ptr(), nch, npx, 0, None, raw.data_ptr() + off)
+        torch.cuda.synchronize()
+        got = raw[off:off + nch * npx].cpu().numpy().reshape(nch, npx)
+        assert np.array_equal(got, want), off

@@ -46,6 +46,11 @@ CASES = {
                        _box(900, (1e-3, 1e-3), (0.05, 0.2), 43)),
     "fine_pitch": (dict(pnx=512, pny=256, ppx=3.74e-6, ppy=3.74e-6, wavelengths=[532e-9]),
                    _box(2000, (3e-3, 3e-3), (0.29, 0.31), 44)),
+    # windows of 830-1250 pixels on a 1536x1024 field: most pairs hold the
+    # tile, many cut it (masked factors on the tensor cores) and a few fail
+    # the cone test at the window edge (CUDA-core complement)
+    "window_cut_tensor": (dict(pnx=1536, pny=1024, ppx=8e-6, ppy=8e-6, wavelengths=[532e-9]),
+                          _box(800, (4e-3, 3e-3), (0.1, 0.15), 49)),
 }
 
 
