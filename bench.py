@@ -53,7 +53,7 @@ WORKLOAD = "sphere_fhd"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=WORKLOAD)
@@ -65,7 +65,8 @@ def parse():
                          "tcrs_fhd (tensor-core RS, sphere_fhd, 20,000 points), tcrs_fhd_full (all 100,000), "
                          "step_fhd (the headline step: tensor-core RS + phase codes), "
                          "tcf_fhd_full (tensor-core Fresnel, sphere_fhd), tcf_4k (tensor-core Fresnel, box_4k "
-                         "geometry, 131,072 points)")
+                         "geometry, 131,072 points), codes_fhd (the headline step's generate, then the phase "
+                         "codes twice)")
     ap.add_argument("--serving-max-points", type=int, default=500_000,
                     help="largest point count of a serving job")
     return ap.parse_args()
@@ -131,7 +132,7 @@ class ClockSampler:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -953,7 +954,7 @@ def profile_case(name: str) -> None:
         w, diff, mode = workloads.sphere_fhd().subset(20_000), 0, oph.MODE_TENSOR_BF16X3
     elif name == "tcrs_fhd_full":   # the headline step's tensor-core RS generate (~110 MB on the device)
         w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
-    elif name == "step_fhd":        # the headline step: tensor-core RS generate + phase codes, sphere_fhd
+    elif name in ("step_fhd", "codes_fhd"):   # tensor-core RS generate + phase codes, sphere_fhd
         w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
     elif name == "tcf_fhd_full":    # tensor-core Fresnel (on-chip factors), sphere_fhd, all points
         w, diff, mode = workloads.sphere_fhd(), 1, oph.MODE_TENSOR_BF16X3
@@ -966,9 +967,11 @@ def profile_case(name: str) -> None:
     dv = torch.from_numpy(w.vertices).cuda()
     f = torch.empty((w.n_channels, w.pny, w.pnx, 2), dtype=torch.float64, device="cuda")
     codes = torch.empty((w.n_channels, w.pny * w.pnx), dtype=torch.uint8, device="cuda")
-    for _ in range(2):
-        ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
-        if name == "step_fhd":
+    for it in range(2):
+        if name != "codes_fhd" or it == 0:
+            ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(),
+                         torch.cuda.current_stream().cuda_stream)
+        if name in ("step_fhd", "codes_fhd"):
             ctx.encode(f.data_ptr(), w.n_channels, w.pny * w.pnx, oph.ENCODE_PHASE, None, codes.data_ptr(),
                        torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
