@@ -26,9 +26,11 @@
  *     exiting the process;
  *   - encoding() supports ENCODE_PHASE, ENCODE_AMPLITUDE, ENCODE_REAL,
  *     ENCODE_IMAGINARY, ENCODE_SIMPLENI, ENCODE_BURCKHARDT and
- *     ENCODE_TWOPHASE on the GPU; the FFT-based SSB / off-axis and the
- *     binary encoders log and do nothing, as an unknown flag does in the
- *     reference.
+ *     ENCODE_TWOPHASE on the GPU, and encoding(flag, passband) ENCODE_SSB
+ *     and ENCODE_OFFSSB (FP64 FFTs on the GPU, computing what the
+ *     reference's code describes: its own FFTW buffers alias the arrays it
+ *     shifts); the binary encoders log and do nothing, as an unknown flag
+ *     does in the reference.
  */
 #ifndef OPHPC_OPHPOINTCLOUD_H
 #define OPHPC_OPHPOINTCLOUD_H
@@ -72,8 +74,17 @@ public:
     T mag() const { return std::sqrt(mag2()); }
     T angle() const { return std::atan2(this->imag(), this->real()); }
 };
+/* vec2 of Openholo/src/ivec.h, as far as the SSB encoder's arguments use
+ * it: two Reals indexable with _X, _Y. */
+struct vec2 {
+    Real v[2];
+    vec2(Real a = 0, Real b = 0) : v{a, b} {}
+    Real& operator[](int i) { return v[i]; }
+    const Real& operator[](int i) const { return v[i]; }
+};
 }  // namespace oph
 using oph::Complex;
+using oph::vec2;
 
 /* Vertex (Openholo/src/struct.h:86-106), layout-identical to ophpc_vertex. */
 #pragma pack(push, 1)
@@ -100,6 +111,7 @@ struct OphConfig {
 class ophPointCloud {
 public:
     enum PC_DIFF_FLAG : int8_t { PC_DIFF_RS = 0x00, PC_DIFF_FRESNEL = 0x01 };
+    enum SSB_PASSBAND { SSB_LEFT, SSB_RIGHT, SSB_TOP, SSB_BOTTOM };
     enum ENCODE_FLAG {
         ENCODE_PHASE, ENCODE_AMPLITUDE, ENCODE_REAL, ENCODE_IMAGINARY, ENCODE_SIMPLENI, ENCODE_BURCKHARDT,
         ENCODE_TWOPHASE, ENCODE_SSB, ENCODE_OFFSSB, ENCODE_SIMPLEBINARY, ENCODE_EDBINARY
@@ -139,6 +151,14 @@ public:
     /* Returns the elapsed seconds, 0.0 on a bad flag or a failure. */
     Real generateHologram(uint diff_flag = PC_DIFF_RS);
     void encoding(unsigned int ENCODE_FLAG);
+    /* ophPointCloud::encoding(flag, passband) (ophPointCloud.cpp:247-251):
+     * ENCODE_SSB runs encodeHologram(), ENCODE_OFFSSB the off-axis
+     * single-sideband encoding of channel 0's field into every channel;
+     * other flags do nothing. */
+    void encoding(unsigned int ENCODE_FLAG, unsigned int SSB_PASSBAND);
+    /* ophPointCloud::encodeHologram (ophPointCloud.cpp:191-240); band_limit
+     * is not used, as in the reference. */
+    void encodeHologram(const vec2 band_limit = vec2(0.8, 0.5), const vec2 spectrum_shift = vec2(0.0, 0.5));
     void normalize(void);
     bool save(const char* fname, uint8_t bitsperpixel = 8, uchar* src = nullptr, uint px = 0, uint py = 0);
     /* Openholo::saveAsOhc / loadAsOhc (Openholo/src/Openholo.cpp:252-319):
@@ -167,6 +187,7 @@ private:
     void freeBuffers();
     bool ensureGpu();
     bool ensureDevice(size_t bytes_vertices, size_t bytes_field, size_t bytes_encoded, size_t bytes_codes);
+    void encodeSideband(unsigned int flag, unsigned int passband, Real shift_x, Real shift_y);
 
     OphConfig context_;
     Real wave_length_[OPHPC_MAX_CHANNELS] = {0, 0, 0};

@@ -76,6 +76,15 @@ typedef enum ophpc_status {
 #define OPHPC_ENCODE_SIMPLENI 4u
 #define OPHPC_ENCODE_BURCKHARDT 5u
 #define OPHPC_ENCODE_TWOPHASE 6u
+#define OPHPC_ENCODE_SSB 7u
+#define OPHPC_ENCODE_OFFSSB 8u
+
+/* ophGen::SSB_PASSBAND (ophgen/src/ophGen.h:295): the half of the spectrum
+ * ENCODE_OFFSSB keeps. */
+#define OPHPC_SSB_LEFT 0u
+#define OPHPC_SSB_RIGHT 1u
+#define OPHPC_SSB_TOP 2u
+#define OPHPC_SSB_BOTTOM 3u
 
 /* Vertex (Openholo/src/struct.h:86-106): packed pos[3], color[3], phase —
  * 56 bytes, colour channels in [0, 1]; color[ch] is channel ch's amplitude. */
@@ -157,11 +166,37 @@ ophpc_status ophpc_generate_host(ophpc_context* ctx, const ophpc_config* cfg,
  * sampled magnitude. BURCKHARDT writes two of every three entries and
  * TWOPHASE the first 2*(n_pixels/2): the others keep what d_encoded held
  * (as m_lpEncoded keeps an earlier encoding in the reference), or count as
- * 0 when d_encoded is NULL. Other flags (SSB, off-axis, binary) are
- * OPHPC_ERROR_UNSUPPORTED. Asynchronous on `stream`. */
+ * 0 when d_encoded is NULL. SSB and off-axis SSB need the 2-D size:
+ * ophpc_encode_ssb; the binary encoders are OPHPC_ERROR_UNSUPPORTED.
+ * Asynchronous on `stream`. */
 ophpc_status ophpc_encode(ophpc_context* ctx, const double* d_field, uint32_t n_channels,
                           uint64_t n_pixels, uint32_t encode_flag, double* d_encoded,
                           uint8_t* d_normalized, void* stream);
+
+/* ophPointCloud::encoding(ENCODE_SSB | ENCODE_OFFSSB, passband)
+ * (ophgen/src/ophPointCloud.cpp:247-251) on device, FP64, on the field
+ * d_field [n_channels][pny][pnx][re, im]:
+ *   OPHPC_ENCODE_SSB: ophPointCloud::encodeHologram
+ *     (ophPointCloud.cpp:191-240) per channel: the field through the
+ *     reference's shifted forward and backward FFTs (unnormalised), its real
+ *     part times cos(pi x shift_x / ppx + pi y shift_y / ppy) at the pixel
+ *     coordinates the reference uses; shift_x, shift_y are its
+ *     spectrum_shift (default 0.0, 0.5); passband is not used (nor is it
+ *     there);
+ *   OPHPC_ENCODE_OFFSSB: ophGen::encoding(ENCODE_OFFSSB, passband)
+ *     (ophgen/src/ophGen.cpp:882-921): freqShift(0, 100) then
+ *     singleSideBand(passband) of channel 0's field, normalised to [0, 1],
+ *     written to every channel (the reference reads complex_H[0] for each).
+ * d_encoded (optional) receives m_lpEncoded, d_normalized (optional) the
+ * 8-bit codes of ophGen::normalize over all channels. pnx, pny up to 16384,
+ * each factoring into 2, 3, 5 and 7 (OPHPC_ERROR_UNSUPPORTED otherwise).
+ * This is what the reference's code describes; its own runs alias the FFT
+ * input with the array being shifted and are not reproducible. Allocates
+ * scratch from the context's pool; asynchronous on `stream`. */
+ophpc_status ophpc_encode_ssb(ophpc_context* ctx, const double* d_field, uint32_t n_channels, int32_t pnx,
+                              int32_t pny, double ppx, double ppy, uint32_t encode_flag, uint32_t passband,
+                              double shift_x, double shift_y, double* d_encoded, uint8_t* d_normalized,
+                              void* stream);
 
 /* Largest n_points * n_channels that ophpc_generate_static_scratch accepts:
  * its scratch is a fixed 32 MiB device array of 64-byte point records. */

@@ -14,6 +14,7 @@
  *   ophpc_pc_set_offset               Openholo::setOffset (Openholo.h:281)
  *   ophpc_pc_generate_hologram        generateHologram  (ophPointCloud.cpp:151-191)
  *   ophpc_pc_encoding                 encoding          (ophPointCloud.cpp:242-245)
+ *   ophpc_pc_encoding_passband        encoding(flag, passband) (ophPointCloud.cpp:247-251)
  *   ophpc_pc_normalize                normalize         (ophGen.cpp:654-687)
  *   ophpc_pc_save                     save              (ophGen.cpp:689-769)
  *   ophpc_pc_save_ohc / _load_ohc     Openholo::saveAsOhc / loadAsOhc (Openholo.cpp:252-319)
@@ -46,6 +47,9 @@ void ophpc_pc_set_distance(ophpc_pc* h, double distance);
 void ophpc_pc_set_offset(ophpc_pc* h, int32_t ox, int32_t oy);
 double ophpc_pc_generate_hologram(ophpc_pc* h, uint32_t diff_flag);
 void ophpc_pc_encoding(ophpc_pc* h, uint32_t encode_flag);
+/* encoding(flag, passband) (ophPointCloud.cpp:247-251): OPHPC_ENCODE_SSB,
+ * OPHPC_ENCODE_OFFSSB with an OPHPC_SSB_* passband. */
+void ophpc_pc_encoding_passband(ophpc_pc* h, uint32_t encode_flag, uint32_t passband);
 void ophpc_pc_normalize(ophpc_pc* h);
 int32_t ophpc_pc_save(ophpc_pc* h, const char* path, uint8_t bits_per_pixel);
 int32_t ophpc_pc_save_ohc(ophpc_pc* h, const char* path);

@@ -14,7 +14,7 @@ from typing import Optional, Sequence
 
 from ._abi import (  # noqa: F401
     DIFF_FRESNEL, DIFF_RS, ENCODE_AMPLITUDE, ENCODE_BURCKHARDT, ENCODE_IMAGINARY, ENCODE_PHASE, ENCODE_REAL,
-    ENCODE_SIMPLENI, ENCODE_TWOPHASE, MODE_CPU,
+    ENCODE_OFFSSB, ENCODE_SIMPLENI, ENCODE_SSB, ENCODE_TWOPHASE, MODE_CPU, SSB_BOTTOM, SSB_LEFT, SSB_RIGHT, SSB_TOP,
     MODE_DOUBLE, MODE_FASTMATH, MODE_FLOAT, MODE_GPU, MODE_TENSOR_BF16X3, MODE_TENSOR_FP16, OphpcConfig,
     OphpcError, OphpcWrpConfig, STATUS, lib, lib_path, make_config, make_wrp_config,
 )
@@ -23,7 +23,8 @@ __all__ = [
     "Context", "OphpcConfig", "OphpcError", "make_config", "lib", "lib_path", "OphpcWrpConfig", "make_wrp_config",
     "DIFF_RS", "DIFF_FRESNEL", "MODE_CPU", "MODE_GPU", "MODE_DOUBLE", "MODE_FLOAT", "MODE_FASTMATH",
     "MODE_TENSOR_FP16", "MODE_TENSOR_BF16X3", "ENCODE_PHASE", "ENCODE_AMPLITUDE", "ENCODE_REAL",
-    "ENCODE_IMAGINARY", "ENCODE_SIMPLENI", "ENCODE_BURCKHARDT", "ENCODE_TWOPHASE", "Plan", "PLAN_NO_ENCODE",
+    "ENCODE_IMAGINARY", "ENCODE_SIMPLENI", "ENCODE_BURCKHARDT", "ENCODE_TWOPHASE", "ENCODE_SSB", "ENCODE_OFFSSB",
+    "SSB_LEFT", "SSB_RIGHT", "SSB_TOP", "SSB_BOTTOM", "Plan", "PLAN_NO_ENCODE",
 ]
 
 PLAN_NO_ENCODE = 0xFFFFFFFF
@@ -110,6 +111,16 @@ class Context:
         st = self._lib.ophpc_fresnel_fft(self._h, pnx, pny, ppx, ppy, wavelength, distance, ctypes.c_void_p(d_src),
                                          ctypes.c_void_p(d_dst), ctypes.c_void_p(stream))
         self._check(st, "ophpc_fresnel_fft")
+
+    def encode_ssb(self, d_field: int, n_channels: int, pnx: int, pny: int, ppx: float, ppy: float,
+                   encode_flag: int, passband: int = SSB_LEFT, spectrum_shift=(0.0, 0.5),
+                   d_encoded: Optional[int] = None, d_normalized: Optional[int] = None, stream: int = 0) -> None:
+        """ophPointCloud::encoding(ENCODE_SSB | ENCODE_OFFSSB, passband) (ophpc_encode_ssb)."""
+        st = self._lib.ophpc_encode_ssb(self._h, ctypes.c_void_p(d_field), n_channels, pnx, pny, ppx, ppy,
+                                        encode_flag, passband, float(spectrum_shift[0]), float(spectrum_shift[1]),
+                                        ctypes.c_void_p(d_encoded or 0), ctypes.c_void_p(d_normalized or 0),
+                                        ctypes.c_void_p(stream))
+        self._check(st, "ophpc_encode_ssb")
 
     def encode(self, d_field: int, n_channels: int, n_pixels: int, encode_flag: int,
                d_encoded: Optional[int], d_normalized: Optional[int], stream: int = 0) -> None:

@@ -24,6 +24,9 @@ ENCODE_IMAGINARY = 3
 ENCODE_SIMPLENI = 4
 ENCODE_BURCKHARDT = 5
 ENCODE_TWOPHASE = 6
+ENCODE_SSB = 7
+ENCODE_OFFSSB = 8
+SSB_LEFT, SSB_RIGHT, SSB_TOP, SSB_BOTTOM = 0, 1, 2, 3
 
 STATUS = {
     0: "success", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "I/O error",
@@ -147,6 +150,8 @@ def _declare(L: ctypes.CDLL) -> None:
     d = ctypes.c_double
     L.ophpc_fresnel_fft.argtypes = [vp, i32, i32, d, d, d, d, vp, vp, vp]
     L.ophpc_fresnel_fft.restype = ctypes.c_int
+    L.ophpc_encode_ssb.argtypes = [vp, vp, u32, i32, i32, d, d, u32, u32, d, d, vp, vp, vp]
+    L.ophpc_encode_ssb.restype = ctypes.c_int
 
 
 def lib() -> ctypes.CDLL:

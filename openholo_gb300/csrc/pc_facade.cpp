@@ -342,6 +342,42 @@ void ophPointCloud::encoding(unsigned int flag) {
     encoded_valid_ = true;
 }
 
+void ophPointCloud::encodeSideband(unsigned int flag, unsigned int passband, Real shift_x, Real shift_y) {
+    if (!complex_H_ || !ensureGpu()) return;
+    const size_t plane = (size_t)buffer_pixels_;
+    const uint nch = context_.waveNum;
+    if (!ensureDevice(cap_v_ ? cap_v_ : 1, sizeof(double) * 2 * plane * nch, sizeof(double) * plane * nch, plane * nch))
+        return;
+    context_.ss[_X] = context_.pixel_number[_X] * context_.pixel_pitch[_X];
+    context_.ss[_Y] = context_.pixel_number[_Y] * context_.pixel_pitch[_Y];
+    for (uint ch = 0; ch < nch; ++ch)
+        cudaMemcpy((double*)d_field_ + 2 * plane * ch, complex_H_[ch], sizeof(double) * 2 * plane, cudaMemcpyHostToDevice);
+    if (ophpc_encode_ssb(gpu_, (const double*)d_field_, nch, context_.pixel_number[_X], context_.pixel_number[_Y],
+                         context_.pixel_pitch[_X], context_.pixel_pitch[_Y], flag, passband, shift_x, shift_y,
+                         (double*)d_encoded_, nullptr, nullptr) != OPHPC_SUCCESS) {
+        last_error_ = std::string("encode: ") + ophpc_last_error(gpu_);
+        OPH_LOG("<FAILED> %s\n", last_error_.c_str());
+        return;
+    }
+    for (uint ch = 0; ch < nch; ++ch)
+        cudaMemcpy(encoded_[ch], (double*)d_encoded_ + plane * ch, sizeof(double) * plane, cudaMemcpyDeviceToHost);
+    encoded_valid_ = true;
+}
+
+void ophPointCloud::encoding(unsigned int flag, unsigned int passband) {
+    if (flag == ENCODE_SSB) encodeHologram();
+    else if (flag == ENCODE_OFFSSB) encodeSideband(OPHPC_ENCODE_OFFSSB, passband, 0.0, 0.0);
+}
+
+void ophPointCloud::encodeHologram(const vec2 band_limit, const vec2 spectrum_shift) {
+    (void)band_limit;
+    if (!complex_H_) {
+        OPH_LOG("<FAILED> Not found diffracted data.");
+        return;
+    }
+    encodeSideband(OPHPC_ENCODE_SSB, 0, spectrum_shift[_X], spectrum_shift[_Y]);
+}
+
 void ophPointCloud::normalize(void) {
     if (!encoded_ || !ensureGpu()) return;
     const size_t plane = (size_t)buffer_pixels_;
@@ -495,6 +531,9 @@ double ophpc_pc_generate_hologram(ophpc_pc* h, uint32_t diff_flag) {
 }
 
 void ophpc_pc_encoding(ophpc_pc* h, uint32_t flag) { if (h) h->obj->encoding(flag); }
+void ophpc_pc_encoding_passband(ophpc_pc* h, uint32_t flag, uint32_t passband) {
+    if (h) h->obj->encoding(flag, passband);
+}
 void ophpc_pc_normalize(ophpc_pc* h) { if (h) h->obj->normalize(); }
 
 int32_t ophpc_pc_save(ophpc_pc* h, const char* path, uint8_t bits_per_pixel) {

@@ -79,6 +79,7 @@ def _L():
         L.ophpc_pc_generate_hologram.argtypes = [vp, u32]
         L.ophpc_pc_generate_hologram.restype = d
         L.ophpc_pc_encoding.argtypes = [vp, u32]
+        L.ophpc_pc_encoding_passband.argtypes = [vp, u32, u32]
         L.ophpc_pc_normalize.argtypes = [vp]
         L.ophpc_pc_save.argtypes = [vp, ctypes.c_char_p, ctypes.c_uint8]
         L.ophpc_pc_save.restype = i32
@@ -260,8 +261,13 @@ class PointCloud:
     def generateHologram(self, diff_flag: int = PC_DIFF_RS) -> float:
         return float(self._L.ophpc_pc_generate_hologram(self._h, diff_flag))
 
-    def encoding(self, flag: int) -> None:
-        self._L.ophpc_pc_encoding(self._h, flag)
+    def encoding(self, flag: int, passband: Optional[int] = None) -> None:
+        """encoding(flag), or encoding(flag, passband) for ENCODE_SSB /
+        ENCODE_OFFSSB (ophPointCloud.cpp:242-251)."""
+        if passband is None:
+            self._L.ophpc_pc_encoding(self._h, flag)
+        else:
+            self._L.ophpc_pc_encoding_passband(self._h, flag, passband)
 
     def normalize(self) -> None:
         self._L.ophpc_pc_normalize(self._h)

@@ -318,6 +318,85 @@ def wrp_propagate(plane: np.ndarray, geom: WrpGeometry, wavelength: float) -> np
     return out[hy:hy + pny, hx:hx + pnx]
 
 
+def oph_shift(a: np.ndarray) -> np.ndarray:
+    """Openholo::fftShift (Openholo/src/Openholo.cpp:749-767) of a [ny][nx]
+    array: out[(i - nx/2) mod nx, (j - ny/2) mod ny] = in[i, j] (numpy's
+    ifftshift; fftshift too for even sizes)."""
+    ny, nx = a.shape
+    return np.roll(a, (-(ny >> 1), -(nx >> 1)), axis=(0, 1))
+
+
+def oph_fft2(a: np.ndarray, inverse: bool) -> np.ndarray:
+    """Openholo::fft2(src, dst, nx, ny, type) with its default shift
+    (Openholo/src/Openholo.cpp:698-745): shift, FFTW's unnormalised forward
+    (e^-) or backward (e^+) transform, shift."""
+    s = oph_shift(a)
+    t = np.fft.ifft2(s) * s.size if inverse else np.fft.fft2(s)
+    return oph_shift(t)
+
+
+_MAX_DOUBLE = 1.7976931348623158e+308
+_MIN_DOUBLE = 2.2250738585072014e-308
+
+
+def ssb_encode(field: np.ndarray, ppx: float, ppy: float, encode_flag: int, passband: int = 0,
+               spectrum_shift=(0.0, 0.5)) -> np.ndarray:
+    """m_lpEncoded of ophPointCloud::encoding(ENCODE_SSB | ENCODE_OFFSSB,
+    passband) for field [n_channels, pnY, pnX] complex, FP64, as the
+    reference's code describes (its FFTW input aliases the array it shifts,
+    so its own runs cannot pin this):
+
+    * ENCODE_SSB (7): ophPointCloud::encodeHologram
+      (ophgen/src/ophPointCloud.cpp:191-240) per channel: T = B(F(H)), then
+      Re(T) cos(X + Y) at x = -ssX/2 + ppX w + ppX/2, y = (ssY - ppY) - ppY h,
+      X = pi x sx / ppX, Y = pi y sy / ppY, in the reference's order of
+      operations;
+    * ENCODE_OFFSSB (8): ophGen::encoding(flag, passband)
+      (ophgen/src/ophGen.cpp:882-921) on complex_H[0] for every channel:
+      freqShift(0, 100) (:1079-1098; circShift over the x-major view,
+      Openholo/src/function.h:273-283), singleSideBand (:1023-1077: one half
+      of the shifted spectrum zeroed), the real part and oph::normalize to
+      [0, 1] (function.h:79-99, 188-196).
+    """
+    nch, pny, pnx = field.shape
+    if encode_flag == 7:
+        w = np.arange(pnx, dtype=np.float64)
+        h = np.arange(pny, dtype=np.float64)
+        ssx, ssy = pnx * ppx, pny * ppy
+        y = (ssy - ppy) - ppy * h
+        Y = (np.pi * y * spectrum_shift[1]) / ppy
+        x = (-(ssx / 2) + ppx * w) + ppx / 2
+        X = (np.pi * x * spectrum_shift[0]) / ppx
+        c = np.cos(X)[None, :] * np.cos(Y)[:, None] - np.sin(X)[None, :] * np.sin(Y)[:, None]
+        out = np.empty((nch, pny, pnx))
+        for ch in range(nch):
+            t = oph_fft2(oph_fft2(field[ch], False), True)
+            out[ch] = t.real * c - t.imag * 0.0
+        return out
+    if encode_flag != 8:
+        raise ValueError("encode_flag must be 7 (SSB) or 8 (OFFSSB)")
+    a = oph_fft2(field[0], False)
+    shifted = np.roll(a.reshape(pnx, pny), 100, axis=1).reshape(pny, pnx)
+    tmp = oph_fft2(shifted, True)
+    spec = oph_fft2(tmp, False)
+    flat = spec.reshape(-1)
+    hx, half = pnx >> 1, flat.size >> 1
+    if passband == 0:
+        spec[:, hx:2 * hx] = 0
+    elif passband == 1:
+        spec[:, :hx] = 0
+    elif passband == 2:
+        flat[half:2 * half] = 0
+    else:
+        flat[:half] = 0
+    re = oph_fft2(spec, True).real
+    ok = re[~np.isnan(re)]
+    mn = min(_MAX_DOUBLE, ok.min()) if ok.size else _MAX_DOUBLE
+    mx = max(_MIN_DOUBLE, ok.max()) if ok.size else _MIN_DOUBLE
+    enc = (re - mn) / (mx - mn)
+    return np.stack([enc] * nch)
+
+
 def wrp_generate(geom: WrpGeometry, vertices: np.ndarray) -> np.ndarray:
     """ophWRP::generateHologram restated: per channel the splat, then the
     propagation; complex128 [n_channels, pnY, pnX]."""
