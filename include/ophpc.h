@@ -198,6 +198,19 @@ ophpc_status ophpc_encode_ssb(ophpc_context* ctx, const double* d_field, uint32_
                               double shift_x, double shift_y, double* d_encoded, uint8_t* d_normalized,
                               void* stream);
 
+/* ophGen::encodeSideBand(passband) (ophgen/src/ophGen.cpp:1607-1695, with
+ * getShiftPhaseValue :1741-1781) on device, FP64: per channel the field
+ * cropped to the central half along the passband's axis, the reference's
+ * shifted inverse FFT normalised by pnX pnY, times the passband's carrier,
+ * real part, into d_encoded (m_lpEncoded; optional), and ophGen::normalize's
+ * codes into d_normalized (optional). passband: OPHPC_SSB_*. The reference
+ * keeps this method protected (ophDepthMap and ophIFTA call it); it is
+ * exposed here for callers of the device buffers. Same size limits as
+ * ophpc_encode_ssb; asynchronous on `stream`. */
+ophpc_status ophpc_encode_sideband(ophpc_context* ctx, const double* d_field, uint32_t n_channels, int32_t pnx,
+                                   int32_t pny, double ppx, double ppy, uint32_t passband, double* d_encoded,
+                                   uint8_t* d_normalized, void* stream);
+
 /* Largest n_points * n_channels that ophpc_generate_static_scratch accepts:
  * its scratch is a fixed 32 MiB device array of 64-byte point records. */
 #define OPHPC_STATIC_SCRATCH_RECORDS 524288u

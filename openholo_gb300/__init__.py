@@ -122,6 +122,15 @@ class Context:
                                         ctypes.c_void_p(stream))
         self._check(st, "ophpc_encode_ssb")
 
+    def encode_sideband(self, d_field: int, n_channels: int, pnx: int, pny: int, ppx: float, ppy: float,
+                        passband: int, d_encoded: Optional[int] = None, d_normalized: Optional[int] = None,
+                        stream: int = 0) -> None:
+        """ophGen::encodeSideBand(passband) (ophpc_encode_sideband)."""
+        st = self._lib.ophpc_encode_sideband(self._h, ctypes.c_void_p(d_field), n_channels, pnx, pny, ppx, ppy,
+                                             passband, ctypes.c_void_p(d_encoded or 0),
+                                             ctypes.c_void_p(d_normalized or 0), ctypes.c_void_p(stream))
+        self._check(st, "ophpc_encode_sideband")
+
     def encode(self, d_field: int, n_channels: int, n_pixels: int, encode_flag: int,
                d_encoded: Optional[int], d_normalized: Optional[int], stream: int = 0) -> None:
         st = self._lib.ophpc_encode(self._h, ctypes.c_void_p(d_field), n_channels, ctypes.c_uint64(n_pixels),

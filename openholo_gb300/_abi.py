@@ -152,6 +152,8 @@ def _declare(L: ctypes.CDLL) -> None:
     L.ophpc_fresnel_fft.restype = ctypes.c_int
     L.ophpc_encode_ssb.argtypes = [vp, vp, u32, i32, i32, d, d, u32, u32, d, d, vp, vp, vp]
     L.ophpc_encode_ssb.restype = ctypes.c_int
+    L.ophpc_encode_sideband.argtypes = [vp, vp, u32, i32, i32, d, d, u32, vp, vp, vp]
+    L.ophpc_encode_sideband.restype = ctypes.c_int
 
 
 def lib() -> ctypes.CDLL:

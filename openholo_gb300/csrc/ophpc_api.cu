@@ -41,6 +41,7 @@ ophpc_status fresnel_fft_device(cudaMemPool_t pool, int pnx, int pny, double ppx
                                 double distance, const double2* src, double2* dst, cudaStream_t s,
                                 std::string* err);
 bool ssb_sizes_supported(int pnx, int pny);
+extern const uint32_t kSsbSidebandFlag;
 ophpc_status ssb_encode_device(cudaMemPool_t pool, const double2* d_field, int n_channels, int pnx, int pny,
                                double ppx, double ppy, uint32_t encode_flag, uint32_t passband, double shift_x,
                                double shift_y, double* d_encoded, uint8_t* d_normalized, cudaStream_t s,
@@ -659,6 +660,34 @@ ophpc_status ophpc_encode_ssb(ophpc_context* ctx, const double* d_field, uint32_
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_encoded 8-byte aligned");
     return ssb_encode_device(ctx->pool, (const double2*)d_field, (int)n_channels, pnx, pny, ppx, ppy, encode_flag,
                              passband, shift_x, shift_y, d_encoded, d_normalized, (cudaStream_t)stream,
+                             &ctx->last_error);
+}
+
+ophpc_status ophpc_encode_sideband(ophpc_context* ctx, const double* d_field, uint32_t n_channels, int32_t pnx,
+                                   int32_t pny, double ppx, double ppy, uint32_t passband, double* d_encoded,
+                                   uint8_t* d_normalized, void* stream) {
+    if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->last_error.clear();
+    if (passband > OPHPC_SSB_BOTTOM)
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "passband: OPHPC_SSB_LEFT, _RIGHT, _TOP or _BOTTOM");
+    if (n_channels < 1 || n_channels > OPHPC_MAX_CHANNELS)
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "n_channels must be 1..3");
+    if (pnx <= 0 || pny <= 0 || pnx > 16384 || pny > 16384)
+        return fail(ctx, OPHPC_ERROR_CONFIG, "pixel numbers must be 1..16384");
+    if (!finite_pos(ppx) || !finite_pos(ppy)) return fail(ctx, OPHPC_ERROR_CONFIG, "pitches must be finite and positive");
+    if (!ssb_sizes_supported(pnx, pny))
+        return fail(ctx, OPHPC_ERROR_UNSUPPORTED, "pnX and pnY must factor into 2, 3, 5 and 7");
+    DeviceGuard guard(ctx->device);
+    if (!d_field || !is_device_ptr(d_field)) return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be device memory");
+    if (d_encoded && !is_device_ptr(d_encoded))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_encoded must be device memory");
+    if (d_normalized && !is_device_ptr(d_normalized))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_normalized must be device memory");
+    if (!aligned(d_field, 16) || !aligned(d_encoded, 8))
+        return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_field must be 16-byte and d_encoded 8-byte aligned");
+    return ssb_encode_device(ctx->pool, (const double2*)d_field, (int)n_channels, pnx, pny, ppx, ppy,
+                             kSsbSidebandFlag, passband, 0.0, 0.0, d_encoded, d_normalized, (cudaStream_t)stream,
                              &ctx->last_error);
 }
 

@@ -22,6 +22,18 @@
 // the real part, and oph::normalize to [0, 1] with minOfArr / maxOfArr,
 // function.h:79-99, 188-196).
 //
+// SIDEBAND — ophGen::encodeSideBand(passband) (ophgen/src/ophGen.cpp:
+// 1607-1653, encodeSideBand_CPU :1655-1695, getShiftPhaseValue :1741-1781)
+// per channel: the field cropped to the central half along one axis (all
+// columns and rows [c1, c2] for SSB_TOP / SSB_BOTTOM, all rows and columns
+// [c1, c2] for SSB_LEFT / SSB_RIGHT; h = floor(n/2), c1 = h - floor(h/2) - 1,
+// c2 = c1 + h - 1), B normalised by N, times the carrier e^{i theta} and the
+// real part; theta = +-2 pi yy / (4 ppY), yy = ssY/2 - ppY r - ppY (TOP +,
+// BOTTOM -), or theta = -+2 pi xx / (4 ppX), xx = -ssX/2 - ppX c - ppX (LEFT
+// -, RIGHT +). That path's FFTW plan reads FFTW's own buffer, so the
+// reference's output is well defined and pins this one
+// (tests/golden/sideband.npz).
+//
 // The reference runs these transforms through FFTW plans whose input buffer
 // aliases the array being shifted, so its own outputs are not reproducible;
 // what is computed here is what the code describes, restated in FP64 numpy
@@ -38,6 +50,8 @@ namespace ophpc {
 namespace {
 
 constexpr double kPiSsb = 3.14159265358979323846;
+// ssb_encode_device's flag for ophGen::encodeSideBand (not an ENCODE_FLAG)
+constexpr uint32_t kEncodeSideband = 0x10000u;
 constexpr double kMaxDoubleSsb = 1.7976931348623158e+308;
 constexpr double kMinDoubleSsb = 2.2250738585072014e-308;
 
@@ -79,6 +93,41 @@ __global__ void ssb_passband_kernel(double2* __restrict__ as, int nx, int ny, in
         }
         if (zero) as[f] = make_double2(0.0, 0.0);
     }
+}
+
+// The field inside the crop rectangle [x1, x2] x [y1, y2] (inclusive), zero
+// elsewhere.
+__global__ void ssb_crop_kernel(const double2* __restrict__ in, double2* __restrict__ out, int nx, int ny, int x1,
+                                int x2, int y1, int y2) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= nx) return;
+    const int64_t i = (int64_t)y * nx + x;
+    out[i] = (x >= x1 && x <= x2 && y >= y1 && y <= y2) ? in[i] : make_double2(0.0, 0.0);
+}
+
+// encodeSideBand_CPU's carrier and real part (one channel); t is the
+// unnormalised inverse transform, divided by n here as fft2's bNormalized
+// does.
+__global__ void ssb_fringe_kernel(const double2* __restrict__ t, double* __restrict__ enc, int pnx, int pny,
+                                  double ppx, double ppy, int passband) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (c >= pnx) return;
+    const double n = (double)((int64_t)pnx * pny);
+    const double two_pi = 2 * kPiSsb;
+    double theta;
+    if (passband == OPHPC_SSB_TOP || passband == OPHPC_SSB_BOTTOM) {
+        const double ssy = __dmul_rn((double)pny, ppy);
+        const double yy = __dsub_rn(__dsub_rn(ssy / 2.0, __dmul_rn(ppy, (double)r)), ppy);
+        theta = __dmul_rn(two_pi, __ddiv_rn(passband == OPHPC_SSB_TOP ? yy : -yy, __dmul_rn(4.0, ppy)));
+    } else {
+        const double ssx = __dmul_rn((double)pnx, ppx);
+        const double xx = __dsub_rn(__dsub_rn(-ssx / 2.0, __dmul_rn(ppx, (double)c)), ppx);
+        theta = __dmul_rn(two_pi, __ddiv_rn(passband == OPHPC_SSB_LEFT ? -xx : xx, __dmul_rn(4.0, ppx)));
+    }
+    const int64_t i = (int64_t)r * pnx + c;
+    const double2 v = t[i];
+    const double re = __ddiv_rn(v.x, n), im = __ddiv_rn(v.y, n);
+    enc[i] = __dsub_rn(__dmul_rn(re, cos(theta)), __dmul_rn(im, sin(theta)));
 }
 
 // encodeHologram's shifted real part into enc (one channel).
@@ -171,6 +220,7 @@ cudaError_t shifted_fft2(const double2* src, double2* dst, double2* const buf[2]
 }  // namespace
 
 bool ssb_sizes_supported(int pnx, int pny) { return fft_supported(pnx) && fft_supported(pny); }
+extern const uint32_t kSsbSidebandFlag = kEncodeSideband;
 
 ophpc_status ssb_encode_device(cudaMemPool_t pool, const double2* d_field, int n_channels, int pnx, int pny,
                                double ppx, double ppy, uint32_t encode_flag, uint32_t passband, double shift_x,
@@ -198,7 +248,29 @@ ophpc_status ssb_encode_device(cudaMemPool_t pool, const double2* d_field, int n
     fft_plan_init(&plan_x, pnx, tw, s);
     fft_plan_init(&plan_y, pny, tw + fft_twiddle_count(pnx), s);
     cudaError_t e = cudaSuccess;
-    if (encode_flag == OPHPC_ENCODE_SSB) {
+    const dim3 g2((unsigned)((pnx + 255) / 256), (unsigned)pny);
+    if (encode_flag == kEncodeSideband) {
+        int x1 = 0, x2 = pnx - 1, y1 = 0, y2 = pny - 1;
+        if (passband == OPHPC_SSB_TOP || passband == OPHPC_SSB_BOTTOM) {
+            const int h = pny / 2;
+            y1 = h - h / 2 - 1;
+            y2 = y1 + h - 1;
+        } else {
+            const int h = pnx / 2;
+            x1 = h - h / 2 - 1;
+            x2 = x1 + h - 1;
+        }
+        for (int c = 0; c < n_channels && e == cudaSuccess; ++c) {
+            count_launches(1);
+            ssb_crop_kernel<<<g2, 256, 0, s>>>(d_field + (int64_t)c * n, w2, pnx, pny, x1, x2, y1, y2);
+            e = shifted_fft2(w2, w2, buf, plan_x, plan_y, pnx, pny, true, s);
+            if (e == cudaSuccess) {
+                count_launches(1);
+                ssb_fringe_kernel<<<g2, 256, 0, s>>>(w2, enc + (int64_t)c * n, pnx, pny, ppx, ppy, (int)passband);
+                e = cudaGetLastError();
+            }
+        }
+    } else if (encode_flag == OPHPC_ENCODE_SSB) {
         for (int c = 0; c < n_channels && e == cudaSuccess; ++c) {
             e = shifted_fft2(d_field + (int64_t)c * n, w2, buf, plan_x, plan_y, pnx, pny, false, s);
             if (e == cudaSuccess) e = shifted_fft2(w2, w2, buf, plan_x, plan_y, pnx, pny, true, s);

@@ -397,6 +397,47 @@ def ssb_encode(field: np.ndarray, ppx: float, ppy: float, encode_flag: int, pass
     return np.stack([enc] * nch)
 
 
+def sideband_encode(field: np.ndarray, ppx: float, ppy: float, passband: int) -> np.ndarray:
+    """m_lpEncoded of ophGen::encodeSideBand(passband)
+    (ophgen/src/ophGen.cpp:1607-1653 with encodeSideBand_CPU, :1655-1695,
+    and getShiftPhaseValue, :1741-1781) for field [n_channels, pnY, pnX]:
+    per channel the field cropped to the central half along one axis
+    (1-based bounds c1 = h - floor(h/2), c2 = c1 + h - 1, h = floor(n/2),
+    made 0-based), B = S IFFT S normalised by N, times the carrier
+    e^{i theta} — TOP / BOTTOM: theta = +-2 pi yy / (4 ppY), yy = ssY/2 -
+    ppY r - ppY; LEFT / RIGHT: theta = -+2 pi xx / (4 ppX), xx = -ssX/2 -
+    ppX c - ppX — and the real part. Pinned to the reference's own output
+    (tests/golden/sideband.npz)."""
+    nch, pny, pnx = field.shape
+    if passband in (2, 3):
+        h = pny // 2
+        y1 = h - h // 2 - 1
+        rows, cols = slice(y1, y1 + h), slice(0, pnx)
+    else:
+        h = pnx // 2
+        x1 = h - h // 2 - 1
+        rows, cols = slice(0, pny), slice(x1, x1 + h)
+    ssx, ssy = pnx * ppx, pny * ppy
+    r = np.arange(pny, dtype=np.float64)[:, None]
+    c = np.arange(pnx, dtype=np.float64)[None, :]
+    if passband in (2, 3):
+        yy = (ssy / 2.0) - ppy * r - ppy
+        theta = 2 * np.pi * ((yy if passband == 2 else -yy) / (4 * ppy)) + 0.0 * c
+    else:
+        xx = (-ssx / 2.0) - ppx * c - ppx
+        theta = 2 * np.pi * ((-xx if passband == 0 else xx) / (4 * ppx)) + 0.0 * r
+    cs, sn = np.cos(theta), np.sin(theta)
+    out = np.empty((nch, pny, pnx))
+    n = pnx * pny
+    for ch in range(nch):
+        crop = np.zeros((pny, pnx), dtype=np.complex128)
+        crop[rows, cols] = field[ch][rows, cols]
+        s = oph_shift(crop)
+        t = oph_shift((np.fft.ifft2(s) * n) / n)
+        out[ch] = t.real * cs - t.imag * sn
+    return out
+
+
 def wrp_generate(geom: WrpGeometry, vertices: np.ndarray) -> np.ndarray:
     """ophWRP::generateHologram restated: per channel the splat, then the
     propagation; complex128 [n_channels, pnY, pnX]."""
@@ -404,6 +445,28 @@ def wrp_generate(geom: WrpGeometry, vertices: np.ndarray) -> np.ndarray:
 
 
 REF_WRP_LIB = os.path.join(HERE, "_ref", "libophref_wrp.so")
+REF_SIDEBAND_LIB = os.path.join(HERE, "_ref", "libophref_sideband.so")
+
+
+def ref_sideband_available() -> bool:
+    return os.path.exists(REF_SIDEBAND_LIB)
+
+
+def ref_sideband(xml_path: str, field: np.ndarray, passband: int) -> np.ndarray:
+    """The reference's own ophGen::encodeSideBand on field [n_channels,
+    pnY, pnX] (oracle/ref_sideband_driver.cpp; FFTW replaced by the FP64 DFT
+    of oracle/ref_dft_stubs.c): m_lpEncoded, float64 [n_channels, pnY, pnX]."""
+    lib = ctypes.CDLL(REF_SIDEBAND_LIB)
+    lib.ophref_sideband.argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_uint, ctypes.c_void_p, ctypes.c_int]
+    lib.ophref_sideband.restype = ctypes.c_int
+    nch = field.shape[0]
+    f = np.ascontiguousarray(field, dtype=np.complex128)
+    out = np.zeros(field.shape, dtype=np.float64)
+    with _QuietStdout():
+        rc = lib.ophref_sideband(xml_path.encode(), f.ctypes.data, passband, out.ctypes.data, nch)
+    if rc != nch:
+        raise RuntimeError(f"ophref_sideband failed ({rc})")
+    return out
 
 
 def ref_wrp_available() -> bool:

@@ -324,6 +324,33 @@ def make_wrp(xml):
     return out
 
 
+SIDEBAND_CASES = {   # (pnx, pny, ppx, ppy, wavelengths, seed)
+    "even_2ch": (24, 16, 8e-6, 6.4e-6, [532e-9, 638e-9], 61),
+    "odd_1ch": (15, 9, 8e-6, 8e-6, [532e-9], 62),
+    "mixed_3ch": (20, 21, 6.4e-6, 7.1e-6, [638e-9, 532e-9, 473e-9], 63),
+}
+
+
+def make_sideband(xml):
+    """The reference's own ophGen::encodeSideBand (ophgen/src/ophGen.cpp:
+    1607-1695) on seeded random fields, every passband (oracle/
+    ref_sideband_driver.cpp; FFTW replaced by the FP64 DFT of
+    oracle/ref_dft_stubs.c)."""
+    arrays = {}
+    for name, (pnx, pny, ppx, ppy, wl, seed) in SIDEBAND_CASES.items():
+        g = oracle.Geometry(pnx=pnx, pny=pny, ppx=ppx, ppy=ppy, wavelengths=wl)
+        with open(xml, "w") as f:
+            f.write(g.xml())
+        rng = np.random.default_rng(seed)
+        field = rng.normal(size=(len(wl), pny, pnx)) + 1j * rng.normal(size=(len(wl), pny, pnx))
+        arrays[name + "_field"] = field
+        arrays[name + "_geom"] = np.array([pnx, pny, ppx, ppy])
+        for pb in range(4):
+            arrays[f"{name}_enc{pb}"] = oracle.ref_sideband(xml, field, pb)
+    np.savez_compressed(os.path.join(HERE, "sideband.npz"), **arrays)
+    return {"sideband": len(arrays)}
+
+
 def main():
     if not oracle.ref_available():
         oracle.build(with_reference=True)
@@ -405,15 +432,16 @@ def main():
         out.update(make_ply_faces())
         out.update(make_dice(xml))
         out.update(make_wrp(xml))
+        out.update(make_sideband(xml))
     for k, v in out.items():
         print(k, v)
 
 
 if __name__ == "__main__":
     only = {"ohc": make_ohc, "encoders": make_encoders, "ply_faces": lambda xml: make_ply_faces(),
-            "dice": make_dice, "wrp": make_wrp}
+            "dice": make_dice, "wrp": make_wrp, "sideband": make_sideband}
     if len(sys.argv) == 2 and sys.argv[1] in only:   # one group of fixtures
-        if not oracle.ref_available() or not oracle.ref_wrp_available():
+        if not oracle.ref_available() or not oracle.ref_wrp_available() or not oracle.ref_sideband_available():
             oracle.build(with_reference=True)
         with tempfile.TemporaryDirectory() as d:
             print(only[sys.argv[1]](os.path.join(d, "cfg.xml")))

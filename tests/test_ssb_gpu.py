@@ -131,3 +131,41 @@ def test_facade_ssb_encoding(tmp_path, gpu_ctx, oracle_mod):
             codes_ref, _, _ = oracle_mod.normalize(want.reshape(2, -1))
             exact, maxd = code_agreement(codes.reshape(2, -1), codes_ref.reshape(2, -1), False)
             assert exact >= 0.9999 and maxd <= 1, flag
+
+
+def _sideband(ctx, field, ppx, ppy, passband):
+    import torch
+    nch, pny, pnx = field.shape
+    f = torch.from_numpy(np.ascontiguousarray(field).view(np.float64).reshape(nch, pny, pnx, 2)).cuda()
+    enc = torch.full((nch, pny * pnx), float("nan"), dtype=torch.float64, device="cuda")
+    codes = torch.empty((nch, pny * pnx), dtype=torch.uint8, device="cuda")
+    ctx.encode_sideband(f.data_ptr(), nch, pnx, pny, ppx, ppy, passband, enc.data_ptr(), codes.data_ptr(),
+                        torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    return enc.cpu().numpy().reshape(nch, pny, pnx), codes.cpu().numpy()
+
+
+def test_sideband_matches_reference_fixtures(gpu_ctx):
+    """ophpc_encode_sideband against the reference's own encodeSideBand
+    (tests/golden/sideband.npz), every passband."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sideband.npz"))
+    names = sorted({k[:-len("_field")] for k in z.files if k.endswith("_field")})
+    for name in names:
+        pnx, pny, ppx, ppy = z[name + "_geom"]
+        for pb in range(4):
+            want = z[f"{name}_enc{pb}"]
+            got, _ = _sideband(gpu_ctx, z[name + "_field"], float(ppx), float(ppy), pb)
+            assert rel_l2(got, want) <= 1e-12, (name, pb)
+
+
+@pytest.mark.parametrize("pnx,pny", [(128, 36), (105, 49), (1920, 1080)])
+@pytest.mark.parametrize("passband", [0, 1, 2, 3])
+def test_sideband_matches_oracle(gpu_ctx, oracle_mod, pnx, pny, passband):
+    field = _field(2, pny, pnx, pnx + pny + passband)
+    enc, codes = _sideband(gpu_ctx, field, 8e-6, 8e-6, passband)
+    want = oracle_mod.sideband_encode(field, 8e-6, 8e-6, passband)
+    assert rel_l2(enc, want) <= 1e-10
+    codes_ref, _, _ = oracle_mod.normalize(want.reshape(2, -1))
+    exact, maxd = code_agreement(codes, codes_ref.reshape(2, -1), False)
+    assert exact >= 0.9999 and maxd <= 1

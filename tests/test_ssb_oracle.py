@@ -13,8 +13,14 @@ maxOfArr and oph::normalize (function.h:79-99, 188-196), and the pixel
 coordinates of ophPointCloud::encodeHologram
 (ophgen/src/ophPointCloud.cpp:191-240) — and the numpy oracle must agree
 with them to rounding.
+
+ophGen::encodeSideBand (ophgen/src/ophGen.cpp:1607-1695) transforms through
+FFTW's own buffer, so the reference's output is well defined: its oracle
+(oracle.sideband_encode) is pinned to the reference run itself
+(tests/golden/sideband.npz).
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -136,3 +142,28 @@ def test_ssb_round_trip_is_the_field_times_n_for_even_sizes(oracle_mod):
     y = (ny * 8e-6 - 8e-6) - 8e-6 * np.arange(ny)
     c = np.cos(np.pi * y * 0.5 / 8e-6)
     assert np.allclose(got, nx * ny * h[0].real * c[:, None], rtol=0, atol=1e-12 * np.abs(got).max())
+
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _sideband_cases():
+    z = np.load(os.path.join(GOLD, "sideband.npz"))
+    names = sorted({k[:-len("_field")] for k in z.files if k.endswith("_field")})
+    return z, names
+
+
+def test_sideband_oracle_matches_reference(oracle_mod):
+    """oracle.sideband_encode against the reference's own encodeSideBand
+    (tests/golden/sideband.npz: ophGen.cpp:1607-1695 run from the reference
+    build, FFTW replaced by an FP64 DFT), every passband, even, odd and
+    mixed sizes."""
+    z, names = _sideband_cases()
+    assert len(names) == 3
+    for name in names:
+        pnx, pny, ppx, ppy = z[name + "_geom"]
+        field = z[name + "_field"]
+        for pb in range(4):
+            want = z[f"{name}_enc{pb}"]
+            got = oracle_mod.sideband_encode(field, float(ppx), float(ppy), pb)
+            assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max(), (name, pb)
