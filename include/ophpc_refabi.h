@@ -17,8 +17,12 @@
  * before upload; work is queued on the legacy default stream.
  *
  * Differences: nBlocks and nThreads are ignored (launch shapes are chosen
- * for sm_103a), `mode` selects nothing (one kernel per method, FP32 with an
- * FP64 phase reduction and FP64 output), and k is taken as 2*pi/lambda.
+ * for sm_103a); the reference's `mode` bits (MODE_FLOAT, MODE_FASTMATH)
+ * select nothing (one kernel per method, FP32 with an FP64 phase reduction
+ * and FP64 output), while OPHPC_MODE_TENSOR_BF16X3 (0x200) in `mode`
+ * selects the tensor-core tile kernels (split-BF16, relL2 ~1e-5 against
+ * FP64), with which the call also waits for its kernels to read their
+ * timeout word; k is taken as 2*pi/lambda.
  * The launch sizes and the scratch depend on the config, which lives in
  * device memory, so each call first reads the 120-byte config back with a
  * copy on the legacy stream: the call waits for the work queued on that

@@ -227,6 +227,56 @@ cudaError_t pool_alloc(ophpc_context* ctx, T** p, size_t bytes, cudaStream_t s) 
 // accumulate: add into d_field instead of overwriting it (plain kernels only).
 // d_err_out: the tensor-core paths copy their kernels' timeout word there
 // instead of waiting for the stream (graph capture).
+// Tensor-core generate added into d_field (the reference-signature
+// launchers with OPHPC_MODE_TENSOR_BF16X3): point preparation, the
+// amplitude bound (and, for RS, the window flag), then the tile kernel over
+// the whole point range adding into the field, with the CUDA-core complement
+// for RS. The kernels' timeout word is read back, so the call waits for its
+// kernels.
+ophpc_status tc_generate_accumulate(ophpc_context* ctx, const JobGeom& jg, const ophpc_config* cfg,
+                                    const ophpc_vertex* d_vertices, uint64_t n_points, uint32_t diff_flag,
+                                    int color_offset, double* d_field, cudaStream_t s) {
+    const int64_t n = (int64_t)n_points;
+    const int nch = (int)cfg->n_channels, pnx = cfg->pixel_number[0], pny = cfg->pixel_number[1];
+    const bool rs = diff_flag == OPHPC_DIFF_RS;
+    const size_t tiles = (size_t)nch * ((pnx + kRsTcTile - 1) / kRsTcTile) * ((pny + kRsTcTile - 1) / kRsTcTile);
+    const int64_t mask_words = tc_rs_mask_words(n);
+    auto al = [](size_t v) { return (v + 255) & ~(size_t)255; };
+    const size_t rec_bytes = al(sizeof(PointRec) * (size_t)n * nch);
+    const size_t left_bytes = rs ? al(sizeof(int32_t) * tiles) : 0;
+    size_t mask_bytes = rs ? al(sizeof(uint32_t) * tiles * (size_t)mask_words) : 0;
+    if (mask_bytes > ((size_t)4 << 30)) mask_bytes = 0;   // the complement re-tests eligibility instead
+    unsigned char* mem = nullptr;
+    cudaError_t e = pool_alloc(ctx, &mem, rec_bytes + left_bytes + mask_bytes + 256, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scratch allocation (tensor-core generate)");
+    PointRec* recs = (PointRec*)mem;
+    int32_t* left = rs ? (int32_t*)(mem + rec_bytes) : nullptr;
+    uint32_t* mask = mask_bytes ? (uint32_t*)(mem + rec_bytes + left_bytes) : nullptr;
+    float* amax = (float*)(mem + rec_bytes + left_bytes + mask_bytes);   // [4] words, then the error word
+    int* errw = (int*)(amax + 4);
+    e = cudaMemsetAsync(amax, 0, 32, s);
+    launch_prep(d_vertices, n, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window, (int)diff_flag, jg,
+                recs, s, color_offset);
+    if (e == cudaSuccess) {
+        if (rs) {
+            launch_rs_amax(recs, n, nch, pnx, pny, amax, s);
+            e = launch_tc_rs_range(jg, recs, 0, n, true, (double2*)d_field, amax, left, mask,
+                                   mask ? mask_words : 0, errw, s);
+        } else {
+            launch_fresnel_amax(recs, n, nch, amax, s);
+            e = launch_tc_fresnel_range(jg, recs, 0, n, true, (double2*)d_field, amax, errw, s);
+        }
+    }
+    if (e == cudaSuccess) e = cudaGetLastError();
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, errw, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(mem, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "tensor-core generate");
+    if (herr) return fail(ctx, OPHPC_ERROR_TIMEOUT, "tensor-core kernel wait timed out");
+    return OPHPC_SUCCESS;
+}
+
 ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                              uint64_t n_points, uint32_t diff_flag, uint32_t mode, double* d_field,
                              cudaStream_t s, int color_offset = 0, bool accumulate = false,
@@ -241,6 +291,8 @@ ophpc_status generate_device(ophpc_context* ctx, const ophpc_config* cfg, const 
         cudaError_t e = cudaMemsetAsync(d_field, 0, sizeof(double2) * field_elems, s);
         return e == cudaSuccess ? OPHPC_SUCCESS : cuda_fail(ctx, e, "cudaMemsetAsync(field)");
     }
+    if (accumulate && (mode & OPHPC_MODE_TENSOR_BF16X3))
+        return tc_generate_accumulate(ctx, jg, cfg, d_vertices, n_points, diff_flag, color_offset, d_field, s);
     if (tensor && !accumulate) {
         // split-BF16: factors generated on chip per 128x128 tile; FP16:
         // factor tables in HBM and a tcgen05 GEMM over them
@@ -298,14 +350,17 @@ ophpc_status check_job(ophpc_context* ctx, const ophpc_config* cfg, uint64_t n_p
 namespace ophpc {
 
 // For the reference-signature launchers (pc_refabi.cu): one channel, the
-// amplitude from color[color_offset], added into d_field; plain kernels.
+// amplitude from color[color_offset], added into d_field; the plain kernels,
+// or with OPHPC_MODE_TENSOR_BF16X3 in `mode` the tensor-core tile kernels
+// (other mode bits select nothing).
 ophpc_status generate_accumulate(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                                  uint64_t n_points, uint32_t diff_flag, int color_offset, double* d_field,
-                                 cudaStream_t s) {
+                                 cudaStream_t s, uint32_t mode) {
     if (!ctx) return OPHPC_ERROR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ctx->mu);
     ctx->last_error.clear();
-    ophpc_status st = check_job(ctx, cfg, n_points, diff_flag, 0);
+    mode &= OPHPC_MODE_TENSOR_BF16X3;
+    ophpc_status st = check_job(ctx, cfg, n_points, diff_flag, mode);
     if (st != OPHPC_SUCCESS) return st;
     if (color_offset < 0 || color_offset + (int)cfg->n_channels > OPHPC_MAX_CHANNELS)
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "colour index must be 0..2");
@@ -315,7 +370,7 @@ ophpc_status generate_accumulate(ophpc_context* ctx, const ophpc_config* cfg, co
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "vertices must be device memory");
     if (!aligned(d_field, 16) || !aligned(d_vertices, 8))
         return fail(ctx, OPHPC_ERROR_INVALID_ARGUMENT, "d_dst must be 16-byte and vertices 8-byte aligned");
-    return generate_device(ctx, cfg, d_vertices, n_points, diff_flag, 0, d_field, s, color_offset, true);
+    return generate_device(ctx, cfg, d_vertices, n_points, diff_flag, mode, d_field, s, color_offset, true);
 }
 
 }  // namespace ophpc

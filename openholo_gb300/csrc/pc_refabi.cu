@@ -8,8 +8,11 @@
 // the work queued on that stream before it, and no longer), turns it into a
 // one-channel ophpc_config and queues prep + RS/Fresnel on the legacy
 // default stream with the amplitude taken from color[iColor] and the result
-// added into d_dst; it returns while those kernels run. One context per
-// device is created on first use and kept for the life of the process.
+// added into d_dst; it returns while those kernels run. With
+// OPHPC_MODE_TENSOR_BF16X3 set in `mode` (the reference's own mode bits
+// select nothing) the tensor-core tile kernels run instead, and the call
+// waits for them (it reads their timeout word back). One context per device
+// is created on first use and kept for the life of the process.
 #include "ophpc_refabi.h"
 #include "pc_common.cuh"
 
@@ -25,7 +28,7 @@ struct ophpc_context;
 namespace ophpc {
 ophpc_status generate_accumulate(ophpc_context* ctx, const ophpc_config* cfg, const ophpc_vertex* d_vertices,
                                  uint64_t n_points, uint32_t diff_flag, int color_offset, double* d_field,
-                                 cudaStream_t s);
+                                 cudaStream_t s, uint32_t mode);
 }
 
 // The reference's config structs (ophPointCloud_GPU.h:89-217) as laid out by
@@ -76,7 +79,7 @@ void report(const char* fn, ophpc_status st, ophpc_context* ctx) {
 }
 
 void run(const char* fn, uint32_t diff_flag, const ophpc_vertex* d_vertex, double* d_dst, const void* d_config,
-         unsigned i_color) {
+         unsigned i_color, unsigned mode) {
     ophpc_status st = OPHPC_SUCCESS;
     ophpc_context* ctx = context_for_current_device(&st);
     if (!ctx) return report(fn, st, nullptr);
@@ -105,7 +108,7 @@ void run(const char* fn, uint32_t diff_flag, const ophpc_vertex* d_vertex, doubl
     cfg.n_channels = 1;
     cfg.wave_length[0] = c.lambda;
     st = ophpc::generate_accumulate(ctx, &cfg, d_vertex, (uint64_t)c.n_points, diff_flag, (int)i_color, d_dst,
-                                    (cudaStream_t)0);
+                                    (cudaStream_t)0, mode);
     report(fn, st, ctx);
 }
 
@@ -141,13 +144,14 @@ void sum_Kernel(const int&, const int&, double* dst, double* src, int size) {
 }
 
 void cudaPointCloud_RS(const int&, const int&, ophpc_vertex* d_vertex, double* d_dst,
-                       const ophpc_ref_pc_config_rs* d_config, const unsigned& iColor, const unsigned&) {
-    run("cudaPointCloud_RS", OPHPC_DIFF_RS, d_vertex, d_dst, d_config, iColor);
+                       const ophpc_ref_pc_config_rs* d_config, const unsigned& iColor, const unsigned& mode) {
+    run("cudaPointCloud_RS", OPHPC_DIFF_RS, d_vertex, d_dst, d_config, iColor, mode);
 }
 
 void cudaPointCloud_Fresnel(const int&, const int&, ophpc_vertex* d_vertex, double* d_dst,
-                            const ophpc_ref_pc_config_fresnel* d_config, const unsigned& iColor, const unsigned&) {
-    run("cudaPointCloud_Fresnel", OPHPC_DIFF_FRESNEL, d_vertex, d_dst, d_config, iColor);
+                            const ophpc_ref_pc_config_fresnel* d_config, const unsigned& iColor,
+                            const unsigned& mode) {
+    run("cudaPointCloud_Fresnel", OPHPC_DIFF_FRESNEL, d_vertex, d_dst, d_config, iColor, mode);
 }
 
 ophpc_status ophpc_refabi_last_status(void) { return t_last; }

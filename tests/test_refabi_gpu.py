@@ -78,7 +78,7 @@ def _launch(L, diff, d_v, d_dst, d_cfg, ch, mode=0):
     return L.ophpc_refabi_last_status()
 
 
-def _run(L, g, v, diff):
+def _run(L, g, v, diff, mode=0):
     """The reference driver's single-GPU loop; returns [nch, pny, pnx] complex."""
     import torch
     nch = len(g["wavelengths"])
@@ -88,7 +88,7 @@ def _run(L, g, v, diff):
     for ch in range(nch):
         c = _config(g, v.shape[0], ch, diff)
         d_cfg = torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8).cuda()
-        assert _launch(L, diff, d_v.data_ptr(), d_dst.data_ptr(), d_cfg.data_ptr(), ch) == 0
+        assert _launch(L, diff, d_v.data_ptr(), d_dst.data_ptr(), d_cfg.data_ptr(), ch, mode) == 0
         h = d_dst.cpu().numpy()
         out.append((h[:, 0] + 1j * h[:, 1]).reshape(g["pny"], g["pnx"]))
         d_dst.zero_()
@@ -105,6 +105,27 @@ def test_launchers_match_reference_fields(gpu_ctx, name):
     assert rel_l2(got, d["field"]) <= FIELD_TOL
     mine = run_generate(gpu_ctx, g, d["vertices"], diff)
     assert rel_l2(got, mine) <= 1e-12
+
+
+@pytest.mark.parametrize("name", ["rs_window_1ch", "fresnel_window_1ch", "fresnel_3ch"])
+def test_launchers_reach_the_tensor_cores(gpu_ctx, name):
+    """mode = OPHPC_MODE_TENSOR_BF16X3 (with the reference's MODE_GPU bit):
+    the tensor-core tile kernels behind the same launchers, against the
+    reference's fields and ophpc_generate's tensor-core result; adding into a
+    field that already holds one result doubles it."""
+    import openholo_gb300 as oph
+    d = np.load(os.path.join(GOLD, name + ".npz"))
+    g = _geometry(str(d["xml"]))
+    diff = int(d["diff_flag"])
+    L = _lib()
+    before = oph.lib().ophpc_kernel_launches()
+    got = _run(L, g, d["vertices"], diff, mode=0x200 | 1)
+    assert oph.lib().ophpc_kernel_launches() - before >= 3 * len(g["wavelengths"])
+    assert rel_l2(got, d["field"]) <= FIELD_TOL
+    mine = run_generate(gpu_ctx, g, d["vertices"], diff, 0x200)
+    assert rel_l2(got, mine) <= 5e-5
+    plain = _run(L, g, d["vertices"], diff)
+    assert rel_l2(got, plain) <= FIELD_TOL
 
 
 def test_launchers_accumulate_and_sum_kernel(gpu_ctx):
