@@ -202,6 +202,7 @@ private:
     long long buffer_pixels_ = 0;
     ulonglong n_points_ = 0;
     Vertex* vertices_ = nullptr;
+    ulonglong vertices_cap_ = 0;   /* records vertices_ holds */
     Complex<Real>** complex_H_ = nullptr;
     Real** encoded_ = nullptr;
     uchar** normalized_ = nullptr;
@@ -215,6 +216,7 @@ private:
     size_t cap_v_ = 0, cap_f_ = 0, cap_e_ = 0, cap_c_ = 0;
     bool encoded_valid_ = false;
     bool host_pinned_ = false;  /* per-channel buffers are page-locked (cudaHostAlloc) */
+    void* streams_[OPHPC_MAX_CHANNELS] = {};   /* encoding(): one CUDA stream per channel */
 };
 
 #endif /* OPHPC_OPHPOINTCLOUD_H */

@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -69,6 +70,8 @@ ophPointCloud::~ophPointCloud(void) {
     if (d_field_) cudaFree(d_field_);
     if (d_encoded_) cudaFree(d_encoded_);
     if (d_codes_) cudaFree(d_codes_);
+    for (void* st : streams_)
+        if (st) cudaStreamDestroy((cudaStream_t)st);
     if (gpu_) ophpc_destroy(gpu_);
 }
 
@@ -205,15 +208,21 @@ int ophPointCloud::loadPointCloud(const char* pc_file) {
     }
     delete[] vertices_;
     vertices_ = v;
+    vertices_cap_ = (ulonglong)n;
     n_points_ = (ulonglong)n;
     return (int)n;
 }
 
 void ophPointCloud::setPointCloudModel(Vertex* vertex) {
     if (n_points_ < 1 || !vertex) return;
-    delete[] vertices_;
-    vertices_ = new Vertex[n_points_];
-    std::memcpy(vertices_, vertex, sizeof(Vertex) * n_points_);
+    if (vertices_ != vertex) {   // the copy (ophPointCloud.h:577-586); its buffer is reused at the same size
+        if (!vertices_ || vertices_cap_ != n_points_) {
+            delete[] vertices_;
+            vertices_ = new Vertex[n_points_];
+            vertices_cap_ = n_points_;
+        }
+        std::memcpy(vertices_, vertex, sizeof(Vertex) * n_points_);
+    }
 }
 
 void ophPointCloud::fillConfig(ophpc_config* c) const {
@@ -276,10 +285,25 @@ Real ophPointCloud::generateHologram(uint diff_flag) {
         last_error_ = "readConfig must succeed before generateHologram";
         return 0.0;
     }
-    // resetBuffer (ophGen.cpp:801-814)
-    for (uint c = 0; c < context_.waveNum; ++c) {
-        std::memset(encoded_[c], 0, sizeof(Real) * buffer_pixels_);
-        std::memset(normalized_[c], 0, (size_t)buffer_pixels_);
+    // resetBuffer (ophGen.cpp:801-814), on a helper thread while the GPU
+    // generates: the buffers are back to zero before this call returns
+    struct Joiner {
+        std::thread t;
+        ~Joiner() {
+            if (t.joinable()) t.join();
+        }
+    } reset;
+    {
+        Real** enc = encoded_;
+        uchar** nrm = normalized_;
+        const uint nch_reset = context_.waveNum;
+        const size_t px = (size_t)buffer_pixels_;
+        reset.t = std::thread([enc, nrm, nch_reset, px] {
+            for (uint c = 0; c < nch_reset; ++c) {
+                std::memset(enc[c], 0, sizeof(Real) * px);
+                std::memset(nrm[c], 0, px);
+            }
+        });
     }
     encoded_valid_ = false;
     if (!ensureGpu()) return 0.0;
@@ -326,19 +350,46 @@ void ophPointCloud::encoding(unsigned int flag) {
     const uint nch = context_.waveNum;
     if (!ensureDevice(cap_v_ ? cap_v_ : 1, sizeof(double) * 2 * plane * nch, sizeof(double) * plane * nch, plane * nch))
         return;
-    for (uint ch = 0; ch < nch; ++ch)
-        cudaMemcpy((double*)d_field_ + 2 * plane * ch, complex_H_[ch], sizeof(double) * 2 * plane, cudaMemcpyHostToDevice);
-    // Burckhardt and TwoPhase leave some entries of m_lpEncoded as they were
-    if (flag == ENCODE_BURCKHARDT || flag == ENCODE_TWOPHASE)
-        for (uint ch = 0; ch < nch; ++ch)
-            cudaMemcpy((double*)d_encoded_ + plane * ch, encoded_[ch], sizeof(double) * plane, cudaMemcpyHostToDevice);
-    if (ophpc_encode(gpu_, (const double*)d_field_, nch, plane, flag, (double*)d_encoded_, nullptr, nullptr) !=
-        OPHPC_SUCCESS) {
-        last_error_ = std::string("encode: ") + ophpc_last_error(gpu_);
-        return;
+    // Every encoder works on one channel at a time (the normalising ones by
+    // the channel's own largest magnitude), so the channels run as a
+    // pipeline, one stream each: the upload of one overlaps the encoding and
+    // the download of the one before.
+    for (uint ch = 0; ch < nch; ++ch) {
+        cudaStream_t st = nullptr;
+        if (!streams_[ch]) {
+            if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+                cudaGetLastError();
+                last_error_ = "stream creation failed";
+                return;
+            }
+            streams_[ch] = st;
+        }
+    }
+    cudaDeviceSynchronize();   // earlier work on the field buffers (legacy stream) is done
+    bool ok = true;
+    std::string err;
+    for (uint ch = 0; ch < nch && ok; ++ch) {
+        cudaStream_t st = (cudaStream_t)streams_[ch];
+        double* df = (double*)d_field_ + 2 * plane * ch;
+        double* de = (double*)d_encoded_ + plane * ch;
+        ok = cudaMemcpyAsync(df, complex_H_[ch], sizeof(double) * 2 * plane, cudaMemcpyHostToDevice, st) ==
+             cudaSuccess;
+        // Burckhardt and TwoPhase leave some entries of m_lpEncoded as they were
+        if (ok && (flag == ENCODE_BURCKHARDT || flag == ENCODE_TWOPHASE))
+            ok = cudaMemcpyAsync(de, encoded_[ch], sizeof(double) * plane, cudaMemcpyHostToDevice, st) == cudaSuccess;
+        if (ok && ophpc_encode(gpu_, df, 1, plane, flag, de, nullptr, st) != OPHPC_SUCCESS) {
+            err = std::string("encode: ") + ophpc_last_error(gpu_);
+            ok = false;
+        }
+        if (ok) ok = cudaMemcpyAsync(encoded_[ch], de, sizeof(double) * plane, cudaMemcpyDeviceToHost, st) == cudaSuccess;
     }
     for (uint ch = 0; ch < nch; ++ch)
-        cudaMemcpy(encoded_[ch], (double*)d_encoded_ + plane * ch, sizeof(double) * plane, cudaMemcpyDeviceToHost);
+        if (cudaStreamSynchronize((cudaStream_t)streams_[ch]) != cudaSuccess) ok = false;
+    if (!ok) {
+        cudaGetLastError();
+        last_error_ = err.empty() ? std::string("encode copies failed") : err;
+        return;
+    }
     encoded_valid_ = true;
 }
 
