@@ -426,20 +426,31 @@ __global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restric
     }
 }
 
-// The code of one pixel from its cached estimate e (NaN: none), in FP64
-// where the estimate is within its error margin of a code boundary: the
-// rule of est_codes_kernel, so the codes are the same bit for bit.
-template <int FLAG>
-__device__ __forceinline__ uint32_t code_of(float e, const double2* __restrict__ px, bool usable, float mn_f,
-                                            float sc_f, float margin, double gmn, double gap) {
+// The code of one pixel from its cached estimate e (NaN: none) when the
+// estimate decides it: false where it lies within its error margin of a
+// code boundary (or there is none), and code_exact then computes it in
+// FP64. This is est_codes_kernel's rule, so the codes are the same bit for
+// bit.
+__device__ __forceinline__ bool code_fast(float e, bool usable, float mn_f, float sc_f, float margin,
+                                          uint32_t& code) {
     const float v = (e - mn_f) * sc_f + 0.5f;
     const float fl = floorf(v);
-    if (usable && e == e && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f)
-        return (uint32_t)(int)fl;
+    code = (uint32_t)(int)fl;
+    return usable && e == e && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f;
+}
+template <int FLAG>
+__device__ __forceinline__ uint32_t code_exact(const double2* __restrict__ px, double gmn, double gap) {
     const double x = encode_value(*px, FLAG);
     const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(x, gmn), gap), 255.0), 0.5);
     return (val >= 0.0 && val < 256.0) ? (uint32_t)(int)val : 0u;
 }
+
+// Pixels of a CTA that need FP64 (band pixels before the barrier, boundary
+// pixels after it) are listed in shared memory and computed together, one
+// per thread, instead of where a thread meets them: the FP64 pipe then runs
+// a few full warps rather than many warps with one lane each. A list that
+// fills up leaves the rest to be computed where they are met.
+constexpr int kFp64List = 512;
 
 // Single pass of the codes, for fields whose FP32 estimates fit in the
 // shared memory of the CTAs the GPU holds at once (cooperative launch):
@@ -455,7 +466,8 @@ __device__ __forceinline__ uint32_t code_of(float e, const double2* __restrict__
 //   3. waits at a grid barrier (all CTAs are resident; the wait is bounded by
 //      %globaltimer and records a timeout in word [4], after which the CTA
 //      writes zero codes);
-//   4. writes every code from its cached estimate (code_of).
+//   4. writes every code its cached estimate decides (code_fast), then the
+//      others in FP64 (code_exact).
 // The field is read once (plus the few FP64 pixels); words [3] and [4]
 // (barrier count, timeout) are zeroed by init_est_minmax_kernel. `out` is
 // 4-byte aligned.
@@ -464,8 +476,10 @@ __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restr
                                                           unsigned long long* __restrict__ minmax,
                                                           uint8_t* __restrict__ out) {
     extern __shared__ float4 s_est4[];
-    float* s_est = reinterpret_cast<float*>(s_est4);
     __shared__ float s_red[2][8];
+    __shared__ int s_list[kFp64List];
+    __shared__ int s_nlist;
+    if (threadIdx.x == 0) s_nlist = 0;
     const int64_t base = (int64_t)blockIdx.x * per;
     const int cnt = base < n ? (int)min(per, n - base) : 0;
     const double2* fb = field + base;
@@ -516,17 +530,29 @@ __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restr
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
             if (e[k] == e[k] && (e[k] <= mn + band || e[k] >= mx - band)) {
-                const double x = encode_value(fb[j + k], FLAG);
-                if (x < emn) emn = x;
-                if (x > emx) emx = x;
+                const int slot = atomicAdd(&s_nlist, 1);
+                if (slot < kFp64List) {
+                    s_list[slot] = j + k;
+                } else {
+                    const double x = encode_value(fb[j + k], FLAG);
+                    if (x < emn) emn = x;
+                    if (x > emx) emx = x;
+                }
             }
         }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < min(s_nlist, kFp64List); i += blockDim.x) {
+        const double x = encode_value(fb[s_list[i]], FLAG);
+        if (x < emn) emn = x;
+        if (x > emx) emx = x;
     }
     fold_exact(emn, emx, minmax);
     // grid barrier
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
+        s_nlist = 0;   // the list again, for the boundary pixels
         __threadfence();
         atomicAdd(&minmax[3], 1ull);
         const uint64_t t0 = global_ns_enc();
@@ -557,14 +583,28 @@ __global__ void __launch_bounds__(256) fused_codes_kernel(const double2* __restr
         uint32_t c[4] = {0u, 0u, 0u, 0u};
         if (s_ok) {
 #pragma unroll
-            for (int k = 0; k < 4; ++k)
-                if (j + k < cnt) c[k] = code_of<FLAG>(e[k], fb + j + k, usable, mn_f, sc_f, margin, gmn, gap);
+            for (int k = 0; k < 4; ++k) {
+                if (j + k < cnt && !code_fast(e[k], usable, mn_f, sc_f, margin, c[k])) {
+                    const int slot = atomicAdd(&s_nlist, 1);
+                    if (slot < kFp64List) {
+                        s_list[slot] = j + k;
+                        c[k] = 0u;   // written below
+                    } else {
+                        c[k] = code_exact<FLAG>(fb + j + k, gmn, gap);
+                    }
+                }
+            }
         }
         if (j + 4 <= cnt) {
             *reinterpret_cast<uint32_t*>(ob + j) = c[0] | c[1] << 8 | c[2] << 16 | c[3] << 24;
         } else {
             for (int k = 0; j + k < cnt; ++k) ob[j + k] = (uint8_t)c[k];
         }
+    }
+    __syncthreads();   // orders the 4-byte stores above before the byte stores below
+    for (int i = threadIdx.x; i < min(s_nlist, kFp64List); i += blockDim.x) {
+        const int j = s_list[i];
+        ob[j] = (uint8_t)code_exact<FLAG>(fb + j, gmn, gap);
     }
 }
 
