@@ -373,59 +373,6 @@ __device__ __forceinline__ float est_band(float mx_est) {
     return FLAG == 0 ? 2.f * kPhaseErr : 2.f * kAmpErrRel * fabsf(mx_est);
 }
 
-// pass 2: the exact value of every pixel whose estimate is within the band
-// of the estimated min or max
-template <int FLAG>
-__global__ void __launch_bounds__(256) refine_minmax_kernel(const double2* __restrict__ field, int64_t n,
-                                                            unsigned long long* __restrict__ minmax) {
-    const unsigned* w = reinterpret_cast<const unsigned*>(minmax + 2);
-    const float mn_e = from_ordered32(w[0]), mx_e = from_ordered32(w[1]);
-    const float band = est_band<FLAG>(mx_e);
-    double emn = kMaxDouble, emx = kMinDouble;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 h = field[i];
-        bool ok;
-        const float e = estimate<FLAG>(h, ok);
-        if (ok && (e <= mn_e + band || e >= mx_e - band)) {
-            const double x = encode_value(h, FLAG);
-            if (x < emn) emn = x;
-            if (x > emx) emx = x;
-        }
-    }
-    fold_exact(emn, emx, minmax);
-}
-
-// pass 3: the codes
-template <int FLAG>
-__global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restrict__ field, int64_t n,
-                                                        const unsigned long long* __restrict__ minmax,
-                                                        uint8_t* __restrict__ out) {
-    const double mn = from_ordered(minmax[0]);
-    const double mx = from_ordered(minmax[1]);
-    const double gap = __dsub_rn(mx, mn);
-    const bool usable = gap > 0.0 && gap < 1e30 && mn > -1e30 && mn < 1e30;
-    const float mn_f = (float)mn, sc_f = usable ? (float)(255.0 / gap) : 0.f;
-    const float err = FLAG == 0 ? kPhaseErr : kAmpErrRel * (float)fmax(fabs(mx), fabs(mn));
-    // estimate error in code units, the FP32 rounding of the code itself on top
-    const float margin = 2.f * err * sc_f + 1e-4f;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double2 h = field[i];
-        bool ok;
-        const float e = estimate<FLAG>(h, ok);
-        const float v = (e - mn_f) * sc_f + 0.5f;
-        const float fl = floorf(v);
-        uint8_t code;
-        if (usable && ok && v - fl > margin && fl + 1.f - v > margin && fl >= 0.f && fl <= 255.f) {
-            code = (uint8_t)(int)fl;
-        } else {
-            const double x = encode_value(h, FLAG);
-            const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(x, mn), gap), 255.0), 0.5);
-            code = (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
-        }
-        out[i] = code;
-    }
-}
-
 // The code of one pixel from its cached estimate e (NaN: none) when the
 // estimate decides it: false where it lies within its error margin of a
 // code boundary (or there is none), and code_exact then computes it in
@@ -451,6 +398,80 @@ __device__ __forceinline__ uint32_t code_exact(const double2* __restrict__ px, d
 // a few full warps rather than many warps with one lane each. A list that
 // fills up leaves the rest to be computed where they are met.
 constexpr int kFp64List = 512;
+
+// pass 2: the exact value of every pixel whose estimate is within the band
+// of the estimated min or max
+template <int FLAG>
+__global__ void __launch_bounds__(256) refine_minmax_kernel(const double2* __restrict__ field, int64_t n,
+                                                            unsigned long long* __restrict__ minmax) {
+    __shared__ int64_t s_list[kFp64List];
+    __shared__ int s_nlist;
+    if (threadIdx.x == 0) s_nlist = 0;
+    __syncthreads();
+    const unsigned* w = reinterpret_cast<const unsigned*>(minmax + 2);
+    const float mn_e = from_ordered32(w[0]), mx_e = from_ordered32(w[1]);
+    const float band = est_band<FLAG>(mx_e);
+    double emn = kMaxDouble, emx = kMinDouble;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double2 h = field[i];
+        bool ok;
+        const float e = estimate<FLAG>(h, ok);
+        if (ok && (e <= mn_e + band || e >= mx_e - band)) {
+            const int slot = atomicAdd(&s_nlist, 1);
+            if (slot < kFp64List) {
+                s_list[slot] = i;
+            } else {
+                const double x = encode_value(h, FLAG);
+                if (x < emn) emn = x;
+                if (x > emx) emx = x;
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < min(s_nlist, kFp64List); k += blockDim.x) {
+        const double x = encode_value(field[s_list[k]], FLAG);
+        if (x < emn) emn = x;
+        if (x > emx) emx = x;
+    }
+    fold_exact(emn, emx, minmax);
+}
+
+// pass 3: the codes
+template <int FLAG>
+__global__ void __launch_bounds__(256) est_codes_kernel(const double2* __restrict__ field, int64_t n,
+                                                        const unsigned long long* __restrict__ minmax,
+                                                        uint8_t* __restrict__ out) {
+    const double mn = from_ordered(minmax[0]);
+    const double mx = from_ordered(minmax[1]);
+    const double gap = __dsub_rn(mx, mn);
+    const bool usable = gap > 0.0 && gap < 1e30 && mn > -1e30 && mn < 1e30;
+    const float mn_f = (float)mn, sc_f = usable ? (float)(255.0 / gap) : 0.f;
+    const float err = FLAG == 0 ? kPhaseErr : kAmpErrRel * (float)fmax(fabs(mx), fabs(mn));
+    // estimate error in code units, the FP32 rounding of the code itself on top
+    const float margin = 2.f * err * sc_f + 1e-4f;
+    __shared__ int64_t s_list[kFp64List];
+    __shared__ int s_nlist;
+    if (threadIdx.x == 0) s_nlist = 0;
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        bool ok;
+        const float e = estimate<FLAG>(field[i], ok);
+        uint32_t code;
+        if (!code_fast(ok ? e : __int_as_float(0x7fc00000), usable, mn_f, sc_f, margin, code)) {
+            const int slot = atomicAdd(&s_nlist, 1);
+            if (slot < kFp64List) {
+                s_list[slot] = i;
+                code = 0u;   // written below
+            } else {
+                code = code_exact<FLAG>(field + i, mn, gap);
+            }
+        }
+        out[i] = (uint8_t)code;
+    }
+    __syncthreads();   // orders the stores above before those below
+    for (int k = threadIdx.x; k < min(s_nlist, kFp64List); k += blockDim.x)
+        out[s_list[k]] = (uint8_t)code_exact<FLAG>(field + s_list[k], mn, gap);
+}
 
 // Single pass of the codes, for fields whose FP32 estimates fit in the
 // shared memory of the CTAs the GPU holds at once (cooperative launch):
