@@ -311,8 +311,13 @@ def serving_leg(n_jobs: int, max_points: int, loads=(0.5, 0.8, 0.95), seed: int 
         slow = lat / iso
         arr_rel = arrivals - arrivals[0]
         p99_iso = float(np.percentile(iso, 99))
+        # the same, and with the jobs above the isolated p99 deferred behind
+        # all others (the top 1 % may be late without moving the p99)
         model = {"fcfs_p99_over_isolated_p99": single_server_p99(iso, arr_rel, lambda q, a: a) / p99_iso,
                  "edf_p99_over_isolated_p99": single_server_p99(iso, arr_rel, lambda q, a: a + 2 * iso[q] + 0.02)
+                 / p99_iso,
+                 "edf_largest_last_p99_over_isolated_p99": single_server_p99(
+                     iso, arr_rel, lambda q, a: (1e9 if iso[q] > p99_iso else 0.0) + a + 2 * iso[q] + 0.02)
                  / p99_iso}
         return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
                 "single_server_model": model,
