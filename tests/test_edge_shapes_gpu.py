@@ -43,3 +43,21 @@ def test_degenerate_shapes(gpu_ctx, oracle_mod, pnx, pny, name, diff, mode, tol)
     err = rel_l2(got, want)
     print(f"{name} {pnx}x{pny}: relL2 {err:.3e}")
     assert err <= tol
+
+
+@pytest.mark.parametrize("name,diff,mode,tol", PATHS)
+def test_points_behind_the_slm(gpu_ctx, oracle_mod, name, diff, mode, tol):
+    """Negative depths (points behind the SLM, z in [-0.3, -0.2] m) and a
+    mix of both signs: the reference's windows use |z| and its amplitudes
+    and phases carry the sign (ophGen.cpp:361-514)."""
+    pp = 8e-6
+    gk = dict(pnx=200, pny=136, ppx=pp, ppy=pp, wavelengths=[532e-9])
+    g = oracle_mod.Geometry(pnx=200, pny=136, ppx=pp, ppy=pp, wavelengths=[532e-9])
+    v = _points(600, 77 + diff, (1e-3, 1e-3))
+    v[:, 2] = -v[:, 2]
+    v[::3, 2] = -v[::3, 2]   # every third point in front again
+    want = oracle_mod.generate(g, v, diff)
+    got = run_generate(gpu_ctx, gk, v, diff, mode)
+    err = rel_l2(got, want)
+    print(f"{name} behind the SLM: relL2 {err:.3e}")
+    assert err <= tol
