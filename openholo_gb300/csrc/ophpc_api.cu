@@ -255,9 +255,9 @@ ophpc_status tc_generate_accumulate(ophpc_context* ctx, const JobGeom& jg, const
     float* amax = (float*)(mem + rec_bytes + left_bytes + mask_bytes);   // [4] words, then the error word
     int* errw = (int*)(amax + 4);
     e = cudaMemsetAsync(amax, 0, 32, s);
-    launch_prep(d_vertices, n, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window, (int)diff_flag, jg,
-                recs, s, color_offset);
     if (e == cudaSuccess) {
+        launch_prep(d_vertices, n, cfg->scale, cfg->distance, cfg->field_length, cfg->viewing_window,
+                    (int)diff_flag, jg, recs, s, color_offset);
         if (rs) {
             launch_rs_amax(recs, n, nch, pnx, pny, amax, s);
             e = launch_tc_rs_range(jg, recs, 0, n, true, (double2*)d_field, amax, left, mask,
