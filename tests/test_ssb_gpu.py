@@ -169,3 +169,18 @@ def test_sideband_matches_oracle(gpu_ctx, oracle_mod, pnx, pny, passband):
     codes_ref, _, _ = oracle_mod.normalize(want.reshape(2, -1))
     exact, maxd = code_agreement(codes, codes_ref.reshape(2, -1), False)
     assert exact >= 0.9999 and maxd <= 1
+
+
+def test_ssb_encoders_on_an_empty_field(gpu_ctx, oracle_mod):
+    """A field of zeros (no point reached the SLM): every encoder returns
+    what the oracle returns, all finite (oph::normalize's max starts at
+    MIN_DOUBLE, so a constant field normalises to 0, not NaN)."""
+    field = np.zeros((2, 27, 40), dtype=np.complex128)
+    for flag, pb in ((SSB, 0), (OFFSSB, 1), (OFFSSB, 3)):
+        enc, codes = _run(gpu_ctx, field, 8e-6, 8e-6, flag, pb)
+        want = oracle_mod.ssb_encode(field, 8e-6, 8e-6, flag, pb)
+        assert np.all(np.isfinite(enc)) and np.array_equal(enc, want), (flag, pb)
+        assert not np.any(codes)
+    for pb in range(4):
+        enc, _ = _sideband(gpu_ctx, field, 8e-6, 8e-6, pb)
+        assert not np.any(enc)
