@@ -500,10 +500,9 @@ def extra_workload_leg(ctx, w, variants, steps: int) -> dict:
         out[name] = {"value": w.interactions / t, "unit": UNIT, "ms_per_generate": t * 1e3}
     del dv, f, flush
     torch.cuda.empty_cache()
-    if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
-        for name, diff, mode in variants:
-            out[name]["relL2_vs_fp64"] = relL2_at_pixels(ctx, w, diff, mode)
-        out["relL2_samples"] = f"all {w.n_points} points at 256 seeded pixels per channel (FP64 oracle)"
+    for name, diff, mode in variants:
+        out[name]["relL2_vs_fp64"] = relL2_at_pixels(ctx, w, diff, mode)
+    out["relL2_samples"] = f"all {w.n_points} points at 256 seeded pixels per channel (FP64 oracle)"
     return out
 
 
@@ -570,13 +569,12 @@ def wrp_leg(ctx, steps: int) -> dict:
         res = {"pnx": kw["pnx"], "pny": kw["pny"], "channels": cfg.n_channels, "n_points": int(v.shape[0]),
                "splat_half_width_px": wsq, "ms_per_hologram": t * 1e3, "holograms_per_s": 1.0 / t,
                "note": "synchronises once per call to read the depth range"}
-        if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
-            t0 = time.perf_counter()
-            want = oracle.wrp_generate(g, v)
-            res["oracle_cpu_s"] = time.perf_counter() - t0
-            h = f.cpu().numpy()
-            got = h[..., 0] + 1j * h[..., 1]
-            res["relL2_vs_fp64"] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+        t0 = time.perf_counter()
+        want = oracle.wrp_generate(g, v)
+        res["oracle_cpu_s"] = time.perf_counter() - t0
+        h = f.cpu().numpy()
+        got = h[..., 0] + 1j * h[..., 1]
+        res["relL2_vs_fp64"] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
         out[name] = res
         del dv, f
     return out
@@ -728,39 +726,36 @@ def gpu_arm(args, w):
         return res
 
     tensor = {"sphere_fhd": tensor_leg(w, dv, cfg, field, max(3, args.steps // 2))}
-    if os.environ.get("OPHPC_BENCH_SKIP_4K") != "1":
-        from openholo_gb300 import workloads as W
-        w4 = W.box_4k()
-        cfg4 = oph.make_config(**w4.geometry_kwargs())
-        dv4 = torch.from_numpy(w4.vertices).cuda()
-        f4 = torch.empty((1, w4.pny, w4.pnx, 2), dtype=torch.float64, device="cuda")
-        tensor["box_4k"] = tensor_leg(w4, dv4, cfg4, f4, 2)
-        del dv4, f4
-        if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
-            for name, mode in (("fp16", oph.MODE_TENSOR_FP16), ("bf16x3", oph.MODE_TENSOR_BF16X3)):
-                tensor["box_4k"][name]["relL2_vs_fp64"] = relL2_at_pixels(ctx, w4, 1, mode)
-            tensor["box_4k"]["relL2_vs_fp64_samples"] = "all 1,000,000 points at 256 seeded pixels (FP64 oracle)"
+    from openholo_gb300 import workloads as W
+    w4 = W.box_4k()
+    cfg4 = oph.make_config(**w4.geometry_kwargs())
+    dv4 = torch.from_numpy(w4.vertices).cuda()
+    f4 = torch.empty((1, w4.pny, w4.pnx, 2), dtype=torch.float64, device="cuda")
+    tensor["box_4k"] = tensor_leg(w4, dv4, cfg4, f4, 2)
+    del dv4, f4
+    for name, mode in (("fp16", oph.MODE_TENSOR_FP16), ("bf16x3", oph.MODE_TENSOR_BF16X3)):
+        tensor["box_4k"][name]["relL2_vs_fp64"] = relL2_at_pixels(ctx, w4, 1, mode)
+    tensor["box_4k"]["relL2_vs_fp64_samples"] = "all 1,000,000 points at 256 seeded pixels (FP64 oracle)"
 
     # the other benchmark workloads: rs_1k (1024x1024, 5,000 points) and
     # box_8k (7680x4320, 2,000,000 points; tensor-core RS only: the FP32-core
     # kernel would take ~30 s a call)
     from openholo_gb300 import workloads as W
     more = {}
-    if os.environ.get("OPHPC_BENCH_SKIP_MORE") != "1":
-        more["rs_1k"] = extra_workload_leg(ctx, W.rs_1k(), [("rs_plain", 0, 0), ("rs_tc_bf16x3", 0, rs_mode),
-                                                             ("fresnel_plain", 1, 0),
-                                                             ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3)],
-                                           max(3, args.steps // 2))
-        more["box_8k"] = extra_workload_leg(ctx, W.box_8k(), [("rs_tc_bf16x3", 0, rs_mode)], 2)
+    more["rs_1k"] = extra_workload_leg(ctx, W.rs_1k(), [("rs_plain", 0, 0), ("rs_tc_bf16x3", 0, rs_mode),
+                                                         ("fresnel_plain", 1, 0),
+                                                         ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3)],
+                                       max(3, args.steps // 2))
+    more["box_8k"] = extra_workload_leg(ctx, W.box_8k(), [("rs_tc_bf16x3", 0, rs_mode)], 2)
     wrp = None
-    if os.environ.get("OPHPC_BENCH_SKIP_MORE") != "1" and rank == 0:
+    if rank == 0:
         wrp = wrp_leg(ctx, max(3, args.steps // 2))
     codes_full = None
-    if os.environ.get("OPHPC_BENCH_SKIP_FULLCODES") != "1" and rank == 0:
+    if rank == 0:
         codes_full = full_field_codes(ctx, w, rs_mode)
 
     serving = None
-    if os.environ.get("OPHPC_BENCH_SKIP_SERVING") != "1" and world == 1:
+    if world == 1:
         serving = serving_leg(args.serving_jobs, args.serving_max_points)
     plan_replay = plan_leg(ctx, sp)
 
@@ -797,64 +792,63 @@ def gpu_arm(args, w):
         cpu = None
         rel = None
         rel_fp64 = {}
-        if os.environ.get("OPHPC_BENCH_SKIP_CPU") != "1":
-            # cpu_baseline leg: the CPU point-cloud path on a bounded sample of
-            # the same workload, and the GPU result on that sample checked
-            # against it (relative L2 error, FP64 CPU result as reference).
-            n_cpu = args.cpu_points or 300
-            rate, secs, kind, ref_field = cpu_sample_run(w, n_cpu, 0)
-            sub = w.subset(n_cpu)
-            dsub = torch.from_numpy(sub.vertices).cuda()
-            fsub = torch.empty_like(field)
-            ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, rs_mode, fsub.data_ptr(), sp)
+        # cpu_baseline leg: the CPU point-cloud path on a bounded sample of
+        # the same workload, and the GPU result on that sample checked
+        # against it (relative L2 error, FP64 CPU result as reference).
+        n_cpu = args.cpu_points or 300
+        rate, secs, kind, ref_field = cpu_sample_run(w, n_cpu, 0)
+        sub = w.subset(n_cpu)
+        dsub = torch.from_numpy(sub.vertices).cuda()
+        fsub = torch.empty_like(field)
+        ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, rs_mode, fsub.data_ptr(), sp)
+        torch.cuda.synchronize()
+        g = fsub.cpu().numpy()
+        got = g[..., 0] + 1j * g[..., 1]
+        rel = float(np.linalg.norm(got - ref_field) / np.linalg.norm(ref_field))
+        # every Fresnel variant against the FP64 CPU field on a smaller sample
+        n_fr = max(50, n_cpu // 3)
+        _, _, _, ref_fr = cpu_sample_run(w, n_fr, 1)
+        subf = w.subset(n_fr)
+        dsubf = torch.from_numpy(subf.vertices).cuda()
+        for name, mode in (("fresnel_plain", 0), ("fresnel_tc_fp16", oph.MODE_TENSOR_FP16),
+                           ("fresnel_tc_bf16x3", oph.MODE_TENSOR_BF16X3)):
+            ctx.generate(cfg, dsubf.data_ptr(), subf.n_points, oph.DIFF_FRESNEL, mode, fsub.data_ptr(), sp)
             torch.cuda.synchronize()
             g = fsub.cpu().numpy()
             got = g[..., 0] + 1j * g[..., 1]
-            rel = float(np.linalg.norm(got - ref_field) / np.linalg.norm(ref_field))
-            # every Fresnel variant against the FP64 CPU field on a smaller sample
-            n_fr = max(50, n_cpu // 3)
-            _, _, _, ref_fr = cpu_sample_run(w, n_fr, 1)
-            subf = w.subset(n_fr)
-            dsubf = torch.from_numpy(subf.vertices).cuda()
-            for name, mode in (("fresnel_plain", 0), ("fresnel_tc_fp16", oph.MODE_TENSOR_FP16),
-                               ("fresnel_tc_bf16x3", oph.MODE_TENSOR_BF16X3)):
-                ctx.generate(cfg, dsubf.data_ptr(), subf.n_points, oph.DIFF_FRESNEL, mode, fsub.data_ptr(), sp)
-                torch.cuda.synchronize()
-                g = fsub.cpu().numpy()
-                got = g[..., 0] + 1j * g[..., 1]
-                rel_fp64[name] = float(np.linalg.norm(got - ref_fr) / np.linalg.norm(ref_fr))
-            rel_fp64["rs_tc_bf16x3"] = rel
-            ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, 0, fsub.data_ptr(), sp)
+            rel_fp64[name] = float(np.linalg.norm(got - ref_fr) / np.linalg.norm(ref_fr))
+        rel_fp64["rs_tc_bf16x3"] = rel
+        ctx.generate(cfg, dsub.data_ptr(), sub.n_points, oph.DIFF_RS, 0, fsub.data_ptr(), sp)
+        torch.cuda.synchronize()
+        g = fsub.cpu().numpy()
+        rel_fp64["rs_plain"] = float(np.linalg.norm(g[..., 0] + 1j * g[..., 1] - ref_field) /
+                                     np.linalg.norm(ref_field))
+        rel_fp64["samples"] = f"RS {n_cpu} points, Fresnel {n_fr} points, full {w.pnx}x{w.pny}x{w.n_channels}"
+        # all points at seeded pixels: the error at the workload's full
+        # size (it grows with the point count: part of it is common to
+        # every point's phase)
+        import oracle
+        gw = oracle.Geometry(pnx=w.pnx, pny=w.pny, ppx=w.pp, ppy=w.pp, wavelengths=list(w.wavelengths),
+                             scale=w.scale, distance=w.distance)
+        pix = np.sort(np.random.default_rng(17).choice(npx, 256, replace=False))
+        full, wants = {}, {}
+        for name, diff, mode in (("rs_tc_bf16x3", 0, rs_mode), ("rs_plain", 0, 0), ("fresnel_plain", 1, 0),
+                                 ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3),
+                                 ("fresnel_tc_fp16", 1, oph.MODE_TENSOR_FP16)):
+            ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, fsub.data_ptr(), sp)
             torch.cuda.synchronize()
-            g = fsub.cpu().numpy()
-            rel_fp64["rs_plain"] = float(np.linalg.norm(g[..., 0] + 1j * g[..., 1] - ref_field) /
-                                         np.linalg.norm(ref_field))
-            rel_fp64["samples"] = f"RS {n_cpu} points, Fresnel {n_fr} points, full {w.pnx}x{w.pny}x{w.n_channels}"
-            # all points at seeded pixels: the error at the workload's full
-            # size (it grows with the point count: part of it is common to
-            # every point's phase)
-            import oracle
-            gw = oracle.Geometry(pnx=w.pnx, pny=w.pny, ppx=w.pp, ppy=w.pp, wavelengths=list(w.wavelengths),
-                                 scale=w.scale, distance=w.distance)
-            pix = np.sort(np.random.default_rng(17).choice(npx, 256, replace=False))
-            full, wants = {}, {}
-            for name, diff, mode in (("rs_tc_bf16x3", 0, rs_mode), ("rs_plain", 0, 0), ("fresnel_plain", 1, 0),
-                                     ("fresnel_tc_bf16x3", 1, oph.MODE_TENSOR_BF16X3),
-                                     ("fresnel_tc_fp16", 1, oph.MODE_TENSOR_FP16)):
-                ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, fsub.data_ptr(), sp)
-                torch.cuda.synchronize()
-                g = fsub.reshape(nch, npx, 2)[:, torch.from_numpy(pix).cuda()].cpu().numpy()
-                got = g[..., 0] + 1j * g[..., 1]
-                if diff not in wants:
-                    wants[diff] = np.stack([oracle.field_at(gw, w.vertices, diff, c, pix) for c in range(nch)])
-                want = wants[diff]
-                full[name] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
-            full["samples"] = f"all {w.n_points} points at 256 seeded pixels per channel"
-            rel_fp64["full_size"] = full
-            cpu = {"value": rate, "unit": UNIT, "cores": host_cores(), "kind": kind,
-                   "sample": f"{n_cpu} of {w.n_points} points at full {w.pnx}x{w.pny}, {w.n_channels} channels, RS "
-                             f"({secs:.1f} s, OpenMP, {cpu_model()})",
-                   "relL2_gpu_vs_cpu_on_sample": rel}
+            g = fsub.reshape(nch, npx, 2)[:, torch.from_numpy(pix).cuda()].cpu().numpy()
+            got = g[..., 0] + 1j * g[..., 1]
+            if diff not in wants:
+                wants[diff] = np.stack([oracle.field_at(gw, w.vertices, diff, c, pix) for c in range(nch)])
+            want = wants[diff]
+            full[name] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+        full["samples"] = f"all {w.n_points} points at 256 seeded pixels per channel"
+        rel_fp64["full_size"] = full
+        cpu = {"value": rate, "unit": UNIT, "cores": host_cores(), "kind": kind,
+               "sample": f"{n_cpu} of {w.n_points} points at full {w.pnx}x{w.pny}, {w.n_channels} channels, RS "
+                         f"({secs:.1f} s, OpenMP, {cpu_model()})",
+               "relL2_gpu_vs_cpu_on_sample": rel}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True, "scaling": "weak",
