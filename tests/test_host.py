@@ -132,6 +132,37 @@ def test_public_headers_compile(tmp_path, lang):
         assert r.returncode == 0, (h, r.stderr)
 
 
+def test_reference_example_program_builds_unchanged(tmp_path):
+    """The reference's own example program (Example/examPointCloud/
+    examPointCloud.cpp, read where it lies in the reference's source tree,
+    not copied) compiles against include/ophPointCloud.h and links to
+    libophpc.so with no edit to it. The one flag it needs on GCC is
+    `-include experimental/filesystem`: the file names
+    std::experimental::filesystem after including <filesystem>, which MSVC
+    declares there and libstdc++ declares in <experimental/filesystem>.
+    Running it needs a GPU (tests/test_cpp_dropin_gpu.py runs the same call
+    sequence there)."""
+    import shutil
+
+    import oracle
+    src = os.path.join(oracle.REFERENCE_TREE, "Example", "examPointCloud", "examPointCloud.cpp")
+    if not os.path.isfile(src):
+        pytest.skip("the reference's source tree is not on this machine")
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    libdir = os.path.dirname(oph.lib_path())
+    exe = str(tmp_path / "examPointCloud")
+    r = subprocess.run([gxx, "-std=c++17", "-include", "experimental/filesystem", "-I",
+                        os.path.join(ROOT, "include"), src, "-L", libdir, "-lophpc", "-Wl,-rpath," + libdir,
+                        "-Wl,--no-undefined", "-lstdc++fs", "-o", exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nm = subprocess.run(["nm", "-uC", exe], capture_output=True, text=True)
+    if nm.returncode == 0:
+        used = [ln for ln in nm.stdout.splitlines() if "ophPointCloud::" in ln]
+        assert any("generateHologram" in ln for ln in used), nm.stdout
+
+
 def test_reference_launcher_reports_status_without_crashing():
     """cudaPointCloud_RS with the reference's signature: no config -> a
     status on the calling thread (no device here: NO_DEVICE; with one:
