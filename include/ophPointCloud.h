@@ -187,6 +187,7 @@ private:
     void freeBuffers();
     bool ensureGpu();
     bool ensureDevice(size_t bytes_vertices, size_t bytes_field, size_t bytes_encoded, size_t bytes_codes);
+    bool ensureStreams();
     void encodeSideband(unsigned int flag, unsigned int passband, Real shift_x, Real shift_y);
 
     OphConfig context_;
@@ -203,6 +204,7 @@ private:
     ulonglong n_points_ = 0;
     Vertex* vertices_ = nullptr;
     ulonglong vertices_cap_ = 0;   /* records vertices_ holds */
+    bool vertices_pinned_ = false; /* vertices_ is page-locked (cudaHostAlloc) */
     Complex<Real>** complex_H_ = nullptr;
     Real** encoded_ = nullptr;
     uchar** normalized_ = nullptr;

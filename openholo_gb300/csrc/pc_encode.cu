@@ -29,12 +29,126 @@ constexpr double kPi = 3.14159265358979323846;
 constexpr double kMaxDouble = 1.7976931348623158e+308;
 constexpr double kMinDouble = 2.2250738585072014e-308;
 
+// FP32 image of a double from its high word: sign, exponent, the top 20
+// mantissa bits (truncated: relative error < 2^-20). ok turns false where
+// the image cannot stand in: subnormal, or outside 2^-62 .. 2^62 (squares
+// stay normal floats), infinite or NaN.
+__device__ __forceinline__ float hi_float(double d, bool& ok) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const unsigned hi = (unsigned)(b >> 32);
+    const int ex = (int)((hi >> 20) & 0x7ffu);
+    const unsigned sign = hi & 0x80000000u;
+    if (ex == 0) {
+        if ((hi & 0xfffffu) | (unsigned)b) ok = false;   // subnormal
+        return __int_as_float((int)sign);                  // signed zero, as atan2 sees it
+    }
+    if (ex < 1023 - 62 || ex > 1023 + 62) {
+        ok = false;
+        return 0.f;
+    }
+    return __int_as_float((int)(sign | ((unsigned)(ex - 1023 + 127) << 23) | ((hi & 0xfffffu) << 3)));
+}
+
+// ---- the phase encoder's value -----------------------------------------------
+// (atan2(y, x) + pi) / (2 pi) with a table-driven atan2 (argument reduction
+// by a tabulated angle, then the Maclaurin series of atan): about 19 FP64
+// operations, where CUDA's atan2 and a divide take several times that on
+// GB300's narrow FP64 pipe. An FP32 estimate (atan2f of the high words)
+// picks the nearest tabulated angle theta_k = fl(k pi / 128),
+// k = -128..128. Rotating (x, y) by -theta_k with the table's FP64 cos and
+// sin leaves a = |z| cos(delta) > 0 and b = |z| sin(delta),
+// |delta| <= pi / 256 plus the estimate's error, so |t| = |b / a| < 0.0123
+// and delta = atan(t) = t - t^3/3 + t^5/5 - t^7/7, the first omitted term
+// below 1e-18. theta = theta_k + delta lies within a few 1e-16 rad of the
+// correctly rounded atan2, and then goes through the reference's
+// (theta + pi) / (2 pi), the division as a product with the reciprocal and
+// one FMA residual step (Markstein's correction for a quotient). Zeros on
+// both axes, subnormal, huge and non-finite inputs take CUDA's atan2.
+struct AtanTable {
+    double c[257], s[257], th[257];   // cos, sin and theta_k of entry k + 128
+};
+
+// sin and cos of |r| <= pi / 4 by their Maclaurin series: 20 terms each, a
+// term below 1e-200 ending its series (so that none underflows), summed
+// from the smallest
+constexpr double abs_c(double v) { return v < 0.0 ? -v : v; }
+constexpr void series_sincos(double r, double& s, double& c) {
+    const double r2 = r * r;
+    double ts[20] = {}, tc[20] = {};
+    ts[0] = r;
+    tc[0] = 1.0;
+    for (int m = 0; m + 1 < 20; ++m) {
+        ts[m + 1] = abs_c(ts[m]) < 1e-200 ? 0.0 : ts[m] * (-r2 / ((2.0 * m + 2.0) * (2.0 * m + 3.0)));
+        tc[m + 1] = abs_c(tc[m]) < 1e-200 ? 0.0 : tc[m] * (-r2 / ((2.0 * m + 1.0) * (2.0 * m + 2.0)));
+    }
+    s = 0.0;
+    c = 0.0;
+    for (int m = 19; m >= 0; --m) {
+        s += ts[m];
+        c += tc[m];
+    }
+}
+
+// Entry k + 128: theta_k = fl(k pi / 128) and its cos and sin, from the
+// series at theta_k less the nearest multiple q pi / 2 (fl(pi) / 2 taken
+// off exactly, then the rest of pi / 2), turned by the q quarter turns.
+constexpr AtanTable make_atan_table() {
+    AtanTable t{};
+    constexpr double kPiLo = 1.2246467991473532e-16;   // pi - fl(pi)
+    for (int k = 0; k <= 128; ++k) {
+        const double th = (double)k * (kPi / 128.0);
+        const int q = (k + 32) / 64;
+        const double r = (th - q * (kPi / 2.0)) - q * (kPiLo / 2.0);
+        double sr = 0.0, cr = 0.0;
+        series_sincos(r, sr, cr);
+        const double c = q == 0 ? cr : q == 1 ? -sr : -cr;
+        const double sn = q == 0 ? sr : q == 1 ? cr : -sr;
+        t.c[128 + k] = c;
+        t.s[128 + k] = sn;
+        t.th[128 + k] = th;
+        if (k > 0) {
+            t.c[128 - k] = c;
+            t.s[128 - k] = -sn;
+            t.th[128 - k] = -th;
+        }
+    }
+    return t;
+}
+
+__device__ constexpr AtanTable kAtanTab = make_atan_table();
+
+constexpr double kTwoPi = 2.0 * kPi;
+constexpr double kInvTwoPi = 0.15915494309189535;   // fl(1 / (2 pi))
+
+__device__ __forceinline__ double phase_value(double y, double x) {
+    bool ok = true;
+    const float xf = hi_float(x, ok), yf = hi_float(y, ok);
+    double theta;
+    if (!ok || (xf == 0.f && yf == 0.f)) {
+        theta = atan2(y, x);
+    } else {
+        int k = __float2int_rn(atan2f(yf, xf) * 40.74366543152521f);   // 128 / pi
+        k = min(128, max(-128, k)) + 128;
+        const double c = __ldg(&kAtanTab.c[k]), s = __ldg(&kAtanTab.s[k]);
+        const double a = __fma_rn(x, c, __dmul_rn(y, s));
+        const double b = __fma_rn(y, c, -__dmul_rn(x, s));
+        // t = b / a: an FP32 reciprocal, then one residual step
+        const double r0 = (double)__frcp_rn((float)a);
+        const double t0 = __dmul_rn(b, r0);
+        const double t = __fma_rn(__fma_rn(-a, t0, b), r0, t0);
+        const double u = __dmul_rn(t, t);
+        const double p = __fma_rn(__fma_rn(u, -1.0 / 7.0, 1.0 / 5.0), u, -1.0 / 3.0);
+        theta = __dadd_rn(__ldg(&kAtanTab.th[k]), __fma_rn(__dmul_rn(t, u), p, t));
+    }
+    const double sum = __dadd_rn(theta, kPi);
+    const double q = __dmul_rn(sum, kInvTwoPi);
+    return __fma_rn(__fma_rn(-q, kTwoPi, sum), kInvTwoPi, q);
+}
+
 __device__ __forceinline__ double encode_value(double2 h, int flag) {
     switch (flag) {
-        case 0: {  // Phase: (atan2(im, re) + pi) / (2 pi)   (ophGen.cpp:1843-1853)
-            const double pi2 = kPi * 2;
-            return __ddiv_rn(__dadd_rn(atan2(h.y, h.x), kPi), pi2);
-        }
+        case 0:    // Phase: (atan2(im, re) + pi) / (2 pi)   (ophGen.cpp:1843-1853)
+            return phase_value(h.y, h.x);
         case 1:    // Amplitude: sqrt(re^2 + im^2)            (ophGen.cpp:1855-1864)
             return sqrt(__dadd_rn(__dmul_rn(h.x, h.x), __dmul_rn(h.y, h.y)));
         case 2:    // RealPart                                 (ophGen.cpp:1821-1830)
@@ -56,74 +170,86 @@ __device__ __forceinline__ uint64_t global_ns_enc() {
     return t;
 }
 
-__global__ void __launch_bounds__(256) encode_minmax_kernel(const double2* __restrict__ field, int64_t n,
-                                                            int flag, double* __restrict__ encoded,
-                                                            unsigned long long* __restrict__ minmax) {
-    double mn = kMaxDouble, mx = kMinDouble;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const double e = encode_value(field[i], flag);
-        if (encoded) encoded[i] = e;
-        if (e < mn) mn = e;
-        if (e > mx) mx = e;
-    }
+// min and max on the order-preserving integer images of the values (ALU
+// work, not the FP64 pipe's); NaN never wins, as with the reference's strict
+// comparisons
+__device__ __forceinline__ void fold_value(double e, unsigned long long& omn, unsigned long long& omx) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(e);
+    if ((b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull) return;   // NaN
+    const unsigned long long o = (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+    omn = o < omn ? o : omn;
+    omx = o > omx ? o : omx;
+}
+
+// the block's min and max into minmax[0] / minmax[1] (256 threads)
+__device__ __forceinline__ void block_fold(unsigned long long omn, unsigned long long omx,
+                                           unsigned long long* __restrict__ minmax) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const unsigned long long a = __shfl_xor_sync(0xffffffffu, omn, o);
+        const unsigned long long b = __shfl_xor_sync(0xffffffffu, omx, o);
+        omn = a < omn ? a : omn;
+        omx = b > omx ? b : omx;
     }
-    __shared__ double s_mn[8], s_mx[8];
+    __shared__ unsigned long long s_mn[8], s_mx[8];
     const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        s_mn[w] = mn;
-        s_mx[w] = mx;
+        s_mn[w] = omn;
+        s_mx[w] = omx;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-            mn = fmin(mn, s_mn[k]);
-            mx = fmax(mx, s_mx[k]);
+            omn = s_mn[k] < omn ? s_mn[k] : omn;
+            omx = s_mx[k] > omx ? s_mx[k] : omx;
         }
-        atomicMin(&minmax[0], ordered_bits(mn));
-        atomicMax(&minmax[1], ordered_bits(mx));
+        atomicMin(&minmax[0], omn);
+        atomicMax(&minmax[1], omx);
     }
+}
+
+__global__ void __launch_bounds__(256) encode_minmax_kernel(const double2* __restrict__ field, int64_t n,
+                                                            int flag, double* __restrict__ encoded,
+                                                            unsigned long long* __restrict__ minmax) {
+    unsigned long long omn = ordered_bits(kMaxDouble), omx = ordered_bits(kMinDouble);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double e = encode_value(field[i], flag);
+        if (encoded) encoded[i] = e;
+        fold_value(e, omn, omx);
+    }
+    block_fold(omn, omx, minmax);
 }
 
 // min/max of an already encoded buffer (normalize() on its own)
 __global__ void __launch_bounds__(256) minmax_kernel(const double* __restrict__ encoded, int64_t n,
                                                      unsigned long long* __restrict__ minmax) {
-    double mn = kMaxDouble, mx = kMinDouble;
+    unsigned long long omn = ordered_bits(kMaxDouble), omx = ordered_bits(kMinDouble);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const double e = encoded[i];
-        if (e < mn) mn = e;
-        if (e > mx) mx = e;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
-    __shared__ double s_mn[8], s_mx[8];
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_mn[w] = mn;
-        s_mx[w] = mx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int k = 1; k < (int)(blockDim.x >> 5); ++k) {
-            mn = fmin(mn, s_mn[k]);
-            mx = fmax(mx, s_mx[k]);
-        }
-        atomicMin(&minmax[0], ordered_bits(mn));
-        atomicMax(&minmax[1], ordered_bits(mx));
-    }
+         i += (int64_t)gridDim.x * blockDim.x)
+        fold_value(encoded[i], omn, omx);
+    block_fold(omn, omx, minmax);
 }
 
 __device__ __forceinline__ double from_ordered(unsigned long long b) {
     b = (b & 0x8000000000000000ull) ? (b & 0x7fffffffffffffffull) : ~b;
     return __longlong_as_double((long long)b);
+}
+
+// The byte (uchar)(((e - mn) / gap) * 255 + 0.5) with the reference's
+// roundings. In FP32 from d = e - mn it lands within 5e-5 of the reference's
+// value (d and 255 / gap rounded to FP32: 6e-8 relative each of at most
+// 255.5, the FMA's rounding 1.5e-5), so where it lies more than 1e-4 from a
+// code boundary its floor is the code; elsewhere (and for NaN, a gap of 0
+// or a scale FP32 cannot hold) the FP64 division decides. Double -> uchar
+// truncation: NaN and out-of-range values map to 0.
+__device__ __forceinline__ uint8_t code_of(double e, double mn, double gap, float scale) {
+    const double d = __dsub_rn(e, mn);
+    const float v = __fmaf_rn((float)d, scale, 0.5f);
+    const float f = floorf(v);
+    if (v - f > 1e-4f && f + 1.f - v > 1e-4f && f >= 0.f && f <= 255.f) return (uint8_t)(int)f;
+    const double val = __dadd_rn(__dmul_rn(__ddiv_rn(d, gap), 255.0), 0.5);
+    return (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
 }
 
 __global__ void __launch_bounds__(256) normalize_kernel(const double2* __restrict__ field,
@@ -133,12 +259,11 @@ __global__ void __launch_bounds__(256) normalize_kernel(const double2* __restric
     const double mn = from_ordered(minmax[0]);
     const double mx = from_ordered(minmax[1]);
     const double gap = __dsub_rn(mx, mn);
+    const float scale = (gap > 0.0 && gap <= DBL_MAX) ? (float)__ddiv_rn(255.0, gap) : __int_as_float(0x7fc00000);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const double e = encoded ? encoded[i] : encode_value(field[i], flag);
-        const double val = __dadd_rn(__dmul_rn(__ddiv_rn(__dsub_rn(e, mn), gap), 255.0), 0.5);
-        // double -> uchar truncation; NaN (gap == 0) and out-of-range map to 0
-        out[i] = (val >= 0.0 && val < 256.0) ? (uint8_t)(int)val : (uint8_t)0;
+        out[i] = code_of(e, mn, gap, scale);
     }
 }
 
@@ -263,26 +388,6 @@ __global__ void __launch_bounds__(256) encode_normalised_kernel(const double2* _
 // amplitude 4e-6 relative (<= 9.5e-7 from the inputs + 4 ulp, bound 3x).
 constexpr float kPhaseErr = 1e-6f;
 constexpr float kAmpErrRel = 4e-6f;
-
-// FP32 image of a double from its high word: sign, exponent, the top 20
-// mantissa bits (truncated: relative error < 2^-20). ok turns false where
-// the image cannot stand in: subnormal, or outside 2^-62 .. 2^62 (squares
-// stay normal floats), infinite or NaN.
-__device__ __forceinline__ float hi_float(double d, bool& ok) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
-    const unsigned hi = (unsigned)(b >> 32);
-    const int ex = (int)((hi >> 20) & 0x7ffu);
-    const unsigned sign = hi & 0x80000000u;
-    if (ex == 0) {
-        if ((hi & 0xfffffu) | (unsigned)b) ok = false;   // subnormal
-        return __int_as_float((int)sign);                  // signed zero, as atan2 sees it
-    }
-    if (ex < 1023 - 62 || ex > 1023 + 62) {
-        ok = false;
-        return 0.f;
-    }
-    return __int_as_float((int)(sign | ((unsigned)(ex - 1023 + 127) << 23) | ((hi & 0xfffffu) << 3)));
-}
 
 template <int FLAG>
 __device__ __forceinline__ float estimate(double2 h, bool& ok) {

@@ -53,6 +53,41 @@ void host_free(void* p, bool pinned) {
     if (pinned) cudaFreeHost(p);
     else ::operator delete(p);
 }
+
+// The point records: page-locked when the runtime can provide it (their
+// upload in generateHologram then runs at the link's speed), else on the heap.
+Vertex* vertices_alloc(size_t n, bool& pinned) {
+    void* p = nullptr;
+    pinned = cudaHostAlloc(&p, sizeof(Vertex) * (n ? n : 1), cudaHostAllocDefault) == cudaSuccess;
+    if (!pinned) {
+        cudaGetLastError();
+        p = ::operator new(sizeof(Vertex) * (n ? n : 1));
+    }
+    return static_cast<Vertex*>(p);
+}
+
+void vertices_free(Vertex* p, bool pinned) { host_free(p, pinned); }
+
+// memcpy, split over up to four threads above 2 MiB (one core's copy rate
+// is a fraction of the memory system's)
+void copy_parallel(void* dst, const void* src, size_t bytes) {
+    constexpr size_t kChunkMin = (size_t)2 << 20;
+    const size_t parts = bytes >= 4 * kChunkMin ? 4 : bytes >= 2 * kChunkMin ? 2 : 1;
+    if (parts == 1) {
+        std::memcpy(dst, src, bytes);
+        return;
+    }
+    const size_t per = (bytes / parts + 63) / 64 * 64;
+    std::vector<std::thread> ts;
+    for (size_t i = 1; i < parts; ++i) {
+        const size_t off = i * per;
+        if (off >= bytes) break;
+        const size_t len = off + per <= bytes ? per : bytes - off;
+        ts.emplace_back([=] { std::memcpy((char*)dst + off, (const char*)src + off, len); });
+    }
+    std::memcpy(dst, src, per < bytes ? per : bytes);
+    for (auto& t : ts) t.join();
+}
 }  // namespace
 
 ophPointCloud::ophPointCloud(void) { context_.wave_length = wave_length_; }
@@ -64,7 +99,7 @@ ophPointCloud::ophPointCloud(const char* pc_file, const char* cfg_file) : ophPoi
 
 ophPointCloud::~ophPointCloud(void) {
     freeBuffers();
-    delete[] vertices_;
+    vertices_free(vertices_, vertices_pinned_);
     vertices_ = nullptr;
     if (d_vertices_) cudaFree(d_vertices_);
     if (d_field_) cudaFree(d_field_);
@@ -199,15 +234,17 @@ int ophPointCloud::loadPointCloud(const char* pc_file) {
         last_error_ = "cannot load point cloud";
         return -1;
     }
-    Vertex* v = new Vertex[n > 0 ? n : 1];
+    bool pinned = false;
+    Vertex* v = vertices_alloc((size_t)n, pinned);
     if (ophpc_load_ply(pc_file, reinterpret_cast<ophpc_vertex*>(v), (uint64_t)n) != n) {
-        delete[] v;
+        vertices_free(v, pinned);
         OPH_LOG("<FAILED> Loading ply file.\n");
         last_error_ = "cannot load point cloud";
         return -1;
     }
-    delete[] vertices_;
+    vertices_free(vertices_, vertices_pinned_);
     vertices_ = v;
+    vertices_pinned_ = pinned;
     vertices_cap_ = (ulonglong)n;
     n_points_ = (ulonglong)n;
     return (int)n;
@@ -217,11 +254,11 @@ void ophPointCloud::setPointCloudModel(Vertex* vertex) {
     if (n_points_ < 1 || !vertex) return;
     if (vertices_ != vertex) {   // the copy (ophPointCloud.h:577-586); its buffer is reused at the same size
         if (!vertices_ || vertices_cap_ != n_points_) {
-            delete[] vertices_;
-            vertices_ = new Vertex[n_points_];
+            vertices_free(vertices_, vertices_pinned_);
+            vertices_ = vertices_alloc((size_t)n_points_, vertices_pinned_);
             vertices_cap_ = n_points_;
         }
-        std::memcpy(vertices_, vertex, sizeof(Vertex) * n_points_);
+        copy_parallel(vertices_, vertex, sizeof(Vertex) * n_points_);
     }
 }
 
@@ -271,6 +308,20 @@ bool ophPointCloud::ensureDevice(size_t bv, size_t bf, size_t be, size_t bc) {
         !grow(&d_codes_, &cap_c_, bc)) {
         last_error_ = "device allocation failed";
         return false;
+    }
+    return true;
+}
+
+bool ophPointCloud::ensureStreams() {
+    for (uint ch = 0; ch < OPHPC_MAX_CHANNELS; ++ch) {
+        if (streams_[ch]) continue;
+        cudaStream_t st = nullptr;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            last_error_ = "stream creation failed";
+            return false;
+        }
+        streams_[ch] = st;
     }
     return true;
 }
@@ -328,12 +379,15 @@ Real ophPointCloud::generateHologram(uint diff_flag) {
         last_error_ = std::string("generate: ") + ophpc_last_error(gpu_);
         return 0.0;
     }
-    for (uint ch = 0; ch < nch; ++ch) {
-        if (cudaMemcpy(complex_H_[ch], (double*)d_field_ + 2 * plane * ch, sizeof(double) * 2 * plane,
-                       cudaMemcpyDeviceToHost) != cudaSuccess) {
-            last_error_ = "field download failed";
-            return 0.0;
-        }
+    // the channels' downloads queued behind the generate, one wait
+    bool ok = true;
+    for (uint ch = 0; ch < nch && ok; ++ch)
+        ok = cudaMemcpyAsync(complex_H_[ch], (double*)d_field_ + 2 * plane * ch, sizeof(double) * 2 * plane,
+                             cudaMemcpyDeviceToHost, nullptr) == cudaSuccess;
+    if (cudaStreamSynchronize(nullptr) != cudaSuccess || !ok) {
+        cudaGetLastError();
+        last_error_ = "field download failed";
+        return 0.0;
     }
     context_.k = (2 * kPi) / wave_length_[nch - 1];
     progress_ = 0;
@@ -354,17 +408,7 @@ void ophPointCloud::encoding(unsigned int flag) {
     // the channel's own largest magnitude), so the channels run as a
     // pipeline, one stream each: the upload of one overlaps the encoding and
     // the download of the one before.
-    for (uint ch = 0; ch < nch; ++ch) {
-        cudaStream_t st = nullptr;
-        if (!streams_[ch]) {
-            if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
-                cudaGetLastError();
-                last_error_ = "stream creation failed";
-                return;
-            }
-            streams_[ch] = st;
-        }
-    }
+    if (!ensureStreams()) return;
     cudaDeviceSynchronize();   // earlier work on the field buffers (legacy stream) is done
     bool ok = true;
     std::string err;
@@ -434,14 +478,27 @@ void ophPointCloud::normalize(void) {
     const size_t plane = (size_t)buffer_pixels_;
     const uint nch = context_.waveNum;
     if (!ensureDevice(cap_v_ ? cap_v_ : 1, cap_f_ ? cap_f_ : 1, sizeof(double) * plane * nch, plane * nch)) return;
-    for (uint ch = 0; ch < nch; ++ch)
-        cudaMemcpy((double*)d_encoded_ + plane * ch, encoded_[ch], sizeof(double) * plane, cudaMemcpyHostToDevice);
-    if (ophpc_normalize(gpu_, (const double*)d_encoded_, nch, plane, (uint8_t*)d_codes_, nullptr) != OPHPC_SUCCESS) {
-        last_error_ = std::string("normalize: ") + ophpc_last_error(gpu_);
-        return;
+    if (!ensureStreams()) return;
+    cudaDeviceSynchronize();   // earlier work on the buffers (legacy stream) is done
+    // uploads, min/max and codes, downloads queued on one stream, one wait
+    cudaStream_t st = (cudaStream_t)streams_[0];
+    bool ok = true;
+    std::string err;
+    for (uint ch = 0; ch < nch && ok; ++ch)
+        ok = cudaMemcpyAsync((double*)d_encoded_ + plane * ch, encoded_[ch], sizeof(double) * plane,
+                             cudaMemcpyHostToDevice, st) == cudaSuccess;
+    if (ok && ophpc_normalize(gpu_, (const double*)d_encoded_, nch, plane, (uint8_t*)d_codes_, st) != OPHPC_SUCCESS) {
+        err = std::string("normalize: ") + ophpc_last_error(gpu_);
+        ok = false;
     }
-    for (uint ch = 0; ch < nch; ++ch)
-        cudaMemcpy(normalized_[ch], (uint8_t*)d_codes_ + plane * ch, plane, cudaMemcpyDeviceToHost);
+    for (uint ch = 0; ch < nch && ok; ++ch)
+        ok = cudaMemcpyAsync(normalized_[ch], (uint8_t*)d_codes_ + plane * ch, plane, cudaMemcpyDeviceToHost, st) ==
+             cudaSuccess;
+    if (cudaStreamSynchronize(st) != cudaSuccess) ok = false;
+    if (!ok) {
+        cudaGetLastError();
+        last_error_ = err.empty() ? std::string("normalize copies failed") : err;
+    }
 }
 
 bool ophPointCloud::save(const char* fname, uint8_t bitsperpixel, uchar* src, uint px, uint py) {
