@@ -404,19 +404,30 @@ def facade_e2e(w, mode: int, steps: int) -> dict:
             h.SetMode(mode)
             v = np.ascontiguousarray(w.vertices)
             gen_s = []
+            calls = {"setPointCloudModel": [], "generateHologram": [], "encoding": [], "normalize": []}
 
             def step():
+                t0 = time.perf_counter()
                 h.setPointCloudModel(v)
+                t1 = time.perf_counter()
                 secs = h.generateHologram(0)
                 if secs <= 0.0:
                     raise RuntimeError(f"generateHologram: {h.lastError()}")
-                gen_s.append(secs)
+                t2 = time.perf_counter()
                 h.encoding(0)
+                t3 = time.perf_counter()
                 h.normalize()
+                t4 = time.perf_counter()
+                gen_s.append(secs)
+                for k, a, b in (("setPointCloudModel", t0, t1), ("generateHologram", t1, t2), ("encoding", t2, t3),
+                                ("normalize", t3, t4)):
+                    calls[k].append((b - a) * 1e3)
 
             for _ in range(3):
                 step()
             gen_s.clear()
+            for c in calls.values():
+                c.clear()
             t0 = time.perf_counter()
             for _ in range(steps):
                 step()
@@ -425,6 +436,7 @@ def facade_e2e(w, mode: int, steps: int) -> dict:
             h.release()
     npx = w.pnx * w.pny * w.n_channels
     return {"s_per_step": t, "generate_s": sum(gen_s) / len(gen_s),
+            "calls_ms_median": {k: float(np.median(c)) for k, c in calls.items()},
             "h2d": w.n_points * 56 + npx * 16 + npx * 8, "d2h": npx * 16 + npx * 8 + npx}
 
 
@@ -772,6 +784,37 @@ def gpu_arm(args, w):
     # genCghPointCloudGPU equivalent, without encoding
     gh = generate_host_e2e(ctx, w, cfg, rs_mode, max(3, args.steps // 2))
 
+    # --- the encoders on the device-resident sphere_fhd field (the last RS
+    # generate above): FP64 phase values (m_lpEncoded), normalize of those
+    # values into codes, and the codes-only phase path; L2 flushed between
+    # calls
+    import ctypes
+    lib.ophpc_normalize.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
+                                    ctypes.c_void_p, ctypes.c_void_p]
+    lib.ophpc_normalize.restype = ctypes.c_int
+    enc_vals = torch.empty((nch, npx), dtype=torch.float64, device="cuda")
+
+    def normalize_call():
+        if lib.ophpc_normalize(ctx._h, enc_vals.data_ptr(), nch, npx, codes.data_ptr(), sp) != 0:
+            raise RuntimeError("ophpc_normalize failed")
+
+    encoders = {}
+    for name, fn in (
+            ("phase_values", lambda: ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, enc_vals.data_ptr(),
+                                                None, sp)),
+            ("normalize", normalize_call),
+            ("phase_codes_only", lambda: ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None,
+                                                    codes.data_ptr(), sp)),
+            ("amplitude_values", lambda: ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_AMPLITUDE,
+                                                    enc_vals.data_ptr(), None, sp))):
+        fn()
+        ts = timed(fn, 10)
+        encoders[name] = {"ms": 1e3 * sum(ts) / len(ts)}
+    encoders["pixels"] = nch * npx
+    encoders["note"] = ("phase_values: FP64 (atan2(im, re) + pi) / (2 pi) per pixel, 16 B read and 8 B written; "
+                        "normalize: min/max and codes of 8 B values; phase_codes_only: the single-pass FP32-estimate "
+                        "codes kernel")
+
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 1995.0
     props = torch.cuda.get_device_properties(local)
@@ -896,8 +939,9 @@ def gpu_arm(args, w):
                     "call": "ophPointCloud facade C ABI (ophpc_pc_set_point_cloud, ophpc_pc_generate_hologram, "
                             "ophpc_pc_encoding(PHASE), ophpc_pc_normalize): host Vertex[] in, host complex_H, "
                             "m_lpEncoded and m_lpNormalized out; wall clock around the synchronous calls",
-                    "generate_s_reported": e2e["generate_s"]},
+                    "generate_s_reported": e2e["generate_s"], "calls_ms_median": e2e["calls_ms_median"]},
             "e2e_generate_host": gh,
+            "encoders": encoders,
             "gpu_launches": int(launches),
             "clocks": {"sm_mhz": clocks["sm_mhz"], "sm_max_mhz": clocks["sm_max_mhz"],
                        "reasons": clocks["reasons"], "samples": clocks["samples"]},

@@ -445,17 +445,28 @@ void ophPointCloud::encodeSideband(unsigned int flag, unsigned int passband, Rea
         return;
     context_.ss[_X] = context_.pixel_number[_X] * context_.pixel_pitch[_X];
     context_.ss[_Y] = context_.pixel_number[_Y] * context_.pixel_pitch[_Y];
-    for (uint ch = 0; ch < nch; ++ch)
-        cudaMemcpy((double*)d_field_ + 2 * plane * ch, complex_H_[ch], sizeof(double) * 2 * plane, cudaMemcpyHostToDevice);
-    if (ophpc_encode_ssb(gpu_, (const double*)d_field_, nch, context_.pixel_number[_X], context_.pixel_number[_Y],
-                         context_.pixel_pitch[_X], context_.pixel_pitch[_Y], flag, passband, shift_x, shift_y,
-                         (double*)d_encoded_, nullptr, nullptr) != OPHPC_SUCCESS) {
-        last_error_ = std::string("encode: ") + ophpc_last_error(gpu_);
+    // uploads, the transforms and downloads queued on the legacy stream, one wait
+    bool ok = true;
+    std::string err;
+    for (uint ch = 0; ch < nch && ok; ++ch)
+        ok = cudaMemcpyAsync((double*)d_field_ + 2 * plane * ch, complex_H_[ch], sizeof(double) * 2 * plane,
+                             cudaMemcpyHostToDevice, nullptr) == cudaSuccess;
+    if (ok && ophpc_encode_ssb(gpu_, (const double*)d_field_, nch, context_.pixel_number[_X],
+                               context_.pixel_number[_Y], context_.pixel_pitch[_X], context_.pixel_pitch[_Y], flag,
+                               passband, shift_x, shift_y, (double*)d_encoded_, nullptr, nullptr) != OPHPC_SUCCESS) {
+        err = std::string("encode: ") + ophpc_last_error(gpu_);
+        ok = false;
+    }
+    for (uint ch = 0; ch < nch && ok; ++ch)
+        ok = cudaMemcpyAsync(encoded_[ch], (double*)d_encoded_ + plane * ch, sizeof(double) * plane,
+                             cudaMemcpyDeviceToHost, nullptr) == cudaSuccess;
+    if (cudaStreamSynchronize(nullptr) != cudaSuccess) ok = false;
+    if (!ok) {
+        cudaGetLastError();
+        last_error_ = err.empty() ? std::string("encode copies failed") : err;
         OPH_LOG("<FAILED> %s\n", last_error_.c_str());
         return;
     }
-    for (uint ch = 0; ch < nch; ++ch)
-        cudaMemcpy(encoded_[ch], (double*)d_encoded_ + plane * ch, sizeof(double) * plane, cudaMemcpyDeviceToHost);
     encoded_valid_ = true;
 }
 
