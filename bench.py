@@ -1003,6 +1003,8 @@ def profile_case(name: str) -> None:
         w, diff, mode = workloads.sphere_fhd(), 1, oph.MODE_TENSOR_BF16X3
     elif name == "tcf_4k":          # tensor-core Fresnel (on-chip factors), box_4k geometry, 131,072 points
         w, diff, mode = workloads.box_4k(n_points=131_072), 1, oph.MODE_TENSOR_BF16X3
+    elif name == "values_fhd":      # FP64 phase values of the sphere_fhd field, then normalize of them
+        w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
     else:
         raise SystemExit(f"unknown profile case {name}")
     ctx = oph.Context(0)
@@ -1010,13 +1012,23 @@ def profile_case(name: str) -> None:
     dv = torch.from_numpy(w.vertices).cuda()
     f = torch.empty((w.n_channels, w.pny, w.pnx, 2), dtype=torch.float64, device="cuda")
     codes = torch.empty((w.n_channels, w.pny * w.pnx), dtype=torch.uint8, device="cuda")
+    sp = torch.cuda.current_stream().cuda_stream
+    npx = w.pny * w.pnx
     for it in range(2):
-        if name != "codes_fhd" or it == 0:
-            ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(),
-                         torch.cuda.current_stream().cuda_stream)
+        if name not in ("codes_fhd", "values_fhd") or it == 0:
+            ctx.generate(cfg, dv.data_ptr(), w.n_points, diff, mode, f.data_ptr(), sp)
         if name in ("step_fhd", "codes_fhd"):
-            ctx.encode(f.data_ptr(), w.n_channels, w.pny * w.pnx, oph.ENCODE_PHASE, None, codes.data_ptr(),
-                       torch.cuda.current_stream().cuda_stream)
+            ctx.encode(f.data_ptr(), w.n_channels, npx, oph.ENCODE_PHASE, None, codes.data_ptr(), sp)
+        if name == "values_fhd":
+            import ctypes
+            lib = oph.lib()
+            lib.ophpc_normalize.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64,
+                                            ctypes.c_void_p, ctypes.c_void_p]
+            lib.ophpc_normalize.restype = ctypes.c_int
+            vals = torch.empty((w.n_channels, npx), dtype=torch.float64, device="cuda")
+            ctx.encode(f.data_ptr(), w.n_channels, npx, oph.ENCODE_PHASE, vals.data_ptr(), None, sp)
+            if lib.ophpc_normalize(ctx._h, vals.data_ptr(), w.n_channels, npx, codes.data_ptr(), sp) != 0:
+                raise RuntimeError("ophpc_normalize failed")
     torch.cuda.synchronize()
     print(f"profile case {name}: done")
 
