@@ -83,7 +83,12 @@ void copy_parallel(void* dst, const void* src, size_t bytes) {
         const size_t off = i * per;
         if (off >= bytes) break;
         const size_t len = off + per <= bytes ? per : bytes - off;
-        ts.emplace_back([=] { std::memcpy((char*)dst + off, (const char*)src + off, len); });
+        auto part = [=] { std::memcpy((char*)dst + off, (const char*)src + off, len); };
+        try {
+            ts.emplace_back(part);
+        } catch (...) {   // no thread to be had: this one copies the part
+            part();
+        }
     }
     std::memcpy(dst, src, per < bytes ? per : bytes);
     for (auto& t : ts) t.join();
@@ -349,12 +354,17 @@ Real ophPointCloud::generateHologram(uint diff_flag) {
         uchar** nrm = normalized_;
         const uint nch_reset = context_.waveNum;
         const size_t px = (size_t)buffer_pixels_;
-        reset.t = std::thread([enc, nrm, nch_reset, px] {
+        auto clear = [enc, nrm, nch_reset, px] {
             for (uint c = 0; c < nch_reset; ++c) {
                 std::memset(enc[c], 0, sizeof(Real) * px);
                 std::memset(nrm[c], 0, px);
             }
-        });
+        };
+        try {
+            reset.t = std::thread(clear);
+        } catch (...) {   // no thread to be had: clear them here
+            clear();
+        }
     }
     encoded_valid_ = false;
     if (!ensureGpu()) return 0.0;
