@@ -1005,6 +1005,18 @@ def profile_case(name: str) -> None:
         w, diff, mode = workloads.box_4k(n_points=131_072), 1, oph.MODE_TENSOR_BF16X3
     elif name == "values_fhd":      # FP64 phase values of the sphere_fhd field, then normalize of them
         w, diff, mode = workloads.sphere_fhd(), 0, oph.MODE_TENSOR_BF16X3
+    elif name == "wrp_fhd":         # WRP generator, sphere_fhd points, WRP 1 mm in front, 0.5 m propagation
+        w = workloads.sphere_fhd()
+        ctx = oph.Context(0)
+        wcfg = oph.make_wrp_config(pnx=w.pnx, pny=w.pny, ppx=w.pp, ppy=w.pp, wavelengths=list(w.wavelengths),
+                                   wrp_location=float(w.vertices[:, 2].max()) + 1e-3, distance=0.5)
+        dv = torch.from_numpy(w.vertices).cuda()
+        f = torch.empty((w.n_channels, w.pny, w.pnx, 2), dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            ctx.wrp_generate(wcfg, dv.data_ptr(), w.n_points, f.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.synchronize()
+        print(f"profile case {name}: done")
+        return
     else:
         raise SystemExit(f"unknown profile case {name}")
     ctx = oph.Context(0)

@@ -65,24 +65,10 @@ __device__ __forceinline__ void dft<8>(double2* v, bool inv) {
     }
 }
 
-// Odd prime radices: the direct sum with the R-th roots of unity,
-// cos(2 pi m / R) and sin(2 pi m / R) as literal constants.
+// Radix 7: the direct sum with the 7th roots of unity, cos(2 pi m / 7) and
+// sin(2 pi m / 7) as literal constants.
 template <int R>
 __device__ __forceinline__ double2 root(int m, double sg);
-
-template <>
-__device__ __forceinline__ double2 root<3>(int m, double sg) {
-    constexpr double c[3] = {1.00000000000000000000, -0.49999999999999977796, -0.50000000000000044409};
-    constexpr double s[3] = {0.00000000000000000000, 0.86602540378443870761, -0.86602540378443837454};
-    return make_double2(c[m], sg * s[m]);
-}
-
-template <>
-__device__ __forceinline__ double2 root<5>(int m, double sg) {
-    constexpr double c[5] = {1.00000000000000000000, 0.30901699437494745126, -0.80901699437494734024, -0.80901699437494756229, 0.30901699437494722922};
-    constexpr double s[5] = {0.00000000000000000000, 0.95105651629515353118, 0.58778525229247324813, -0.58778525229247302608, -0.95105651629515364220};
-    return make_double2(c[m], sg * s[m]);
-}
 
 template <>
 __device__ __forceinline__ double2 root<7>(int m, double sg) {
@@ -108,10 +94,42 @@ __device__ __forceinline__ void dft_direct(double2* v, bool inv) {
 #pragma unroll
     for (int q = 0; q < R; ++q) v[q] = out[q];
 }
+// Radix 3 and 5 from the sums and differences of the entries paired by
+// symmetry (the textbook small DFTs: X_k and X_(R-k) share the real-cosine
+// part and differ in the sign of the sine part), 4.7 and 7.2 FP64
+// operations an element against 12 and 24 for the direct sum; GB300's FP64
+// pipe is narrow, so a pass costs its operation count. Constants are the
+// correctly rounded cos and sin of 2 pi / 3, 2 pi / 5 and 4 pi / 5.
 template <>
-__device__ __forceinline__ void dft<3>(double2* v, bool inv) { dft_direct<3>(v, inv); }
+__device__ __forceinline__ void dft<3>(double2* v, bool inv) {
+    constexpr double s = 0.866025403784438646763723170753;   // sin(2 pi / 3)
+    const double2 t1 = cadd(v[1], v[2]), t2 = csub(v[1], v[2]);
+    const double2 a = make_double2(__fma_rn(-0.5, t1.x, v[0].x), __fma_rn(-0.5, t1.y, v[0].y));
+    const double2 b = rot_q(make_double2(s * t2.x, s * t2.y), inv);
+    v[0] = cadd(v[0], t1);
+    v[1] = cadd(a, b);
+    v[2] = csub(a, b);
+}
 template <>
-__device__ __forceinline__ void dft<5>(double2* v, bool inv) { dft_direct<5>(v, inv); }
+__device__ __forceinline__ void dft<5>(double2* v, bool inv) {
+    constexpr double c1 = 0.309016994374947424102293417183;    // cos(2 pi / 5)
+    constexpr double c2 = -0.809016994374947424102293417183;   // cos(4 pi / 5)
+    constexpr double s1 = 0.951056516295153572116439333379;    // sin(2 pi / 5)
+    constexpr double s2 = 0.587785252292473129168705954639;    // sin(4 pi / 5)
+    const double2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
+    const double2 t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    const double2 a1 = make_double2(__fma_rn(c2, t2.x, __fma_rn(c1, t1.x, v[0].x)),
+                                    __fma_rn(c2, t2.y, __fma_rn(c1, t1.y, v[0].y)));
+    const double2 a2 = make_double2(__fma_rn(c1, t2.x, __fma_rn(c2, t1.x, v[0].x)),
+                                    __fma_rn(c1, t2.y, __fma_rn(c2, t1.y, v[0].y)));
+    const double2 b1 = rot_q(make_double2(__fma_rn(s2, t4.x, s1 * t3.x), __fma_rn(s2, t4.y, s1 * t3.y)), inv);
+    const double2 b2 = rot_q(make_double2(__fma_rn(-s1, t4.x, s2 * t3.x), __fma_rn(-s1, t4.y, s2 * t3.y)), inv);
+    v[0] = cadd(v[0], cadd(t1, t2));
+    v[1] = cadd(a1, b1);
+    v[4] = csub(a1, b1);
+    v[2] = cadd(a2, b2);
+    v[3] = csub(a2, b2);
+}
 template <>
 __device__ __forceinline__ void dft<7>(double2* v, bool inv) { dft_direct<7>(v, inv); }
 

@@ -17,6 +17,8 @@
 //   wrp_bin_kernel     amplitudes into per-channel anchor grids of 64-bit
 //                      fixed point (integer atomics: the same sums in any
 //                      order, so the result is deterministic)
+//   wrp_amp_kernel     the fixed-point sums turned into FP64 amplitudes in
+//                      place, once per anchor
 //   wrp_kernel_table   the (2w)^2 kernel values in FP64
 //   wrp_conv_kernel    per plane pixel the FP64 sum over the square, written
 //                      into the centre of the zero-padded FFT buffer
@@ -32,6 +34,7 @@
 #include "pc_common.cuh"
 #include "pc_fft.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -106,6 +109,16 @@ __global__ void wrp_bin_kernel(const double* __restrict__ verts, int64_t n, BinA
     }
 }
 
+// The anchor grids' fixed-point sums as FP64 amplitudes, in place (the
+// conversion the splat would otherwise repeat for every pixel an anchor
+// reaches; GB300's FP64 pipe is narrow).
+__global__ void wrp_amp_kernel(unsigned long long* __restrict__ grid, int64_t n, double inv_fixed) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const long long q = (long long)grid[i];
+        if (q != 0) grid[i] = (unsigned long long)__double_as_longlong((double)q * inv_fixed);
+    }
+}
+
 // Kernel values K[wy + w][wx + w] of one channel (ophWRP.cpp:396-408, with
 // the amplitude factored out).
 __global__ void wrp_kernel_table(double2* __restrict__ K, int w, double ppx, double ppy, double dzz, int sign_pos,
@@ -126,13 +139,14 @@ __global__ void wrp_kernel_table(double2* __restrict__ K, int w, double ppx, dou
 
 struct ConvArgs {
     int pnx, pny, w, gx, gy;
-    double inv_fixed;           // 1 / fixed-point scale (a power of two)
     int64_t out_stride;         // elements per output row
 };
 
 // Plane pixel (px, py): sum over the square of anchor amplitude x kernel,
-// wy outer, wx inner (a fixed order). The kernel table sits in shared
-// memory when it fits.
+// wy outer, wx inner (a fixed order), anchors without points skipped by
+// their bits (an integer test: zero bits are +0.0, the only zero
+// wrp_amp_kernel writes). The kernel table sits in shared memory when it
+// fits.
 __global__ void __launch_bounds__(256) wrp_conv_kernel(const unsigned long long* __restrict__ grid,
                                                        const double2* __restrict__ K, ConvArgs a,
                                                        double2* __restrict__ out, int k_in_smem) {
@@ -151,9 +165,9 @@ __global__ void __launch_bounds__(256) wrp_conv_kernel(const unsigned long long*
         const unsigned long long* row = grid + (int64_t)(py - wy + a.w) * a.gx + (px + a.w);
         const double2* krow = Kt + (wy + a.w) * side + a.w;
         for (int wx = -a.w; wx < a.w; ++wx) {
-            const long long q = (long long)__ldg(row - wx);
+            const unsigned long long q = __ldg(row - wx);
             if (q != 0) {
-                const double amp = (double)q * a.inv_fixed;
+                const double amp = __longlong_as_double((long long)q);
                 const double2 kv = krow[wx];
                 re = fma(amp, kv.x, re);
                 im = fma(amp, kv.y, im);
@@ -313,9 +327,12 @@ ophpc_status wrp_generate_device(cudaMemPool_t pool, const ophpc_wrp_config* cfg
         ba.gx = gx;
         ba.gy = gy;
         ba.nch = nch;
-        count_launches(1);
+        const int64_t cells = (int64_t)gx * gy * nch;
+        count_launches(2);
         wrp_bin_kernel<<<(unsigned)((n_points + 255) / 256), 256, 0, s>>>(reinterpret_cast<const double*>(d_vertices),
                                                                          (int64_t)n_points, ba, grid);
+        wrp_amp_kernel<<<(unsigned)std::min<int64_t>((cells + 255) / 256, 4096), 256, 0, s>>>(grid, cells,
+                                                                                            1.0 / fixed);
     }
     // the reference's random-phase factor with RandomPhase off: 2 pi * 1.0
     const double crand = std::cos(pi2 * 1.0), srand_ = std::sin(pi2 * 1.0);
@@ -334,7 +351,6 @@ ophpc_status wrp_generate_device(cudaMemPool_t pool, const ophpc_wrp_config* cfg
         ca.w = wc;
         ca.gx = gx;
         ca.gy = gy;
-        ca.inv_fixed = 1.0 / fixed;
         const unsigned long long* gch = grid + (size_t)c * gx * gy + (size_t)(wmax - wc) * gx + (wmax - wc);
         double2* dst;
         if (full) {
