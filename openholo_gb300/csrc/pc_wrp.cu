@@ -143,11 +143,17 @@ struct ConvArgs {
 };
 
 // Plane pixel (px, py): sum over the square of anchor amplitude x kernel,
-// wy outer, wx inner (a fixed order), anchors without points skipped by
-// their bits (an integer test: zero bits are +0.0, the only zero
-// wrp_amp_kernel writes). The kernel table sits in shared memory when it
-// fits.
-__global__ void __launch_bounds__(256) wrp_conv_kernel(const unsigned long long* __restrict__ grid,
+// wy outer, wx inner (a fixed order). Anchors without points hold zero bits
+// (+0.0, the only zero wrp_amp_kernel writes), and an FMA with them leaves
+// the sum as it is (the kernel values are finite, the sum never -0.0), so a
+// warp skips a row of the square where none of its 32 pixels meets a point:
+// an integer OR over the row's anchors, a vote, and the row's FMAs only
+// when some lane needs them. On GB300's narrow FP64 pipe the FMAs are the
+// cost; a per-anchor test is turned into predicated FMAs that still take
+// the pipe. Every lane of a warp reaches the vote (lanes past the plane's
+// edge read nothing and store nothing). The kernel table sits in shared
+// memory when it fits.
+__global__ void __launch_bounds__(256, 4) wrp_conv_kernel(const unsigned long long* __restrict__ grid,
                                                        const double2* __restrict__ K, ConvArgs a,
                                                        double2* __restrict__ out, int k_in_smem) {
     extern __shared__ double2 sK[];
@@ -159,38 +165,55 @@ __global__ void __launch_bounds__(256) wrp_conv_kernel(const unsigned long long*
     }
     const double2* Kt = k_in_smem ? sK : K;
     const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
-    if (px >= a.pnx || py >= a.pny) return;
+    const bool inside = px < a.pnx && py < a.pny;
+    const int qx = inside ? px : 0, qy = inside ? py : 0;
     double re = 0.0, im = 0.0;
     for (int wy = -a.w; wy < a.w; ++wy) {
-        const unsigned long long* row = grid + (int64_t)(py - wy + a.w) * a.gx + (px + a.w);
+        const unsigned long long* row = grid + (int64_t)(qy - wy + a.w) * a.gx + (qx + a.w);
+        unsigned long long any = 0;
+        if (inside)
+            for (int wx = -a.w; wx < a.w; ++wx) any |= __ldg(row - wx);
+        if (!__any_sync(0xffffffffu, any != 0)) continue;
         const double2* krow = Kt + (wy + a.w) * side + a.w;
         for (int wx = -a.w; wx < a.w; ++wx) {
-            const unsigned long long q = __ldg(row - wx);
-            if (q != 0) {
-                const double amp = __longlong_as_double((long long)q);
-                const double2 kv = krow[wx];
-                re = fma(amp, kv.x, re);
-                im = fma(amp, kv.y, im);
-            }
+            const double amp = inside ? __longlong_as_double((long long)__ldg(row - wx)) : 0.0;
+            const double2 kv = krow[wx];
+            re = fma(amp, kv.x, re);
+            im = fma(amp, kv.y, im);
         }
     }
-    out[(int64_t)py * a.out_stride + px] = make_double2(re, im);
+    if (inside) out[(int64_t)py * a.out_stride + px] = make_double2(re, im);
 }
 
 // buf *= exp(i 2 pi d sqrt(1/lambda^2 - fx^2 - fy^2)), natural frequency
 // order (signed index / (2 ss), as Fresnel_FFT's LUT_fx after its shift).
+// T depends on fx^2 and fy^2 only, and (-k) / (2 ss) is exactly -(k / (2 ss)),
+// so one thread computes T for |kx| = j, |ky| = i (j <= nx/2, i <= ny/2)
+// and applies it to the up to four entries with those magnitudes: a quarter
+// of the FP64 sqrt and sincos, bit for bit the values of one per entry.
 __global__ void wrp_transfer_kernel(double2* __restrict__ buf, int nx, int ny, double ssx2, double ssy2,
                                     double inv_lambda_sq, double two_pi_d) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
-    if (j >= nx || i >= ny) return;
-    const int kx = j < nx / 2 ? j : j - nx, ky = i < ny / 2 ? i : i - ny;
+    const int hx = nx / 2, hy = ny / 2;
+    if (j > hx || i > hy) return;
+    // index j < nx/2 holds kx = j; index nx/2 holds kx = -nx/2 (no mirror)
+    const int kx = j < hx ? j : -hx, ky = i < hy ? i : -hy;
     const double fx = (double)kx / ssx2, fy = (double)ky / ssy2;
     const double sq = sqrt(inv_lambda_sq - fx * fx - fy * fy);
     double s, c;
     sincos(two_pi_d * sq, &s, &c);
-    const int64_t o = (int64_t)i * nx + j;
-    const double2 v = buf[o];
-    buf[o] = make_double2(v.x * c - v.y * s, v.x * s + v.y * c);
+    const int cols[2] = {j, (j > 0 && j < hx) ? nx - j : -1};
+    const int rows[2] = {i, (i > 0 && i < hy) ? ny - i : -1};
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            if (rows[a] < 0 || cols[b] < 0) continue;
+            const int64_t o = (int64_t)rows[a] * nx + cols[b];
+            const double2 v = buf[o];
+            buf[o] = make_double2(v.x * c - v.y * s, v.x * s + v.y * c);
+        }
+    }
 }
 
 // dst[py][px] = src[(hy + py) * nx + hx + px]
@@ -224,7 +247,7 @@ cudaError_t propagate(double2* const buf[2], const FftPlan& px_plan, const FftPl
     double2* spec = cols[c1];
     const double ssx2 = (pnx * ppx) * 2, ssy2 = (pny * ppy) * 2;
     count_launches(1);
-    wrp_transfer_kernel<<<dim3((unsigned)((nx + 255) / 256), (unsigned)ny), 256, 0, s>>>(
+    wrp_transfer_kernel<<<dim3((unsigned)((nx / 2 + 1 + 255) / 256), (unsigned)(ny / 2 + 1)), 256, 0, s>>>(
         spec, nx, ny, ssx2, ssy2, 1.0 / (lambda * lambda), 2 * M_PI * distance);
     double2* icol[2] = {spec, cols[c1 ^ 1]};
     const int c2 = fft_run(py_plan, icol, nx, nx, 1, true, s);
