@@ -68,8 +68,8 @@ Vertex* vertices_alloc(size_t n, bool& pinned) {
 
 void vertices_free(Vertex* p, bool pinned) { host_free(p, pinned); }
 
-// memcpy, split over up to four threads above 2 MiB (one core's copy rate
-// is a fraction of the memory system's)
+// memcpy in one part below 4 MiB, two threads' parts from 4 MiB and four
+// from 8 MiB (one core's copy rate is a fraction of the memory system's)
 void copy_parallel(void* dst, const void* src, size_t bytes) {
     constexpr size_t kChunkMin = (size_t)2 << 20;
     const size_t parts = bytes >= 4 * kChunkMin ? 4 : bytes >= 2 * kChunkMin ? 2 : 1;

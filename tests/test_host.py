@@ -114,6 +114,21 @@ def test_facade_config_and_model_state(tmp_path):
         assert not h.readConfig(str(tmp_path / "missing.xml"))
 
 
+@pytest.mark.parametrize("n", [37_449, 74_899, 150_001, 200_000])
+def test_facade_keeps_large_models_whole(n):
+    """setPointCloudModel copies the caller's records (ophPointCloud.h:577-586)
+    in one part below 4 MiB, two from 4 MiB and four from 8 MiB: every record
+    arrives, at sizes either side of those steps and off the 64-byte part
+    boundaries, and a second model of the same size reuses the buffer."""
+    rng = np.random.default_rng(n)
+    with P.PointCloud() as h:
+        for _ in range(2):
+            v = rng.normal(size=(n, 7))
+            h.setPointCloudModel(v)
+            assert h.getNumberOfPoints() == n
+            assert np.array_equal(h.getPointCloudModel(), v)
+
+
 @pytest.mark.parametrize("lang", ["c", "c++"])
 def test_public_headers_compile(tmp_path, lang):
     """Every include/*.h compiles on its own as C11 and as C++17."""
