@@ -114,7 +114,7 @@ def test_facade_config_and_model_state(tmp_path):
         assert not h.readConfig(str(tmp_path / "missing.xml"))
 
 
-@pytest.mark.parametrize("n", [37_449, 74_899, 150_001, 200_000])
+@pytest.mark.parametrize("n", [74_897, 74_899, 149_796, 149_797, 200_001])
 def test_facade_keeps_large_models_whole(n):
     """setPointCloudModel copies the caller's records (ophPointCloud.h:577-586)
     in one part below 4 MiB, two from 4 MiB and four from 8 MiB: every record
