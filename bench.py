@@ -806,14 +806,23 @@ def gpu_arm(args, w):
             ("phase_codes_only", lambda: ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_PHASE, None,
                                                     codes.data_ptr(), sp)),
             ("amplitude_values", lambda: ctx.encode(field.data_ptr(), nch, npx, oph.ENCODE_AMPLITUDE,
-                                                    enc_vals.data_ptr(), None, sp))):
+                                                    enc_vals.data_ptr(), None, sp)),
+            ("ssb", lambda: ctx.encode_ssb(field.data_ptr(), nch, pnx, pny, w.pp, w.pp, oph.ENCODE_SSB, 0,
+                                           (0.0, 0.5), enc_vals.data_ptr(), codes.data_ptr(), sp)),
+            ("off_axis_ssb", lambda: ctx.encode_ssb(field.data_ptr(), nch, pnx, pny, w.pp, w.pp, oph.ENCODE_OFFSSB,
+                                                    oph.SSB_LEFT, (0.0, 0.5), enc_vals.data_ptr(), codes.data_ptr(),
+                                                    sp)),
+            ("sideband", lambda: ctx.encode_sideband(field.data_ptr(), nch, pnx, pny, w.pp, w.pp, oph.SSB_TOP,
+                                                     enc_vals.data_ptr(), codes.data_ptr(), sp))):
         fn()
         ts = timed(fn, 10)
         encoders[name] = {"ms": 1e3 * sum(ts) / len(ts)}
     encoders["pixels"] = nch * npx
     encoders["note"] = ("phase_values: FP64 (atan2(im, re) + pi) / (2 pi) per pixel, 16 B read and 8 B written; "
                         "normalize: min/max and codes of 8 B values; phase_codes_only: the single-pass FP32-estimate "
-                        "codes kernel")
+                        "codes kernel; ssb (encodeHologram, two shifted FP64 transforms per channel), off_axis_ssb "
+                        "(SSB_LEFT: four transforms of channel 0) and sideband (SSB_TOP: one transform per channel), "
+                        "each with its 8-bit codes")
 
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 1995.0

@@ -105,42 +105,72 @@ __global__ void ssb_crop_kernel(const double2* __restrict__ in, double2* __restr
     out[i] = (x >= x1 && x <= x2 && y >= y1 && y <= y2) ? in[i] : make_double2(0.0, 0.0);
 }
 
-// encodeSideBand_CPU's carrier and real part (one channel); t is the
-// unnormalised inverse transform, divided by n here as fft2's bNormalized
-// does.
-__global__ void ssb_fringe_kernel(const double2* __restrict__ t, double* __restrict__ enc, int pnx, int pny,
-                                  double ppx, double ppy, int passband) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
-    if (c >= pnx) return;
-    const double n = (double)((int64_t)pnx * pny);
+// encodeSideBand_CPU's carrier angle theta of one row (SSB_TOP / _BOTTOM)
+// or column (SSB_LEFT / _RIGHT), k < the axis length: cs[k] = (cos, sin),
+// evaluated once per row or column instead of at every pixel (the same
+// values; FP64 sin and cos are costly on GB300's narrow FP64 pipe).
+__global__ void ssb_carrier_kernel(double2* __restrict__ cs, int pnx, int pny, double ppx, double ppy, int passband) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool rows = passband == OPHPC_SSB_TOP || passband == OPHPC_SSB_BOTTOM;
+    if (k >= (rows ? pny : pnx)) return;
     const double two_pi = 2 * kPiSsb;
     double theta;
-    if (passband == OPHPC_SSB_TOP || passband == OPHPC_SSB_BOTTOM) {
+    if (rows) {
         const double ssy = __dmul_rn((double)pny, ppy);
-        const double yy = __dsub_rn(__dsub_rn(ssy / 2.0, __dmul_rn(ppy, (double)r)), ppy);
+        const double yy = __dsub_rn(__dsub_rn(ssy / 2.0, __dmul_rn(ppy, (double)k)), ppy);
         theta = __dmul_rn(two_pi, __ddiv_rn(passband == OPHPC_SSB_TOP ? yy : -yy, __dmul_rn(4.0, ppy)));
     } else {
         const double ssx = __dmul_rn((double)pnx, ppx);
-        const double xx = __dsub_rn(__dsub_rn(-ssx / 2.0, __dmul_rn(ppx, (double)c)), ppx);
+        const double xx = __dsub_rn(__dsub_rn(-ssx / 2.0, __dmul_rn(ppx, (double)k)), ppx);
         theta = __dmul_rn(two_pi, __ddiv_rn(passband == OPHPC_SSB_LEFT ? -xx : xx, __dmul_rn(4.0, ppx)));
     }
+    cs[k] = make_double2(cos(theta), sin(theta));
+}
+
+// encodeSideBand_CPU's carrier and real part (one channel); t is the
+// unnormalised inverse transform, divided by n here as fft2's bNormalized
+// does; cs from ssb_carrier_kernel.
+__global__ void ssb_fringe_kernel(const double2* __restrict__ t, double* __restrict__ enc, int pnx, int pny,
+                                  const double2* __restrict__ cs, int passband) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (c >= pnx) return;
+    const double n = (double)((int64_t)pnx * pny);
+    const double2 ct = cs[(passband == OPHPC_SSB_TOP || passband == OPHPC_SSB_BOTTOM) ? r : c];
     const int64_t i = (int64_t)r * pnx + c;
     const double2 v = t[i];
     const double re = __ddiv_rn(v.x, n), im = __ddiv_rn(v.y, n);
-    enc[i] = __dsub_rn(__dmul_rn(re, cos(theta)), __dmul_rn(im, sin(theta)));
+    enc[i] = __dsub_rn(__dmul_rn(re, ct.x), __dmul_rn(im, ct.y));
 }
 
-// encodeHologram's shifted real part into enc (one channel).
+// cos and sin of encodeHologram's X for every column (cs[0, pnx)) and Y for
+// every row (cs[pnx, pnx + pny)), once each instead of at every pixel (the
+// same values).
+__global__ void ssb_axis_kernel(double2* __restrict__ cs, int pnx, int pny, double ppx, double ppy, double shift_x,
+                                double shift_y) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= pnx + pny) return;
+    double a;
+    if (k < pnx) {
+        const double ssx = __dmul_rn((double)pnx, ppx);
+        const double x = __dadd_rn(__dadd_rn(-(ssx / 2), __dmul_rn(ppx, (double)k)), ppx / 2);
+        a = __ddiv_rn(__dmul_rn(__dmul_rn(kPiSsb, x), shift_x), ppx);
+    } else {
+        const double ssy = __dmul_rn((double)pny, ppy);
+        const double y = __dsub_rn(__dsub_rn(ssy, ppy), __dmul_rn(ppy, (double)(k - pnx)));
+        a = __ddiv_rn(__dmul_rn(__dmul_rn(kPiSsb, y), shift_y), ppy);
+    }
+    cs[k] = make_double2(cos(a), sin(a));
+}
+
+// encodeHologram's shifted real part into enc (one channel): with X of the
+// column and Y of the row (cs from ssb_axis_kernel),
+// Re(T) (cos X cos Y - sin X sin Y).
 __global__ void ssb_point_cloud_kernel(const double2* __restrict__ t, double* __restrict__ enc, int pnx, int pny,
-                                       double ppx, double ppy, double shift_x, double shift_y) {
+                                       const double2* __restrict__ cs) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x, h = blockIdx.y;
     if (w >= pnx) return;
-    const double ssx = __dmul_rn((double)pnx, ppx), ssy = __dmul_rn((double)pny, ppy);
-    const double y = __dsub_rn(__dsub_rn(ssy, ppy), __dmul_rn(ppy, (double)h));
-    const double Y = __ddiv_rn(__dmul_rn(__dmul_rn(kPiSsb, y), shift_y), ppy);
-    const double x = __dadd_rn(__dadd_rn(-(ssx / 2), __dmul_rn(ppx, (double)w)), ppx / 2);
-    const double X = __ddiv_rn(__dmul_rn(__dmul_rn(kPiSsb, x), shift_x), ppx);
-    const double c = __dsub_rn(__dmul_rn(cos(X), cos(Y)), __dmul_rn(sin(X), sin(Y)));
+    const double2 cx = cs[w], cy = cs[pnx + h];
+    const double c = __dsub_rn(__dmul_rn(cx.x, cy.x), __dmul_rn(cx.y, cy.y));
     const int64_t i = (int64_t)h * pnx + w;
     const double2 v = t[i];
     // (T * (c, 0)).real()
@@ -231,9 +261,10 @@ ophpc_status ssb_encode_device(cudaMemPool_t pool, const double2* d_field, int n
     const size_t tw_bytes = align_ssb(sizeof(double2) * (size_t)(fft_twiddle_count(pnx) + fft_twiddle_count(pny)));
     const size_t enc_bytes = d_encoded ? 0 : align_ssb(sizeof(double) * (size_t)n * n_channels);
     const size_t re_bytes = align_ssb(sizeof(double) * (size_t)n);
+    const size_t cs_bytes = align_ssb(sizeof(double2) * (size_t)(pnx + pny));
     unsigned char* mem = nullptr;
-    if (cudaMallocFromPoolAsync((void**)&mem, 4 * plane + tw_bytes + enc_bytes + re_bytes + 256, pool, s) !=
-        cudaSuccess) {
+    if (cudaMallocFromPoolAsync((void**)&mem, 4 * plane + tw_bytes + enc_bytes + re_bytes + cs_bytes + 256, pool,
+                                s) != cudaSuccess) {
         if (err) *err = "SSB scratch allocation failed";
         return OPHPC_ERROR_OUT_OF_MEMORY;
     }
@@ -243,7 +274,8 @@ ophpc_status ssb_encode_device(cudaMemPool_t pool, const double2* d_field, int n
     double2* tw = (double2*)(mem + 4 * plane);
     double* enc = d_encoded ? d_encoded : (double*)(mem + 4 * plane + tw_bytes);
     double* re = (double*)(mem + 4 * plane + tw_bytes + enc_bytes);
-    unsigned long long* mm = (unsigned long long*)(mem + 4 * plane + tw_bytes + enc_bytes + re_bytes);
+    double2* cs = (double2*)(mem + 4 * plane + tw_bytes + enc_bytes + re_bytes);
+    unsigned long long* mm = (unsigned long long*)(mem + 4 * plane + tw_bytes + enc_bytes + re_bytes + cs_bytes);
     FftPlan plan_x, plan_y;
     fft_plan_init(&plan_x, pnx, tw, s);
     fft_plan_init(&plan_y, pny, tw + fft_twiddle_count(pnx), s);
@@ -260,24 +292,29 @@ ophpc_status ssb_encode_device(cudaMemPool_t pool, const double2* d_field, int n
             x1 = h - h / 2 - 1;
             x2 = x1 + h - 1;
         }
+        const int axis = (passband == OPHPC_SSB_TOP || passband == OPHPC_SSB_BOTTOM) ? pny : pnx;
+        count_launches(1);
+        ssb_carrier_kernel<<<(unsigned)((axis + 255) / 256), 256, 0, s>>>(cs, pnx, pny, ppx, ppy, (int)passband);
         for (int c = 0; c < n_channels && e == cudaSuccess; ++c) {
             count_launches(1);
             ssb_crop_kernel<<<g2, 256, 0, s>>>(d_field + (int64_t)c * n, w2, pnx, pny, x1, x2, y1, y2);
             e = shifted_fft2(w2, w2, buf, plan_x, plan_y, pnx, pny, true, s);
             if (e == cudaSuccess) {
                 count_launches(1);
-                ssb_fringe_kernel<<<g2, 256, 0, s>>>(w2, enc + (int64_t)c * n, pnx, pny, ppx, ppy, (int)passband);
+                ssb_fringe_kernel<<<g2, 256, 0, s>>>(w2, enc + (int64_t)c * n, pnx, pny, cs, (int)passband);
                 e = cudaGetLastError();
             }
         }
     } else if (encode_flag == OPHPC_ENCODE_SSB) {
+        count_launches(1);
+        ssb_axis_kernel<<<(unsigned)((pnx + pny + 255) / 256), 256, 0, s>>>(cs, pnx, pny, ppx, ppy, shift_x, shift_y);
         for (int c = 0; c < n_channels && e == cudaSuccess; ++c) {
             e = shifted_fft2(d_field + (int64_t)c * n, w2, buf, plan_x, plan_y, pnx, pny, false, s);
             if (e == cudaSuccess) e = shifted_fft2(w2, w2, buf, plan_x, plan_y, pnx, pny, true, s);
             if (e == cudaSuccess) {
                 count_launches(1);
                 ssb_point_cloud_kernel<<<dim3((unsigned)((pnx + 255) / 256), (unsigned)pny), 256, 0, s>>>(
-                    w2, enc + (int64_t)c * n, pnx, pny, ppx, ppy, shift_x, shift_y);
+                    w2, enc + (int64_t)c * n, pnx, pny, cs);
                 e = cudaGetLastError();
             }
         }
